@@ -1,0 +1,116 @@
+// Internal structures shared by the host planner (planner.cpp) and the
+// sm_103a kernels (kernels.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fftj {
+
+// q = n / d for 0 <= n < 2^31 by multiply-high and shift (d = 1: q = n).
+struct FastDiv {
+  uint32_t d = 1, mul = 0, shr = 0;
+  FastDiv() {}
+  explicit FastDiv(uint32_t div) : d(div) {
+    if (div <= 1) { d = 1; mul = 0; shr = 0; return; }
+    uint32_t l = 0;
+    while ((1ull << l) < div) ++l;  // ceil(log2 d)
+    uint32_t p = 31 + l;
+    unsigned long long m = ((1ull << p) + div - 1) / div;  // ceil(2^p / d)
+    mul = (uint32_t)m;
+    shr = p - 32;
+  }
+#ifdef __CUDACC__
+  __host__ __device__ __forceinline__ uint32_t div(uint32_t n) const {
+#ifdef __CUDA_ARCH__
+    return d == 1 ? n : (__umulhi(n, mul) >> shr);
+#else
+    return n / d;
+#endif
+  }
+#endif
+};
+
+constexpr int kMaxSub = 12;
+
+// One radix sub-stage inside a pass: Stockham stage of radix r on the
+// pass's R-point sub-transforms at current length L = R / S.
+struct SubStage {
+  int r;
+  int S;         // stride R / L (product of the earlier sub-radices)
+  FastDiv fS;    // divide by S
+  int Rr;        // R / r
+};
+
+enum LoadOp : int {
+  LOAD_PLAIN = 0,     // complex x[b*idist + g]
+  LOAD_DECONV = 1,    // resampling: deconvolve and zero-pad n -> m
+  LOAD_C2R_PRE = 2,   // irfft even pre-pass Z[k] from X[k], conj X[h-k]
+  LOAD_REAL = 3,      // real x -> (x, 0)
+};
+
+// Parameters of one Stockham super-radix pass over the data: radix-R
+// butterflies (R points each, an R-point DFT done in shared memory),
+// reading x[s*p + j*m*s + q] and writing y[R*s*p + j*s + q] * w_ncur^(p*j).
+struct PassParams {
+  int R;
+  int nsub;
+  SubStage sub[kMaxSub];
+  // tile: NBt batches x P butterflies p x Q lanes q, NB = NBt*P*Q columns
+  int P, Q, NBt, NB;
+  FastDiv fQ, fP, fR, fNB;
+  int64_t m, s, ncur;
+  int64_t in_bstride, out_bstride, nbatch;
+  uint32_t tiles_q, tiles_p, tiles_b;
+  FastDiv ftq, ftp;
+  // outer twiddle: 0 none, 1 full table tw[p*R + j], 2 two-level hi/lo
+  int tw_mode;
+  int tw_shift;            // K = 1 << tw_shift for two-level
+  const void* tw_full;
+  const void* tw_hi;
+  const void* tw_lo;
+  const void* twR;         // w_R^t, t < R (inner twiddles, sign of the pass)
+  double scale;            // applied on store when != 1
+  int smem_elems;          // padded elements per buffer
+  int threads;
+  // fused load op parameters
+  int load_op;
+  int64_t ld_n, ld_m, ld_hp;     // DECONV: n, m, ceil(n/2); C2R_PRE: h = ld_n
+  int64_t ld_stride;             // input batch stride of the raw input
+  const void* ld_tab;            // DECONV: corr[n]; C2R_PRE: w[h]
+  double ld_pre;                 // C2R_PRE pair factor (1/2 or 1)
+};
+
+// Resampling interpolation: y[b*ody + k] = sum_i wt[k*w+i] g[b*m + (l0[k]+i) mod m]
+struct InterpParams {
+  int64_t n, m, w, nbatch;
+  int64_t g_bstride, y_bstride;
+  const void* wt;
+  const int32_t* l0;
+};
+
+// rfft even post-pass: Y[k] (k = 0..h) from Z (length h) per batch.
+struct RealPostParams {
+  int64_t h, nbatch, z_bstride, y_bstride;
+  const void* tw;  // e^{-2 pi i k/n}, k = 0..h
+};
+
+// Generic elementwise helpers for odd-length real transforms.
+struct CopyParams {
+  int64_t n, nbatch, in_bstride, out_bstride;
+  int mode;  // 0: real -> complex, 1: hermitian expand (n real), 2: complex -> real, 3: truncate h+1
+  int64_t nc;  // complex length per batch (mode 1/3)
+};
+
+template <typename T>
+cudaError_t launch_pass(const PassParams& pp, int dir, const void* in, void* out, cudaStream_t st);
+template <typename T>
+cudaError_t launch_interp(const InterpParams& ip, const void* g, void* y, cudaStream_t st);
+template <typename T>
+cudaError_t launch_real_post(const RealPostParams& rp, const void* z, void* y, cudaStream_t st);
+template <typename T>
+cudaError_t launch_copy(const CopyParams& cp, const void* in, void* out, cudaStream_t st);
+// Opt a pass configuration into the dynamic shared memory it needs.
+template <typename T>
+cudaError_t prepare_pass(const PassParams& pp, int dir);
+
+}  // namespace fftj

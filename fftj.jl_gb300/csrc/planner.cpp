@@ -1,0 +1,902 @@
+// Host planner and C ABI of the GB300 FFTJ transform library.
+//
+// The planner restates FFTJ's plan-time work for the GPU: factorization over
+// {2, 3, 5, 7, 11, 13} (src/plan.jl:16-45), twiddle tables from FP64
+// sincospi with exact angle reduction (src/plan.jl:66-95), the resampling
+// parameters and weights of src/resample.jl:9-256, and the real-edge twiddles
+// of src/real.jl:26-39. Instead of FFTJ's radix-4/8 stage chain and its
+// cache-driven routing between direct chains and four-step, a transform of
+// length N is split into the fewest HBM passes whose per-pass radix fits one
+// CTA tile (a pass = one Stockham stage of radix R_i, its R_i-point DFT done
+// in shared memory by radix-2..16 sub-stages).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/fftj.h"
+#include "fftj_internal.h"
+
+using namespace fftj;
+typedef int64_t i64;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+// sin(pi x), cos(pi x) with exact reduction of x to [0, 1/4].
+void sincospi(double x, double* s, double* c) {
+  double sg = 1.0;
+  if (x < 0) { x = -x; sg = -1.0; }
+  double r = std::fmod(x, 2.0);
+  double ss = 1.0, cs = 1.0;
+  if (r >= 1.0) { r -= 1.0; ss = -ss; cs = -cs; }
+  bool swap = false;
+  if (r > 0.5) { r = 1.0 - r; cs = -cs; }
+  if (r > 0.25) { r = 0.5 - r; swap = true; }
+  double a = M_PI * r;
+  double sv = std::sin(a), cv = std::cos(a);
+  if (swap) std::swap(sv, cv);
+  *s = sg * ss * sv;
+  *c = cs * cv;
+}
+// w_n^e = exp(dir * 2 pi i e / n), exact integer reduction of e mod n
+void omega(i64 e, i64 n, int dir, double* re, double* im) {
+  i64 r = e % n;
+  if (r < 0) r += n;
+  double s, c;
+  // angle in units of pi: 2 r / n, reduced so that 2r/n in [0, 2)
+  sincospi((double)(2 * r) / (double)n, &s, &c);
+  *re = c;
+  *im = dir * s;
+}
+
+bool smooth13(i64 n, std::vector<int>* primes) {
+  if (n < 1) return false;
+  std::vector<int> ps;
+  for (int p : {2, 3, 5, 7, 11, 13})
+    while (n % p == 0) { n /= p; ps.push_back(p); }
+  if (primes) *primes = ps;
+  return n == 1;
+}
+
+// ---- resampling parameters (FFTJ src/resample.jl) -------------------------
+const int SMOOTH_ODD[7] = {1, 3, 5, 7, 9, 15, 21};
+int top_set_bit(i64 x) { return x <= 0 ? 0 : 64 - __builtin_clzll((unsigned long long)x); }
+i64 nextsmooth(i64 N) {  // src/resample.jl:13-21
+  i64 best = INT64_MAX;
+  for (int o : SMOOTH_ODD) {
+    int k = std::max(6, top_set_bit((N + o - 1) / o - 1));
+    i64 c = (i64)o << k;
+    if (c < best) best = c;
+  }
+  return best;
+}
+void gausslegendre(int nq, std::vector<double>& z, std::vector<double>& wq) {  // src/resample.jl:33-53
+  z.assign(nq, 0);
+  wq.assign(nq, 0);
+  const double eps = 2.220446049250313e-16;
+  for (int i = 1; i <= nq; ++i) {
+    double s, x;
+    sincospi((i - 0.25) / (nq + 0.5), &s, &x);
+    double dp = 1;
+    for (int it = 0; it < 20; ++it) {
+      double p0 = 1, p1 = x;
+      for (int k = 2; k <= nq; ++k) {
+        double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = nq * (x * p1 - p0) / (x * x - 1);
+      double dx = p1 / dp;
+      x -= dx;
+      if (std::fabs(dx) < 4 * eps) break;
+    }
+    z[i - 1] = x;
+    wq[i - 1] = 2 / ((1 - x * x) * dp * dp);
+  }
+}
+double es_kernel(double z, double beta) {  // src/resample.jl:55
+  return std::fabs(z) >= 1 ? 0.0 : std::exp(beta * (std::sqrt(1 - z * z) - 1));
+}
+
+struct Resample {
+  i64 n, m, w, h;
+  double beta;
+  std::vector<double> corr;  // scale / (w Phi(j'/m))
+  std::vector<double> wt;    // n*w weights
+  std::vector<int32_t> l0;   // first grid index per output (unwrapped)
+};
+// _resample_parts with table weights (src/resample.jl:202-256)
+Resample resample_parts(i64 n, bool f64, double scale) {
+  Resample r;
+  r.n = n;
+  const double epsT = f64 ? 2.220446049250313e-16 : 1.1920928955078125e-07;
+  const double tol = 10 * epsT;
+  r.m = nextsmooth((i64)std::ceil(2.0 * n));
+  const double ratio = std::max((double)n / r.m, 0.5);
+  i64 wc = (i64)std::ceil(std::log(1 / tol) / (M_PI * std::sqrt(1 - ratio)));
+  r.w = 4 * ((wc + 3) / 4);
+  r.beta = 0.97 * M_PI * r.w * (1 - (double)n / (2.0 * r.m));
+  r.h = r.w / 2;
+  std::vector<double> zq, wq;
+  gausslegendre((int)(2 * r.w + 20), zq, wq);
+  r.corr.resize(n);
+  const i64 hp = (n + 1) / 2;
+  for (i64 j = 0; j < n; ++j) {
+    const i64 jp = j < hp ? j : j - n;
+    const double nu = (double)jp / r.m;
+    double Phi = 0;
+    for (size_t q = 0; q < zq.size(); ++q) {
+      if (!(zq[q] > 0)) continue;
+      double s, c;
+      sincospi(nu * r.w * zq[q], &s, &c);
+      Phi += wq[q] * es_kernel(zq[q], r.beta) * c;
+    }
+    r.corr[j] = scale / (r.w * Phi);
+  }
+  r.wt.resize(n * r.w);
+  r.l0.resize(n);
+  for (i64 k = 0; k < n; ++k) {
+    const __int128 km = (__int128)k * r.m;
+    const i64 q = (i64)(km / n), rr = (i64)(km % n);
+    r.l0[k] = (int32_t)(q - r.h + 1);
+    const double delta = (double)rr / n;
+    for (i64 i = 0; i < r.w; ++i) r.wt[k * r.w + i] = es_kernel((delta + r.h - 1 - i) / r.h, r.beta);
+  }
+  return r;
+}
+
+// ---- pass decomposition ----------------------------------------------------
+struct DtypeCfg {
+  int esize;        // bytes per complex element
+  int tile_max;     // elements per CTA tile (one shared buffer)
+  int threads_max;  // CTA size bound of the kernel
+  int rmax_multi;   // largest per-pass radix when more than one pass
+  int min_run;      // minimum contiguous elements per tile row (coalescing)
+};
+DtypeCfg dtype_cfg(bool f64) {
+  if (f64) return DtypeCfg{16, 4096, 256, 1024, 4};
+  return DtypeCfg{8, 8192, 512, 1024, 8};
+}
+
+// split the prime multiset into k bins with every bin <= rmax (LPT on logs)
+bool split_bins(const std::vector<int>& primes, int k, i64 rmax, std::vector<i64>* bins) {
+  std::vector<int> ps(primes);
+  std::sort(ps.rbegin(), ps.rend());
+  std::vector<i64> b(k, 1);
+  for (int p : ps) {
+    int best = 0;
+    for (int i = 1; i < k; ++i)
+      if (b[i] < b[best]) best = i;
+    b[best] *= p;
+  }
+  for (i64 v : b)
+    if (v > rmax) return false;
+  std::sort(b.rbegin(), b.rend());
+  *bins = b;
+  return true;
+}
+
+// Passes of a length-n axis: one pass when the whole transform fits a tile
+// and the axis is contiguous; otherwise the fewest passes whose radices keep
+// >= min_run contiguous elements per tile row.
+std::vector<i64> pass_radices(i64 n, const DtypeCfg& cfg, bool strided) {
+  std::vector<int> primes;
+  smooth13(n, &primes);
+  if (!strided && n <= cfg.tile_max) return {n};
+  if (n <= cfg.rmax_multi) return {n};
+  for (int k = 1; k < 16; ++k) {
+    std::vector<i64> bins;
+    if (split_bins(primes, k, cfg.rmax_multi, &bins)) return bins;
+  }
+  return {};
+}
+
+// sub-radix sequence of one pass: odd primes first, then the power-of-two
+// part as balanced radix-16/8/4/2 sub-stages
+std::vector<int> sub_radices(i64 R) {
+  std::vector<int> out;
+  i64 r = R;
+  int a = 0;
+  while (r % 2 == 0) { r /= 2; a++; }
+  for (int p : {3, 5, 7, 11, 13})
+    while (r % p == 0) { r /= p; out.push_back(p); }
+  if (a > 0) {
+    int k = (a + 3) / 4;
+    int base = a / k, extra = a % k;
+    for (int i = 0; i < k; ++i) out.push_back(1 << (base + (i < extra ? 1 : 0)));
+  }
+  if (out.empty()) out.push_back(1);
+  return out;
+}
+
+i64 largest_divisor_le(i64 n, i64 cap) {
+  if (cap >= n) return n;
+  for (i64 d = std::max<i64>(cap, 1); d >= 1; --d)
+    if (n % d == 0) return d;
+  return 1;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+enum OpKind { OP_PASS = 0, OP_INTERP = 1, OP_RPOST = 2, OP_COPY = 3 };
+enum BufId { B_IN = 0, B_OUT = 1, B_W0 = 2, B_W1 = 3 };
+
+struct Op {
+  OpKind kind;
+  int src, dst;
+  int dir = -1;
+  PassParams pp;
+  InterpParams ip;
+  RealPostParams rp;
+  CopyParams cp;
+  size_t dst_bytes = 0;  // bytes written (for workspace sizing)
+};
+
+struct fftj_plan_s {
+  int dtype = 0;
+  int kind = 0;  // 0 c2c, 1 r2c, 2 c2r
+  int route = FFTJ_ROUTE_DIRECT;
+  std::vector<i64> dims;
+  i64 n = 1, batch = 1;
+  i64 resample_m = 0, resample_w = 0;
+  std::vector<Op> ops;
+  std::vector<DevBuf> tables;
+  DevBuf ws[2];
+  size_t table_bytes = 0;
+  bool inplace_safe = false;
+  int npasses = 0;
+  std::vector<int> pass_R;
+  ~fftj_plan_s() {
+    for (auto& t : tables)
+      if (t.p) cudaFree(t.p);
+    for (auto& w : ws)
+      if (w.p) cudaFree(w.p);
+  }
+};
+
+namespace {
+
+// upload a table of complex values (re, im pairs in double) as T
+template <typename T>
+const void* upload_cplx(fftj_plan_s* P, const std::vector<double>& ri) {
+  std::vector<T> h(ri.size());
+  for (size_t i = 0; i < ri.size(); ++i) h[i] = (T)ri[i];
+  DevBuf b;
+  b.bytes = h.size() * sizeof(T);
+  if (cudaMalloc(&b.p, std::max<size_t>(b.bytes, 16)) != cudaSuccess) return nullptr;
+  if (cudaMemcpy(b.p, h.data(), b.bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(b.p);
+    return nullptr;
+  }
+  P->tables.push_back(b);
+  P->table_bytes += b.bytes;
+  return b.p;
+}
+const void* upload_raw(fftj_plan_s* P, const void* data, size_t bytes) {
+  DevBuf b;
+  b.bytes = bytes;
+  if (cudaMalloc(&b.p, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+  if (cudaMemcpy(b.p, data, bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(b.p);
+    return nullptr;
+  }
+  P->tables.push_back(b);
+  P->table_bytes += bytes;
+  return b.p;
+}
+
+// the complex table w_n^e for e in [0, count), sign dir
+template <typename T>
+const void* omega_table(fftj_plan_s* P, i64 n, i64 count, i64 stride, int dir) {
+  std::vector<double> ri(2 * count);
+  for (i64 e = 0; e < count; ++e) omega(e * stride, n, dir, &ri[2 * e], &ri[2 * e + 1]);
+  return upload_cplx<T>(P, ri);
+}
+
+// Build the passes of a length-n transform along an axis with inner stride
+// Bi (elements between consecutive points of one transform... folded into s)
+// for nbatch independent blocks at batch strides ibs/obs. The first pass may
+// use a fused load op (filled in by the caller).
+template <typename T>
+int build_axis_passes(fftj_plan_s* P, i64 n, i64 Bi, i64 nbatch, i64 ibs, i64 obs, int dir, double scale,
+                      std::vector<Op>* out_ops) {
+  const bool f64 = sizeof(T) == 8;
+  const DtypeCfg cfg = dtype_cfg(f64);
+  std::vector<i64> Rs = pass_radices(n, cfg, Bi > 1);
+  if (Rs.empty()) return fail(FFTJ_ERR_UNSUPPORTED, "no pass decomposition for length " + std::to_string(n));
+  i64 s1 = 1;  // 1-D stride before this pass
+  i64 ncur = n;
+  for (size_t pi = 0; pi < Rs.size(); ++pi) {
+    const i64 R = Rs[pi];
+    Op op;
+    op.kind = OP_PASS;
+    op.dir = dir;
+    PassParams& pp = op.pp;
+    std::memset(&pp, 0, sizeof(pp));
+    pp.R = (int)R;
+    std::vector<int> subs = sub_radices(R);
+    if ((int)subs.size() > kMaxSub) return fail(FFTJ_ERR_UNSUPPORTED, "too many sub-stages");
+    pp.nsub = 0;
+    i64 S = 1;
+    for (int r : subs) {
+      if (r == 1) continue;
+      SubStage& ss = pp.sub[pp.nsub++];
+      ss.r = r;
+      ss.S = (int)S;
+      ss.fS = FastDiv((uint32_t)S);
+      ss.Rr = (int)(R / r);
+      S *= r;
+    }
+    const i64 m = ncur / R;
+    const i64 s = s1 * Bi;  // effective stride
+    pp.m = m;
+    pp.s = s;
+    pp.ncur = ncur;
+    pp.in_bstride = ibs;
+    pp.out_bstride = obs;
+    pp.nbatch = nbatch;
+    // tile: columns (batch, p, q)
+    const i64 tmax = std::max<i64>(cfg.tile_max, R);
+    const i64 cols = std::max<i64>(1, tmax / R);
+    i64 Pt = 1, Qt = 1, NBt = 1;
+    if (s == 1) {
+      Pt = largest_divisor_le(m, cols);
+      if (Pt == m) NBt = std::max<i64>(1, cols / m);
+    } else {
+      Qt = largest_divisor_le(s, cols);
+      if (Qt == s) {
+        Pt = largest_divisor_le(m, cols / Qt);
+        if (Pt == m) NBt = std::max<i64>(1, cols / (m * s));
+      }
+    }
+    NBt = std::min(NBt, nbatch);
+    pp.P = (int)Pt;
+    pp.Q = (int)Qt;
+    pp.NBt = (int)NBt;
+    pp.NB = (int)(Pt * Qt * NBt);
+    pp.fQ = FastDiv((uint32_t)Qt);
+    pp.fP = FastDiv((uint32_t)Pt);
+    pp.fR = FastDiv((uint32_t)R);
+    pp.fNB = FastDiv((uint32_t)pp.NB);
+    pp.tiles_q = (uint32_t)(s / Qt);
+    pp.tiles_p = (uint32_t)(m / Pt);
+    pp.tiles_b = (uint32_t)((nbatch + NBt - 1) / NBt);
+    pp.ftq = FastDiv(pp.tiles_q);
+    pp.ftp = FastDiv(pp.tiles_p);
+    const double ntiles = (double)pp.tiles_q * pp.tiles_p * pp.tiles_b;
+    if (ntiles >= 2147483647.0) return fail(FFTJ_ERR_UNSUPPORTED, "grid too large");
+    const i64 E = (i64)pp.NB * R;
+    // threads: enough that each sub-stage's butterflies fit IPT(r) per thread
+    i64 th = 32;
+    for (int i = 0; i < pp.nsub; ++i) {
+      const int r = pp.sub[i].r;
+      const int ipt = std::max(1, 16 / r);
+      const i64 need = (E / r + ipt - 1) / ipt;
+      th = std::max(th, need);
+    }
+    th = std::max<i64>(th, std::min<i64>(E, 128));
+    th = (th + 31) / 32 * 32;
+    if (th > cfg.threads_max) return fail(FFTJ_ERR_UNSUPPORTED, "tile needs too many threads");
+    pp.threads = (int)th;
+    const int padsh = f64 ? 3 : 4;
+    pp.smem_elems = (int)(E + (E >> padsh) + 2);
+    // inner twiddles w_R^t
+    pp.twR = omega_table<T>(P, R, R, 1, dir);
+    if (!pp.twR) return fail(FFTJ_ERR_CUDA, "table upload failed");
+    // outer twiddles w_ncur^(p*j), p*j < ncur
+    if (m > 1) {
+      const i64 full_max = f64 ? (1 << 21) : (1 << 22);
+      if (ncur <= full_max) {
+        pp.tw_mode = 1;
+        pp.tw_full = omega_table<T>(P, ncur, ncur, 1, dir);
+        if (!pp.tw_full) return fail(FFTJ_ERR_CUDA, "table upload failed");
+      } else {
+        int sh = 0;
+        while (((i64)1 << (2 * sh)) < ncur) sh++;
+        const i64 K = (i64)1 << sh;
+        const i64 nh = (ncur + K - 1) / K;
+        pp.tw_mode = 2;
+        pp.tw_shift = sh;
+        pp.tw_hi = omega_table<T>(P, ncur, nh, K, dir);
+        pp.tw_lo = omega_table<T>(P, ncur, K, 1, dir);
+        if (!pp.tw_hi || !pp.tw_lo) return fail(FFTJ_ERR_CUDA, "table upload failed");
+      }
+    }
+    pp.scale = (pi + 1 == Rs.size()) ? scale : 1.0;
+    pp.load_op = LOAD_PLAIN;
+    if (prepare_pass<T>(pp, dir) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
+    op.dst_bytes = (size_t)(nbatch * obs) * sizeof(T) * 2;
+    out_ops->push_back(op);
+    P->pass_R.push_back((int)R);
+    s1 *= R;
+    ncur /= R;
+  }
+  return FFTJ_OK;
+}
+
+// Chain ops: first reads IN, last writes OUT, intermediates alternate W0/W1.
+void wire(std::vector<Op>& ops) {
+  const size_t k = ops.size();
+  for (size_t i = 0; i < k; ++i) {
+    ops[i].src = (i == 0) ? B_IN : ((i - 1) % 2 == 0 ? B_W0 : B_W1);
+    ops[i].dst = (i + 1 == k) ? B_OUT : (i % 2 == 0 ? B_W0 : B_W1);
+  }
+}
+
+int alloc_workspace(fftj_plan_s* P) {
+  size_t need[2] = {0, 0};
+  for (auto& op : P->ops) {
+    if (op.dst == B_W0) need[0] = std::max(need[0], op.dst_bytes);
+    if (op.dst == B_W1) need[1] = std::max(need[1], op.dst_bytes);
+  }
+  // one-op plans that are not in-place safe run through W0 when in == out
+  if (P->ops.size() == 1 && !P->inplace_safe) need[0] = std::max(need[0], P->ops[0].dst_bytes);
+  for (int i = 0; i < 2; ++i) {
+    if (need[i] == 0) continue;
+    P->ws[i].bytes = need[i];
+    if (cudaMalloc(&P->ws[i].p, need[i]) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "workspace allocation failed");
+  }
+  return FFTJ_OK;
+}
+
+// complex 1-D transform of length n (batch at idist/odist) appended to ops;
+// if load_op != PLAIN, the first pass uses it with the given parameters.
+template <typename T>
+int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir, double scale,
+                 std::vector<Op>* ops, int* route) {
+  std::vector<int> primes;
+  if (smooth13(n, &primes)) {
+    // intermediate passes use dense strides n
+    std::vector<Op> tmp;
+    int rc = build_axis_passes<T>(P, n, 1, batch, n, n, dir, scale, &tmp);
+    if (rc) return rc;
+    tmp.front().pp.in_bstride = idist;
+    tmp.back().pp.out_bstride = odist;
+    tmp.back().dst_bytes = (size_t)(batch * odist) * sizeof(T) * 2;
+    *route = tmp.size() > 1 ? FFTJ_ROUTE_FOURSTEP : FFTJ_ROUTE_DIRECT;
+    for (auto& o : tmp) ops->push_back(o);
+    return FFTJ_OK;
+  }
+  // non-smooth: resample onto m (src/resample.jl:258-276)
+  Resample rs = resample_parts(n, sizeof(T) == 8, scale);
+  P->resample_m = rs.m;
+  P->resample_w = rs.w;
+  std::vector<Op> tmp;
+  int rc = build_axis_passes<T>(P, rs.m, 1, batch, rs.m, rs.m, dir, 1.0, &tmp);
+  if (rc) return rc;
+  PassParams& f = tmp.front().pp;
+  f.load_op = LOAD_DECONV;
+  f.ld_n = n;
+  f.ld_m = rs.m;
+  f.ld_hp = (n + 1) / 2;
+  f.ld_stride = idist;
+  {
+    std::vector<T> c(n);
+    for (i64 j = 0; j < n; ++j) c[j] = (T)rs.corr[j];
+    f.ld_tab = upload_raw(P, c.data(), c.size() * sizeof(T));
+    if (!f.ld_tab) return fail(FFTJ_ERR_CUDA, "table upload failed");
+  }
+  if (prepare_pass<T>(f, dir) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
+  Op ip;
+  ip.kind = OP_INTERP;
+  ip.ip.n = n;
+  ip.ip.m = rs.m;
+  ip.ip.w = rs.w;
+  ip.ip.nbatch = batch;
+  ip.ip.g_bstride = rs.m;
+  ip.ip.y_bstride = odist;
+  {
+    std::vector<T> w(rs.wt.size());
+    for (size_t i = 0; i < w.size(); ++i) w[i] = (T)rs.wt[i];
+    ip.ip.wt = upload_raw(P, w.data(), w.size() * sizeof(T));
+    ip.ip.l0 = (const int32_t*)upload_raw(P, rs.l0.data(), rs.l0.size() * sizeof(int32_t));
+    if (!ip.ip.wt || !ip.ip.l0) return fail(FFTJ_ERR_CUDA, "table upload failed");
+  }
+  ip.dst_bytes = (size_t)(batch * odist) * sizeof(T) * 2;
+  for (auto& o : tmp) ops->push_back(o);
+  ops->push_back(ip);
+  *route = FFTJ_ROUTE_RESAMPLE;
+  return FFTJ_OK;
+}
+
+template <typename T>
+int plan_c2c_t(fftj_plan_s* P, const std::vector<i64>& dims, i64 batch, i64 idist, i64 odist, int dir,
+               double scale) {
+  const i64 len = P->n;
+  if (dims.size() == 1) {
+    int route = 0;
+    int rc = build_c2c_1d<T>(P, len, batch, idist, odist, dir, scale, &P->ops, &route);
+    if (rc) return rc;
+    P->route = route;
+  } else {
+    if (idist != len || odist != len)
+      return fail(FFTJ_ERR_UNSUPPORTED, "N-d plans need dense batches (idist = odist = prod(dims))");
+    P->route = FFTJ_ROUTE_ND;
+    // per-dim passes (src/ndplan.jl:57-118), dims of length 1 skipped
+    std::vector<size_t> active;
+    for (size_t d = 0; d < dims.size(); ++d)
+      if (dims[d] > 1) active.push_back(d);
+    for (size_t ai = 0; ai < active.size(); ++ai) {
+      const size_t d = active[ai];
+      const i64 nd = dims[d];
+      if (!smooth13(nd, nullptr))
+        return fail(FFTJ_ERR_UNSUPPORTED, "N-d plans with a non-smooth dimension are not supported yet");
+      i64 Bi = 1, Bo = 1;
+      for (size_t e = 0; e < d; ++e) Bi *= dims[e];
+      for (size_t e = d + 1; e < dims.size(); ++e) Bo *= dims[e];
+      const bool last = ai + 1 == active.size();
+      int rc = build_axis_passes<T>(P, nd, Bi, Bo * batch, Bi * nd, Bi * nd, dir, last ? scale : 1.0, &P->ops);
+      if (rc) return rc;
+    }
+    if (P->ops.empty()) {
+      // all dims 1: y = scale * x as a single radix-1 pass
+      return fail(FFTJ_ERR_UNSUPPORTED, "all dimensions have length 1");
+    }
+  }
+  return FFTJ_OK;
+}
+
+// rfft (src/real.jl:41-52, 80-142) along dim 1, batched over nb pencils
+template <typename T>
+int build_r2c_1d(fftj_plan_s* P, i64 n, i64 nb, i64 idist, i64 odist, std::vector<Op>* ops, int* route) {
+  const i64 h = n / 2;
+  if (n % 2 == 0 && idist % 2 == 0) {
+    std::vector<Op> inner;
+    int rc = build_c2c_1d<T>(P, h, nb, idist / 2, h, -1, 1.0, &inner, route);
+    if (rc) return rc;
+    Op post;
+    post.kind = OP_RPOST;
+    post.rp.h = h;
+    post.rp.nbatch = nb;
+    post.rp.z_bstride = h;
+    post.rp.y_bstride = odist;
+    std::vector<double> tw(2 * (h + 1));
+    for (i64 k = 0; k <= h; ++k) omega(k, n, -1, &tw[2 * k], &tw[2 * k + 1]);
+    post.rp.tw = upload_cplx<T>(P, tw);
+    if (!post.rp.tw) return fail(FFTJ_ERR_CUDA, "table upload failed");
+    post.dst_bytes = (size_t)(nb * odist) * sizeof(T) * 2;
+    for (auto& o : inner) ops->push_back(o);
+    ops->push_back(post);
+    return FFTJ_OK;
+  }
+  // odd n: full complex transform (src/real.jl:136-140)
+  Op cvt;
+  cvt.kind = OP_COPY;
+  cvt.cp.mode = 0;
+  cvt.cp.n = n;
+  cvt.cp.nbatch = nb;
+  cvt.cp.in_bstride = idist;
+  cvt.cp.out_bstride = n;
+  cvt.dst_bytes = (size_t)(nb * n) * sizeof(T) * 2;
+  ops->push_back(cvt);
+  std::vector<Op> inner;
+  int rc = build_c2c_1d<T>(P, n, nb, n, n, -1, 1.0, &inner, route);
+  if (rc) return rc;
+  for (auto& o : inner) ops->push_back(o);
+  Op tr;
+  tr.kind = OP_COPY;
+  tr.cp.mode = 3;
+  tr.cp.n = h + 1;
+  tr.cp.nbatch = nb;
+  tr.cp.in_bstride = n;
+  tr.cp.out_bstride = odist;
+  tr.dst_bytes = (size_t)(nb * odist) * sizeof(T) * 2;
+  ops->push_back(tr);
+  return FFTJ_OK;
+}
+
+// irfft / brfft (src/real.jl:57-73, 144-211) along dim 1, nb pencils
+template <typename T>
+int build_c2r_1d(fftj_plan_s* P, i64 n, i64 nb, i64 idist, i64 odist, bool normalized, double extra_scale,
+                 std::vector<Op>* ops, int* route) {
+  const i64 h = n / 2;
+  if (n % 2 == 0 && odist % 2 == 0) {
+    std::vector<Op> inner;
+    const double sc = (normalized ? 1.0 / (double)h : 1.0) * extra_scale;
+    int rc = build_c2c_1d<T>(P, h, nb, h, odist / 2, +1, sc, &inner, route);
+    if (rc) return rc;
+    std::vector<double> tw(2 * h);
+    for (i64 k = 0; k < h; ++k) omega(k, n, +1, &tw[2 * k], &tw[2 * k + 1]);
+    const void* twd = upload_cplx<T>(P, tw);
+    if (!twd) return fail(FFTJ_ERR_CUDA, "table upload failed");
+    PassParams& f = inner.front().pp;
+    if (inner.front().kind == OP_PASS && f.load_op == LOAD_PLAIN) {
+      f.load_op = LOAD_C2R_PRE;
+      f.ld_n = h;
+      f.ld_stride = idist;
+      f.ld_tab = twd;
+      f.ld_pre = normalized ? 0.5 : 1.0;
+      if (prepare_pass<T>(f, +1) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
+      for (auto& o : inner) ops->push_back(o);
+      return FFTJ_OK;
+    }
+    return fail(FFTJ_ERR_UNSUPPORTED, "irfft of a length whose half is not 13-smooth is not supported yet");
+  }
+  // odd n: Hermitian expansion, full complex inverse, real part
+  Op ex;
+  ex.kind = OP_COPY;
+  ex.cp.mode = 1;
+  ex.cp.n = n;
+  ex.cp.nc = h + 1;
+  ex.cp.nbatch = nb;
+  ex.cp.in_bstride = idist;
+  ex.cp.out_bstride = n;
+  ex.dst_bytes = (size_t)(nb * n) * sizeof(T) * 2;
+  ops->push_back(ex);
+  std::vector<Op> inner;
+  const double sc = (normalized ? 1.0 / (double)n : 1.0) * extra_scale;
+  int rc = build_c2c_1d<T>(P, n, nb, n, n, +1, sc, &inner, route);
+  if (rc) return rc;
+  for (auto& o : inner) ops->push_back(o);
+  Op re;
+  re.kind = OP_COPY;
+  re.cp.mode = 2;
+  re.cp.n = n;
+  re.cp.nbatch = nb;
+  re.cp.in_bstride = n;
+  re.cp.out_bstride = odist;
+  re.dst_bytes = (size_t)(nb * odist) * sizeof(T);
+  ops->push_back(re);
+  return FFTJ_OK;
+}
+
+template <typename T>
+int plan_r2c_t(fftj_plan_s* P, const std::vector<i64>& dims, i64 batch, i64 idist, i64 odist) {
+  const i64 n1 = dims[0];
+  const i64 h1p = n1 / 2 + 1;
+  i64 rest = 1;
+  for (size_t d = 1; d < dims.size(); ++d) rest *= dims[d];
+  int route = 0;
+  if (dims.size() == 1) {
+    int rc = build_r2c_1d<T>(P, n1, batch, idist, odist, &P->ops, &route);
+    if (rc) return rc;
+    P->route = route;
+    return FFTJ_OK;
+  }
+  if (idist != P->n || odist != h1p * rest)
+    return fail(FFTJ_ERR_UNSUPPORTED, "N-d real plans need dense batches");
+  P->route = FFTJ_ROUTE_ND;
+  // dim-1 real edge per pencil, then complex passes over dims 2..N
+  // (src/ndplan.jl:369-427)
+  int rc = build_r2c_1d<T>(P, n1, rest * batch, n1, h1p, &P->ops, &route);
+  if (rc) return rc;
+  std::vector<i64> cd(dims);
+  cd[0] = h1p;
+  for (size_t d = 1; d < dims.size(); ++d) {
+    if (dims[d] == 1) continue;
+    if (!smooth13(dims[d], nullptr)) return fail(FFTJ_ERR_UNSUPPORTED, "non-smooth N-d real dimension");
+    i64 Bi = 1, Bo = 1;
+    for (size_t e = 0; e < d; ++e) Bi *= cd[e];
+    for (size_t e = d + 1; e < cd.size(); ++e) Bo *= cd[e];
+    rc = build_axis_passes<T>(P, dims[d], Bi, Bo * batch, Bi * dims[d], Bi * dims[d], -1, 1.0, &P->ops);
+    if (rc) return rc;
+  }
+  return FFTJ_OK;
+}
+
+template <typename T>
+int plan_c2r_t(fftj_plan_s* P, const std::vector<i64>& dims, i64 batch, i64 idist, i64 odist, bool normalized) {
+  const i64 n1 = dims[0];
+  const i64 h1p = n1 / 2 + 1;
+  i64 rest = 1;
+  for (size_t d = 1; d < dims.size(); ++d) rest *= dims[d];
+  int route = 0;
+  if (dims.size() == 1) {
+    int rc = build_c2r_1d<T>(P, n1, batch, idist, odist, normalized, 1.0, &P->ops, &route);
+    if (rc) return rc;
+    P->route = route;
+    return FFTJ_OK;
+  }
+  if (odist != P->n || idist != h1p * rest)
+    return fail(FFTJ_ERR_UNSUPPORTED, "N-d real plans need dense batches");
+  P->route = FFTJ_ROUTE_ND;
+  // complex backward passes over dims 2..N, then the dim-1 real edge
+  // (src/ndplan.jl:455-519); normalization folded into the last op
+  std::vector<i64> cd(dims);
+  cd[0] = h1p;
+  for (size_t d = 1; d < dims.size(); ++d) {
+    if (dims[d] == 1) continue;
+    if (!smooth13(dims[d], nullptr)) return fail(FFTJ_ERR_UNSUPPORTED, "non-smooth N-d real dimension");
+    i64 Bi = 1, Bo = 1;
+    for (size_t e = 0; e < d; ++e) Bi *= cd[e];
+    for (size_t e = d + 1; e < cd.size(); ++e) Bo *= cd[e];
+    int rc = build_axis_passes<T>(P, dims[d], Bi, Bo * batch, Bi * dims[d], Bi * dims[d], +1, 1.0, &P->ops);
+    if (rc) return rc;
+  }
+  const double extra = normalized ? 1.0 / (double)rest : 1.0;
+  return build_c2r_1d<T>(P, n1, rest * batch, h1p, n1, normalized, extra, &P->ops, &route);
+}
+
+int check_dims(int rank, const int64_t* dims, std::vector<i64>* out) {
+  if (rank < 1 || !dims) return fail(FFTJ_ERR_ARG, "rank must be >= 1");
+  out->assign(dims, dims + rank);
+  for (i64 d : *out)
+    if (d < 1) return fail(FFTJ_ERR_ARG, "transform length must be positive (got " + std::to_string(d) + ")");
+  return FFTJ_OK;
+}
+
+int finish(fftj_plan_s* P, fftj_plan* out) {
+  wire(P->ops);
+  int rc = alloc_workspace(P);
+  if (rc) return rc;
+  P->npasses = (int)P->ops.size();
+  *out = P;
+  g_err.clear();
+  return FFTJ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fftj_plan_c2c(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch, int64_t idist,
+                  int64_t odist, int dir, double scale) {
+  if (!out) return fail(FFTJ_ERR_ARG, "null plan pointer");
+  *out = nullptr;
+  std::vector<i64> d;
+  if (int rc = check_dims(rank, dims, &d)) return rc;
+  if (dtype != FFTJ_F32 && dtype != FFTJ_F64) return fail(FFTJ_ERR_ARG, "dtype must be F32 or F64");
+  if (dir != -1 && dir != 1) return fail(FFTJ_ERR_ARG, "dir must be -1 or +1");
+  if (batch < 1) return fail(FFTJ_ERR_ARG, "batch must be >= 1");
+  std::unique_ptr<fftj_plan_s> P(new fftj_plan_s());
+  P->dtype = dtype;
+  P->kind = 0;
+  P->dims = d;
+  P->n = 1;
+  for (i64 v : d) P->n *= v;
+  P->batch = batch;
+  if (idist == 0) idist = P->n;
+  if (odist == 0) odist = P->n;
+  if (idist < P->n || odist < P->n) return fail(FFTJ_ERR_DIM, "idist/odist smaller than the transform");
+  int rc = dtype == FFTJ_F32 ? plan_c2c_t<float>(P.get(), d, batch, idist, odist, dir, scale)
+                             : plan_c2c_t<double>(P.get(), d, batch, idist, odist, dir, scale);
+  if (rc) return rc;
+  // a single pass over whole transforms (tile = full transforms) is in-place safe
+  P->inplace_safe = P->ops.size() == 1 && P->ops[0].kind == OP_PASS && P->ops[0].pp.m == 1 &&
+                    P->ops[0].pp.s == 1 && idist == odist;
+  rc = finish(P.get(), out);
+  if (rc) return rc;
+  P.release();
+  return FFTJ_OK;
+}
+
+int fftj_plan_r2c(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch, int64_t idist,
+                  int64_t odist) {
+  if (!out) return fail(FFTJ_ERR_ARG, "null plan pointer");
+  *out = nullptr;
+  std::vector<i64> d;
+  if (int rc = check_dims(rank, dims, &d)) return rc;
+  if (dtype != FFTJ_F32 && dtype != FFTJ_F64) return fail(FFTJ_ERR_ARG, "dtype must be F32 or F64");
+  if (batch < 1) return fail(FFTJ_ERR_ARG, "batch must be >= 1");
+  std::unique_ptr<fftj_plan_s> P(new fftj_plan_s());
+  P->dtype = dtype;
+  P->kind = 1;
+  P->dims = d;
+  P->n = 1;
+  for (i64 v : d) P->n *= v;
+  P->batch = batch;
+  const i64 cn = P->n / d[0] * (d[0] / 2 + 1);
+  if (idist == 0) idist = P->n;
+  if (odist == 0) odist = cn;
+  if (idist < P->n || odist < cn) return fail(FFTJ_ERR_DIM, "idist/odist smaller than the transform");
+  int rc = dtype == FFTJ_F32 ? plan_r2c_t<float>(P.get(), d, batch, idist, odist)
+                             : plan_r2c_t<double>(P.get(), d, batch, idist, odist);
+  if (rc) return rc;
+  rc = finish(P.get(), out);
+  if (rc) return rc;
+  P.release();
+  return FFTJ_OK;
+}
+
+int fftj_plan_c2r(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch, int64_t idist,
+                  int64_t odist, int normalized) {
+  if (!out) return fail(FFTJ_ERR_ARG, "null plan pointer");
+  *out = nullptr;
+  std::vector<i64> d;
+  if (int rc = check_dims(rank, dims, &d)) return rc;
+  if (dtype != FFTJ_F32 && dtype != FFTJ_F64) return fail(FFTJ_ERR_ARG, "dtype must be F32 or F64");
+  if (batch < 1) return fail(FFTJ_ERR_ARG, "batch must be >= 1");
+  std::unique_ptr<fftj_plan_s> P(new fftj_plan_s());
+  P->dtype = dtype;
+  P->kind = 2;
+  P->dims = d;
+  P->n = 1;
+  for (i64 v : d) P->n *= v;
+  P->batch = batch;
+  const i64 cn = P->n / d[0] * (d[0] / 2 + 1);
+  if (idist == 0) idist = cn;
+  if (odist == 0) odist = P->n;
+  if (idist < cn || odist < P->n) return fail(FFTJ_ERR_DIM, "idist/odist smaller than the transform");
+  int rc = dtype == FFTJ_F32 ? plan_c2r_t<float>(P.get(), d, batch, idist, odist, normalized != 0)
+                             : plan_c2r_t<double>(P.get(), d, batch, idist, odist, normalized != 0);
+  if (rc) return rc;
+  rc = finish(P.get(), out);
+  if (rc) return rc;
+  P.release();
+  return FFTJ_OK;
+}
+
+int fftj_execute(fftj_plan plan, const void* d_in, void* d_out, void* stream) {
+  if (!plan) return fail(FFTJ_ERR_ARG, "null plan");
+  if (!d_in || !d_out) return fail(FFTJ_ERR_ARG, "null data pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  fftj_plan_s* P = plan;
+  void* bufs[4] = {const_cast<void*>(d_in), d_out, P->ws[0].p, P->ws[1].p};
+  const bool via_ws = P->ops.size() == 1 && !P->inplace_safe && d_in == d_out;
+  for (size_t i = 0; i < P->ops.size(); ++i) {
+    const Op& op = P->ops[i];
+    const void* src = bufs[op.src];
+    void* dst = via_ws ? P->ws[0].p : bufs[op.dst];
+    cudaError_t e = cudaSuccess;
+    if (P->dtype == FFTJ_F32) {
+      switch (op.kind) {
+        case OP_PASS: e = launch_pass<float>(op.pp, op.dir, src, dst, st); break;
+        case OP_INTERP: e = launch_interp<float>(op.ip, src, dst, st); break;
+        case OP_RPOST: e = launch_real_post<float>(op.rp, src, dst, st); break;
+        case OP_COPY: e = launch_copy<float>(op.cp, src, dst, st); break;
+      }
+    } else {
+      switch (op.kind) {
+        case OP_PASS: e = launch_pass<double>(op.pp, op.dir, src, dst, st); break;
+        case OP_INTERP: e = launch_interp<double>(op.ip, src, dst, st); break;
+        case OP_RPOST: e = launch_real_post<double>(op.rp, src, dst, st); break;
+        case OP_COPY: e = launch_copy<double>(op.cp, src, dst, st); break;
+      }
+    }
+    if (e != cudaSuccess) return fail(FFTJ_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+  }
+  if (via_ws) {
+    cudaError_t e = cudaMemcpyAsync(d_out, P->ws[0].p, P->ops[0].dst_bytes, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return fail(FFTJ_ERR_CUDA, std::string("copy failed: ") + cudaGetErrorString(e));
+  }
+  g_err.clear();
+  return FFTJ_OK;
+}
+
+int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info) {
+  if (!plan || !info) return fail(FFTJ_ERR_ARG, "null argument");
+  std::memset(info, 0, sizeof(*info));
+  info->route = plan->route;
+  info->npasses = (int)plan->ops.size();
+  info->n = plan->n;
+  info->batch = plan->batch;
+  info->resample_m = plan->resample_m;
+  info->resample_w = plan->resample_w;
+  for (size_t i = 0; i < plan->pass_R.size() && i < 8; ++i) info->pass_radix[i] = plan->pass_R[i];
+  info->workspace_bytes = plan->ws[0].bytes + plan->ws[1].bytes;
+  info->table_bytes = plan->table_bytes;
+  return FFTJ_OK;
+}
+
+int fftj_plan_workspace_bytes(fftj_plan plan, size_t* bytes) {
+  if (!plan || !bytes) return fail(FFTJ_ERR_ARG, "null argument");
+  *bytes = plan->ws[0].bytes + plan->ws[1].bytes;
+  return FFTJ_OK;
+}
+
+int fftj_plan_destroy(fftj_plan plan) {
+  delete plan;
+  return FFTJ_OK;
+}
+
+const char* fftj_last_error_string(void) { return g_err.c_str(); }
+
+const char* fftj_version(void) { return "fftj-gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,434 @@
+"""fftj — GB300-native FFTJ transform plans over CUDA tensors.
+
+Host-side mirror of FFTJ.jl's plan surface (src/api.jl, src/plan.jl,
+src/real.jl, src/ndplan.jl) on top of the C ABI in include/fftj.h. Plans are
+built by the native planner (factorization, FP64 twiddles, resampling
+weights) and executed by hand-written sm_103a kernels; there is no CPU path:
+inputs must be CUDA tensors and the library must be built (build()).
+
+Name mapping from Julia: plan_fft! -> plan_fft_, mul!(y, p, x) -> mul_(y, p, x),
+p * x -> p * x, inv(p) -> inv(p) (a Scaled with public .p / .scale), size(p)
+-> size(p). Array-based planners take a tensor; Julia's column-major dims are
+the reverse of a tensor's shape (the last tensor axis is FFTJ's dim 1).
+Extension: plan_fft(T, n, batch=B) plans B transforms laid out as (B, n).
+"""
+import ctypes
+import os
+
+import numpy as np
+import torch
+
+from . import _build
+
+__all__ = [
+    "plan_fft", "plan_ifft", "plan_bfft", "plan_fft_", "plan_ifft_", "plan_bfft_",
+    "plan_rfft", "plan_irfft", "plan_brfft",
+    "fft", "ifft", "bfft", "fft_", "ifft_", "bfft_", "rfft", "irfft", "brfft",
+    "mul_", "inv", "size", "Plan", "InplacePlan", "Scaled",
+    "ArgumentError", "DimensionMismatch", "FFTJError", "lib", "build",
+]
+
+
+class FFTJError(RuntimeError):
+    """A CUDA or unsupported-case failure reported by the library."""
+
+
+class ArgumentError(ValueError):
+    """FFTJ's ArgumentError (bad length, region or keyword)."""
+
+
+class DimensionMismatch(ValueError):
+    """FFTJ's DimensionMismatch (array sizes do not match the plan)."""
+
+
+ROUTES = {0: "FFTPlan", 1: "FourStepPlan", 2: "ResamplePlan", 3: "HvdhPlan", 4: "NdPlan"}
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [
+        ("route", ctypes.c_int), ("npasses", ctypes.c_int), ("n", ctypes.c_int64),
+        ("batch", ctypes.c_int64), ("resample_m", ctypes.c_int64), ("resample_w", ctypes.c_int64),
+        ("pass_radix", ctypes.c_int * 8), ("workspace_bytes", ctypes.c_size_t),
+        ("table_bytes", ctypes.c_size_t),
+    ]
+
+
+_lib = None
+EXPORTS = [
+    "fftj_plan_c2c", "fftj_plan_r2c", "fftj_plan_c2r", "fftj_execute", "fftj_plan_get_info",
+    "fftj_plan_workspace_bytes", "fftj_plan_destroy", "fftj_last_error_string", "fftj_version",
+]
+
+
+def build(force=False):
+    """Compile libfftj_gb300.so for sm_103a (nvcc) if it is missing or stale."""
+    return _build.build(force=force)
+
+
+def lib():
+    """The loaded native library. Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not os.path.exists(path):
+            raise FFTJError("libfftj_gb300.so is not built (call fftj.build()); there is no CPU fallback")
+        L = ctypes.CDLL(path)
+        vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+        P64 = ctypes.POINTER(ctypes.c_int64)
+        L.fftj_plan_c2c.argtypes = [ctypes.POINTER(vp), i32, i32, P64, i64, i64, i64, i32, ctypes.c_double]
+        L.fftj_plan_r2c.argtypes = [ctypes.POINTER(vp), i32, i32, P64, i64, i64, i64]
+        L.fftj_plan_c2r.argtypes = [ctypes.POINTER(vp), i32, i32, P64, i64, i64, i64, i32]
+        L.fftj_execute.argtypes = [vp, vp, vp, vp]
+        L.fftj_plan_get_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
+        L.fftj_plan_workspace_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
+        L.fftj_plan_destroy.argtypes = [vp]
+        L.fftj_last_error_string.restype = ctypes.c_char_p
+        L.fftj_version.restype = ctypes.c_char_p
+        for name in EXPORTS:
+            L[name].restype = L[name].restype if name in ("fftj_last_error_string", "fftj_version") else i32
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc == 0:
+        return
+    msg = lib().fftj_last_error_string().decode()
+    if rc == 1:
+        raise ArgumentError(msg)
+    if rc == 2:
+        raise DimensionMismatch(msg)
+    raise FFTJError("fftj status %d: %s" % (rc, msg))
+
+
+def _dtcode(T):
+    if T in (np.float32, torch.float32, "f32", "float32", np.complex64, torch.complex64):
+        return 0
+    if T in (np.float64, torch.float64, "f64", "float64", np.complex128, torch.complex128):
+        return 1
+    raise ArgumentError("element type must be Float32 or Float64 (got %r)" % (T,))
+
+
+_CDT = {0: torch.complex64, 1: torch.complex128}
+_RDT = {0: torch.float32, 1: torch.float64}
+
+
+class Plan:
+    """A device plan (FFTJ FFTPlan/FourStepPlan/ResamplePlan/NdPlan/Rfft*Plan).
+
+    kind: 'c2c' | 'r2c' | 'c2r'. dims are FFTJ's column-major lengths."""
+
+    def __init__(self, T, dims, kind="c2c", direction=-1, scale=1.0, batch=1, normalized=True):
+        self.dt = _dtcode(T)
+        self.dims = tuple(int(d) for d in dims)
+        if any(d < 1 for d in self.dims):
+            raise ArgumentError("transform length must be positive (got %r)" % (self.dims,))
+        self.kind = kind
+        self.direction = direction
+        self.scale = float(scale)
+        self.batch = int(batch)
+        self.normalized = bool(normalized)
+        self.n = int(np.prod(self.dims))
+        h = ctypes.c_void_p()
+        arr = (ctypes.c_int64 * len(self.dims))(*self.dims)
+        if kind == "c2c":
+            rc = lib().fftj_plan_c2c(ctypes.byref(h), self.dt, len(self.dims), arr, self.batch, 0, 0,
+                                     int(direction), self.scale)
+        elif kind == "r2c":
+            rc = lib().fftj_plan_r2c(ctypes.byref(h), self.dt, len(self.dims), arr, self.batch, 0, 0)
+        else:
+            rc = lib().fftj_plan_c2r(ctypes.byref(h), self.dt, len(self.dims), arr, self.batch, 0, 0,
+                                     1 if normalized else 0)
+        _check(rc)
+        self._h = h
+
+    # shapes as torch (row-major) shapes, batch first
+    def _cshape(self):
+        d = list(self.dims)
+        if self.kind != "c2c":
+            d[0] = d[0] // 2 + 1
+        s = tuple(reversed(d))
+        return s if self.batch == 1 else (self.batch,) + s
+
+    def _rshape(self):
+        s = tuple(reversed(self.dims))
+        return s if self.batch == 1 else (self.batch,) + s
+
+    def in_spec(self):
+        if self.kind == "r2c":
+            return self._rshape(), _RDT[self.dt]
+        return self._cshape() if self.kind == "c2r" else self._rshape(), _CDT[self.dt]
+
+    def out_spec(self):
+        if self.kind == "c2r":
+            return self._rshape(), _RDT[self.dt]
+        return self._cshape() if self.kind == "r2c" else self._rshape(), _CDT[self.dt]
+
+    @property
+    def info(self):
+        inf = PlanInfo()
+        _check(lib().fftj_plan_get_info(self._h, ctypes.byref(inf)))
+        return inf
+
+    @property
+    def route(self):
+        return ROUTES[self.info.route]
+
+    @property
+    def handle(self):
+        return self._h.value
+
+    def _validate(self, t, spec, what):
+        shape, dtype = spec
+        if not isinstance(t, torch.Tensor) or not t.is_cuda:
+            raise ArgumentError("%s must be a CUDA tensor (there is no CPU path)" % what)
+        if t.dtype != dtype:
+            raise ArgumentError("%s must have dtype %s (got %s)" % (what, dtype, t.dtype))
+        if t.numel() != int(np.prod(shape)):
+            raise DimensionMismatch("plan size %s, %s size %s" % (tuple(shape), what, tuple(t.shape)))
+        if not t.is_contiguous():
+            raise ArgumentError("%s must be contiguous" % what)
+
+    def __call__(self, y, x=None):
+        """p(y, x) writes y; p(x) allocates y (FFTJ src/plan.jl:359-398)."""
+        if x is None:
+            x = y
+            shape, dtype = self.out_spec()
+            y = torch.empty(shape, dtype=dtype, device=x.device)
+        self._validate(x, self.in_spec(), "input")
+        self._validate(y, self.out_spec(), "output")
+        stream = torch.cuda.current_stream(x.device).cuda_stream
+        _check(lib().fftj_execute(self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                  ctypes.c_void_p(stream)))
+        return y
+
+    def __mul__(self, x):
+        return self(x)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.fftj_plan_destroy(h)
+            self._h = None
+
+    def __repr__(self):
+        return "fftj.Plan(%s, dims=%s, dir=%d, batch=%d, route=%s)" % (
+            self.kind, self.dims, self.direction, self.batch, self.route)
+
+
+class InplacePlan:
+    """FFTJ InplacePlan (src/api.jl:15-24): p * x overwrites x."""
+
+    def __init__(self, p):
+        self.p = p
+
+    def __call__(self, y, x=None):
+        return self.p(y, x)
+
+    def __mul__(self, x):
+        self.p(x, x)
+        return x
+
+
+class Scaled:
+    """A plan scaled by a constant, as inv() returns (src/api.jl:26-31);
+    .p and .scale are public (DSP's inv(p).p idiom)."""
+
+    def __init__(self, p, scale):
+        self.p = p
+        self.scale = scale
+
+    def __call__(self, y, x=None):
+        if x is None:
+            return self * y
+        mul_(y, self.p, x)
+        y.mul_(self.scale)
+        return y
+
+    def __mul__(self, x):
+        y = self.p * x
+        return y.mul_(self.scale)
+
+
+def mul_(y, p, x):
+    """mul!(y, p, x) (src/api.jl:34-55)."""
+    if isinstance(p, Scaled):
+        return p(y, x)
+    p(y, x)
+    return y
+
+
+def size(p):
+    """size(p) (src/api.jl:57-60, 166-168), FFTJ order (dim 1 first)."""
+    if isinstance(p, (InplacePlan, Scaled)):
+        return size(p.p)
+    if p.kind == "c2r":
+        d = list(p.dims)
+        d[0] = d[0] // 2 + 1
+        return tuple(d)
+    return p.dims
+
+
+def _dims_of(x):
+    return tuple(reversed(tuple(x.shape)))
+
+
+def _elt(x):
+    return {torch.complex64: np.float32, torch.complex128: np.float64,
+            torch.float32: np.float32, torch.float64: np.float64}.get(x.dtype)
+
+
+def _check_region(region, N):
+    if region is None:
+        return
+    r = tuple(region) if not isinstance(region, int) else (region,)
+    if r != tuple(range(1, N + 1)) and not (N == 1 and r == (1,)):
+        raise ArgumentError("FFTJ N-d plans transform all dims (expected region 1:%d, got %r)" % (N, region))
+
+
+def _planner(direction, scale_kind):
+    def plan(T_or_x, n=None, region=None, *, batch=1, nthreads=None, flags=None, **kws):
+        if isinstance(T_or_x, torch.Tensor):
+            x = T_or_x
+            if not x.is_complex():
+                raise ArgumentError("complex plans need a complex tensor")
+            dims = _dims_of(x)
+            _check_region(region if n is None else n, len(dims))
+            T = _elt(x)
+            batch = 1
+        else:
+            T, dims = T_or_x, (int(n),) if np.isscalar(n) else tuple(int(v) for v in n)
+        nn = int(np.prod(dims))
+        if any(d < 1 for d in dims):
+            raise ArgumentError("transform length must be positive (got %r)" % (dims,))
+        scale = 1.0 / nn if scale_kind == "inv" else 1.0
+        return Plan(T, dims, "c2c", direction, scale, batch=batch)
+    return plan
+
+
+plan_fft = _planner(-1, "one")
+plan_ifft = _planner(+1, "inv")
+plan_bfft = _planner(+1, "one")
+plan_fft.__doc__ = "plan_fft(T, n) / plan_fft(x) (src/plan.jl:207-208, src/api.jl:107-112)"
+plan_ifft.__doc__ = "plan_ifft(T, n) / plan_ifft(x): normalized inverse (src/plan.jl:209-210)"
+plan_bfft.__doc__ = "plan_bfft(T, n) / plan_bfft(x): unnormalized backward (src/plan.jl:212-213)"
+
+
+def plan_fft_(*a, **k):
+    """plan_fft!: in-place (src/api.jl:15-24, 125-130)."""
+    return InplacePlan(plan_fft(*a, **k))
+
+
+def plan_ifft_(*a, **k):
+    return InplacePlan(plan_ifft(*a, **k))
+
+
+def plan_bfft_(*a, **k):
+    return InplacePlan(plan_bfft(*a, **k))
+
+
+def plan_rfft(T_or_x, n=None, region=None, *, batch=1, nthreads=None, flags=None, **kws):
+    """plan_rfft(T, n) / plan_rfft(x) (src/real.jl:41-52, src/api.jl:347-352)."""
+    if isinstance(T_or_x, torch.Tensor):
+        x = T_or_x
+        dims = _dims_of(x)
+        _check_region(region if n is None else n, len(dims))
+        return Plan(_elt(x), dims, "r2c", -1)
+    T, dims = T_or_x, (int(n),) if np.isscalar(n) else tuple(int(v) for v in n)
+    return Plan(T, dims, "r2c", -1, batch=batch)
+
+
+def _plan_c2r(normalized):
+    def plan(T_or_X, n1=None, region=None, *, batch=1, nthreads=None, flags=None, **kws):
+        if isinstance(T_or_X, torch.Tensor):
+            X = T_or_X
+            cd = _dims_of(X)
+            if n1 is None:
+                raise ArgumentError("the real length n1 is required")
+            if cd[0] != int(n1) // 2 + 1:
+                raise DimensionMismatch("irfft of leading length %d needs %d rows, got %d"
+                                        % (n1, int(n1) // 2 + 1, cd[0]))
+            _check_region(region, len(cd))
+            return Plan(_elt(X), (int(n1),) + cd[1:], "c2r", +1, normalized=normalized)
+        T, dims = T_or_X, (int(n1),) if np.isscalar(n1) else tuple(int(v) for v in n1)
+        return Plan(T, dims, "c2r", +1, batch=batch, normalized=normalized)
+    return plan
+
+
+plan_irfft = _plan_c2r(True)
+plan_brfft = _plan_c2r(False)
+plan_irfft.__doc__ = "plan_irfft(T, n) / plan_irfft(X, n1) (src/real.jl:57-70, src/api.jl:362-370)"
+plan_brfft.__doc__ = "plan_brfft(T, n) / plan_brfft(X, n1) (src/real.jl:72-73, src/api.jl:353-361)"
+
+
+def inv(p):
+    """inv (src/api.jl:75-94, 170-179): forward -> Scaled(bfft, 1/n);
+    normalized inverse -> plain forward; unnormalized backward ->
+    Scaled(forward, 1/n); InplacePlan and Scaled wrap accordingly."""
+    if isinstance(p, InplacePlan):
+        s = inv(p.p)
+        return Scaled(InplacePlan(s.p), s.scale) if isinstance(s, Scaled) else InplacePlan(s)
+    if isinstance(p, Scaled):
+        q = inv(p.p)
+        return Scaled(q.p, q.scale / p.scale) if isinstance(q, Scaled) else Scaled(q, 1.0 / p.scale)
+    n = p.n
+    T = np.float32 if p.dt == 0 else np.float64
+    if p.kind != "c2c":
+        raise ArgumentError("inv is defined for complex plans")
+    if p.direction == -1:
+        return Scaled(Plan(T, p.dims, "c2c", +1, 1.0, batch=p.batch), 1.0 / n)
+    if p.scale == 1.0:
+        return Scaled(Plan(T, p.dims, "c2c", -1, 1.0, batch=p.batch), 1.0 / n)
+    return Plan(T, p.dims, "c2c", -1, 1.0, batch=p.batch)
+
+
+# one-shot transforms (src/api.jl:97-99, 182-203)
+def _as_complex(x):
+    if not x.is_complex():
+        return x.to(torch.complex64 if x.dtype in (torch.float32, torch.float16, torch.bfloat16)
+                    else torch.complex128)
+    return x.contiguous()
+
+
+def fft(x):
+    x = _as_complex(x)
+    return plan_fft(x) * x
+
+
+def ifft(x):
+    x = _as_complex(x)
+    return plan_ifft(x) * x
+
+
+def bfft(x):
+    x = _as_complex(x)
+    return plan_bfft(x) * x
+
+
+def fft_(x):
+    return plan_fft_(x) * x
+
+
+def ifft_(x):
+    return plan_ifft_(x) * x
+
+
+def bfft_(x):
+    return plan_bfft_(x) * x
+
+
+def rfft(x):
+    if x.is_complex():
+        raise ArgumentError("rfft needs real input")
+    x = x.contiguous() if x.dtype in (torch.float32, torch.float64) else x.to(torch.float64).contiguous()
+    return plan_rfft(x) * x
+
+
+def irfft(X, n1):
+    X = _as_complex(X)
+    return plan_irfft(X, n1) * X
+
+
+def brfft(X, n1):
+    X = _as_complex(X)
+    return plan_brfft(X, n1) * X

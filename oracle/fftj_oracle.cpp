@@ -1,0 +1,1414 @@
+// TEST INFRASTRUCTURE ONLY — the oracle. Never part of the product path.
+//
+// CPU restatement of FFTJ.jl's transform path (oscardssmith/FFTJ.jl, pure
+// Julia; Julia is absent here so the reference cannot be run). Every function
+// cites the reference file:line it follows. The scalar branches of FFTJ's
+// SIMD stage loops give the canonical index maps restated here; the loops over
+// the stride lane q are left to the compiler's auto-vectoriser (NEON on the
+// Grace host), standing in for FFTJ's explicit SIMD.Vec code.
+//
+// Parity status: pinned against an FP64 direct DFT (double-double
+// accumulation, exact angle reduction) and numpy's pocketfft at the reference
+// test sizes; see tests/test_oracle.py.
+#include "fftj_oracle.hpp"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <thread>
+#include <vector>
+
+namespace orc {
+
+using i64 = int64_t;
+
+// ---------------------------------------------------------------------------
+// Host SIMD width (src/kernels.jl:11-22): only used for routing and towers.
+static int g_vector_bits = 128;
+template <typename T>
+static inline int pick_width() { return g_vector_bits / (8 * (int)sizeof(T)); }
+
+// ---------------------------------------------------------------------------
+// sin(pi x), cos(pi x) with exact reduction to [0, 1/4] (stands in for
+// Julia's Base.sincospi used for every twiddle, src/plan.jl:76-77).
+static void sincospi(double x, double* s, double* c) {
+  double sg = 1.0;
+  if (x < 0) { x = -x; sg = -1.0; }
+  double r = std::fmod(x, 2.0);
+  double ss = 1.0, cs = 1.0;
+  if (r >= 1.0) { r -= 1.0; ss = -ss; cs = -cs; }
+  bool swap = false;
+  if (r > 0.5) { r = 1.0 - r; cs = -cs; }
+  if (r > 0.25) { r = 0.5 - r; swap = true; }
+  double a = M_PI * r;
+  double sv = std::sin(a), cv = std::cos(a);
+  if (swap) std::swap(sv, cv);
+  *s = sg * ss * sv;
+  *c = cs * cv;
+}
+static inline double cospi_(double x) { double s, c; sincospi(x, &s, &c); return c; }
+static inline double sinpi_(double x) { double s, c; sincospi(x, &s, &c); return s; }
+
+// ---------------------------------------------------------------------------
+// Deterministic fork-join (src/threads.jl:15-41): split [0, len) into at most
+// nt chunks whose starts sit on `align`; the last chunk absorbs the tail.
+class Pool {
+ public:
+  static Pool& get() { static Pool p; return p; }
+  int size() const { return (int)workers_.size() + 1; }
+  // run f(ci) for ci in [0, nchunks) on the workers and the caller
+  void run(int nchunks, const std::function<void(int)>& f) {
+    if (nchunks <= 1) { if (nchunks == 1) f(0); return; }
+    std::unique_lock<std::mutex> lk(mu_);
+    job_ = &f;
+    njob_ = nchunks;
+    next_.store(1);
+    done_ = 0;
+    gen_++;
+    cv_.notify_all();
+    lk.unlock();
+    f(0);
+    for (;;) {
+      int c = next_.fetch_add(1);
+      if (c >= nchunks) break;
+      f(c);
+      std::lock_guard<std::mutex> g(mu_);
+      done_++;
+    }
+    lk.lock();
+    done_cv_.wait(lk, [&] { return done_ >= nchunks - 1; });
+    job_ = nullptr;
+  }
+  ~Pool() {
+    { std::lock_guard<std::mutex> g(mu_); stop_ = true; gen_++; }
+    cv_.notify_all();
+    for (auto& t : workers_) t.join();
+  }
+
+ private:
+  Pool() {
+    unsigned hc = std::thread::hardware_concurrency();
+    int nw = (int)(hc > 1 ? hc - 1 : 0);
+    for (int i = 0; i < nw; ++i) workers_.emplace_back([this] { loop(); });
+  }
+  void loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      const std::function<void(int)>* job;
+      int nj;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (stop_) return;
+        job = job_;
+        nj = njob_;
+      }
+      if (!job) continue;
+      for (;;) {
+        int c = next_.fetch_add(1);
+        if (c >= nj) break;
+        (*job)(c);
+        std::lock_guard<std::mutex> g(mu_);
+        done_++;
+        if (done_ >= nj - 1) done_cv_.notify_all();
+      }
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(int)>* job_ = nullptr;
+  int njob_ = 0;
+  std::atomic<int> next_{0};
+  int done_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
+// tforeach_chunks (src/threads.jl:15-38), 0-based half-open ranges.
+static void tforeach_chunks(i64 len, int nt, i64 align,
+                            const std::function<void(int, i64, i64)>& f) {
+  if (len <= 0) return;
+  i64 units = len / align;
+  i64 nchunks = std::min<i64>(nt, units);
+  if (nchunks <= 1) { f(0, 0, len); return; }
+  i64 per = units / nchunks, rem = units % nchunks;
+  std::vector<i64> lo(nchunks), hi(nchunks);
+  i64 l = 0;
+  for (i64 c = 0; c < nchunks; ++c) {
+    i64 u = per + (c < rem ? 1 : 0);
+    i64 h = (c == nchunks - 1) ? len : l + u * align;
+    lo[c] = l; hi[c] = h; l = h;
+  }
+  Pool::get().run((int)nchunks, [&](int c) { f(c, lo[c], hi[c]); });
+}
+static void tforeach(i64 len, int nt, i64 align, const std::function<void(i64, i64)>& f) {
+  tforeach_chunks(len, nt, align, [&](int, i64 lo, i64 hi) { f(lo, hi); });
+}
+static const i64 MIN_CHUNK = 1 << 15;  // src/threads.jl:7
+static int plan_tasks(i64 work, int nthreads) {  // src/plan.jl:62
+  return (int)std::min<i64>(std::max(nthreads, 1), std::max<i64>(work / MIN_CHUNK, 1));
+}
+
+// ---------------------------------------------------------------------------
+// Factorization (src/plan.jl:16-45).
+static const int ODD_RADICES[5] = {13, 11, 7, 5, 3};
+struct Fac { int a; std::vector<std::pair<int, int>> ps; bool ok; };
+static Fac factor_radices(i64 n) {
+  Fac f; f.ok = false; f.a = 0;
+  if (n < 1) return f;
+  int a = __builtin_ctzll((unsigned long long)n);
+  i64 r = n >> a;
+  for (int p : ODD_RADICES) {
+    int c = 0;
+    while (r % p == 0) { r /= p; c++; }
+    if (c > 0) f.ps.push_back({p, c});
+  }
+  f.a = a;
+  f.ok = (r == 1);
+  return f;
+}
+static bool factor_smooth(i64 n) {
+  if (n < 1) return false;
+  i64 r = n >> __builtin_ctzll((unsigned long long)n);
+  for (int p : {3, 5, 7}) while (r % p == 0) r /= p;
+  return r == 1;
+}
+
+template <typename T>
+struct Stage {
+  int radix;
+  std::vector<T> twr, twi;  // (radix-1) twiddles per butterfly, [(radix-1)*p + j-1]
+};
+
+// make_stage (src/plan.jl:66-95), non-small layout (same values).
+template <typename T>
+static Stage<T> make_stage(int radix, i64 n, int D) {
+  i64 m = n / radix;
+  Stage<T> st;
+  st.radix = radix;
+  st.twr.resize((size_t)(radix - 1) * m);
+  st.twi.resize((size_t)(radix - 1) * m);
+  for (i64 p = 0; p < m; ++p)
+    for (int j = 1; j < radix; ++j) {
+      double th = (double)(2 * D * p * j) / (double)n;
+      double s, c;
+      sincospi(th, &s, &c);
+      st.twr[(size_t)(radix - 1) * p + j - 1] = (T)c;
+      st.twi[(size_t)(radix - 1) * p + j - 1] = (T)s;
+    }
+  return st;
+}
+
+// _tower (src/plan.jl:105-117)
+template <typename T>
+static void tower(int a, bool allow_small, int* f, std::vector<int>* rad) {
+  rad->clear();
+  if (a == 0) { *f = 1; return; }
+  if (a <= 3) { *f = 1 << a; return; }
+  int W = pick_width<T>();
+  int k = 0;
+  while (allow_small && (1 << (2 * k)) < W && 2 * (k + 1) <= a - 2) k++;
+  int b = a - 2 * k;
+  const int n4tab[3] = {0, 2, 1};
+  int n4 = n4tab[b % 3];
+  std::vector<int> r;
+  for (int i = 0; i < k + n4; ++i) r.push_back(4);
+  for (int i = 0; i < (b - 2 * n4) / 3; ++i) r.push_back(8);
+  *f = r.back();
+  r.pop_back();
+  *rad = r;
+}
+
+// build_stages (src/plan.jl:125-151): tower, odd stages smallest first, final f.
+template <typename T>
+static std::vector<Stage<T>> build_stages(i64 n, int D, bool allow_small, int* fout = nullptr) {
+  Fac fac = factor_radices(n);
+  if (!fac.ok) throw std::runtime_error("build_stages requires 13-smooth n");
+  int f;
+  std::vector<int> tw;
+  tower<T>(fac.a, allow_small, &f, &tw);
+  std::vector<Stage<T>> stages;
+  i64 ncur = n;
+  for (int r : tw) { stages.push_back(make_stage<T>(r, ncur, D)); ncur /= r; }
+  for (auto it = fac.ps.rbegin(); it != fac.ps.rend(); ++it)
+    for (int c = 0; c < it->second; ++c) {
+      stages.push_back(make_stage<T>(it->first, ncur, D));
+      ncur /= it->first;
+    }
+  if (f > 1) stages.push_back(make_stage<T>(f, ncur, D));
+  if (fout) *fout = f;
+  return stages;
+}
+
+// ---------------------------------------------------------------------------
+// Butterflies (src/kernels.jl:24-239), scalar.
+template <typename T>
+static inline void cmul(T wr, T wi, T xr, T xi, T* yr, T* yi) {
+  *yr = std::fma(wr, xr, -(wi * xi));
+  *yi = std::fma(wr, xi, wi * xr);
+}
+
+template <typename T>
+static inline void bf4_core(T ar, T ai, T br, T bi, T cr, T ci, T dr, T di, int D, T* y) {
+  T apcr = ar + cr, apci = ai + ci, amcr = ar - cr, amci = ai - ci;
+  T bpdr = br + dr, bpdi = bi + di, bmdr = br - dr, bmdi = bi - di;
+  y[0] = apcr + bpdr; y[1] = apci + bpdi;
+  if (D == -1) {
+    y[2] = amcr + bmdi; y[3] = amci - bmdr;
+    y[6] = amcr - bmdi; y[7] = amci + bmdr;
+  } else {
+    y[2] = amcr - bmdi; y[3] = amci + bmdr;
+    y[6] = amcr + bmdi; y[7] = amci - bmdr;
+  }
+  y[4] = apcr - bpdr; y[5] = apci - bpdi;
+}
+
+template <typename T>
+static inline void bf8_core(const T* xr, const T* xi, T c, int D, T* y) {
+  T e[8], o[8];
+  bf4_core(xr[0], xi[0], xr[2], xi[2], xr[4], xi[4], xr[6], xi[6], D, e);
+  bf4_core(xr[1], xi[1], xr[3], xi[3], xr[5], xi[5], xr[7], xi[7], D, o);
+  T t1r, t1i, t2r, t2i, t3r, t3i;
+  if (D == -1) {
+    t1r = c * (o[2] + o[3]); t1i = c * (o[3] - o[2]);
+    t2r = o[5]; t2i = -o[4];
+    t3r = c * (o[7] - o[6]); t3i = -c * (o[6] + o[7]);
+  } else {
+    t1r = c * (o[2] - o[3]); t1i = c * (o[3] + o[2]);
+    t2r = -o[5]; t2i = o[4];
+    t3r = -c * (o[6] + o[7]); t3i = c * (o[6] - o[7]);
+  }
+  y[0] = e[0] + o[0]; y[1] = e[1] + o[1];
+  y[2] = e[2] + t1r; y[3] = e[3] + t1i;
+  y[4] = e[4] + t2r; y[5] = e[5] + t2i;
+  y[6] = e[6] + t3r; y[7] = e[7] + t3i;
+  y[8] = e[0] - o[0]; y[9] = e[1] - o[1];
+  y[10] = e[2] - t1r; y[11] = e[3] - t1i;
+  y[12] = e[4] - t2r; y[13] = e[5] - t2i;
+  y[14] = e[6] - t3r; y[15] = e[7] - t3i;
+}
+
+// bfp_consts / bfp (src/kernels.jl:158-228): odd-prime DFT by conjugate pairs.
+template <typename T>
+struct BfpConsts {
+  int P, h;
+  std::vector<T> cc, ss;  // [(k-1)*h + (j-1)]
+  BfpConsts(int P_, int D) : P(P_), h((P_ - 1) / 2) {
+    cc.resize(h * h); ss.resize(h * h);
+    for (int k = 1; k <= h; ++k)
+      for (int j = 1; j <= h; ++j) {
+        double th = (double)(2 * (j * k)) / (double)P;
+        cc[(k - 1) * h + j - 1] = (T)cospi_(th);
+        ss[(k - 1) * h + j - 1] = (T)(D * sinpi_(th));
+      }
+  }
+};
+
+template <typename T>
+static inline void bfp(int P, const T* xr, const T* xi, const BfpConsts<T>& K, T* yr, T* yi) {
+  int h = (P - 1) / 2;
+  T tr[6], ti[6], dr[6], di[6];
+  for (int j = 1; j <= h; ++j) {
+    tr[j - 1] = xr[j] + xr[P - j]; ti[j - 1] = xi[j] + xi[P - j];
+    dr[j - 1] = xr[j] - xr[P - j]; di[j - 1] = xi[j] - xi[P - j];
+  }
+  T sr = tr[0], si = ti[0];
+  for (int j = 2; j <= h; ++j) { sr = sr + tr[j - 1]; si = si + ti[j - 1]; }
+  yr[0] = xr[0] + sr; yi[0] = xi[0] + si;
+  for (int k = 1; k <= h; ++k) {
+    T er = xr[0], ei = xi[0];
+    for (int j = h; j >= 1; --j) {
+      T c = K.cc[(k - 1) * h + j - 1];
+      er = std::fma(c, tr[j - 1], er);
+      ei = std::fma(c, ti[j - 1], ei);
+    }
+    T s = K.ss[(k - 1) * h + h - 1];
+    T vr = s * dr[h - 1], vi = s * di[h - 1];
+    for (int j = h - 1; j >= 1; --j) {
+      T sj = K.ss[(k - 1) * h + j - 1];
+      vr = std::fma(sj, dr[j - 1], vr);
+      vi = std::fma(sj, di[j - 1], vi);
+    }
+    yr[k] = er - vi; yi[k] = ei + vr;          // X_k = u + i v
+    yr[P - k] = er + vi; yi[P - k] = ei - vr;  // X_{P-k} = u - i v
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stage loops (src/stockham.jl:26-428), scalar index maps over p in
+// [plo, phi) and q in [qlo, qhi): read x[s*p + j*m*s + q], write
+// y[r*s*p + j*s + q] twiddled by w_j (output 0 untwiddled).
+template <typename T>
+static void run_stage_pq(T* yre, T* yim, const T* xre, const T* xim, i64 n, i64 s,
+                         const Stage<T>& st, int D, i64 plo, i64 phi, i64 qlo, i64 qhi) {
+  const int r = st.radix;
+  const i64 m = n / r, ms = m * s;
+  const T* twr = st.twr.data();
+  const T* twi = st.twi.data();
+  if (r == 4) {
+    for (i64 p = plo; p < phi; ++p) {
+      T w1r = twr[3 * p], w1i = twi[3 * p], w2r = twr[3 * p + 1], w2i = twi[3 * p + 1];
+      T w3r = twr[3 * p + 2], w3i = twi[3 * p + 2];
+      i64 xb = s * p, yb = 4 * s * p;
+      for (i64 q = qlo; q < qhi; ++q) {
+        T y[8];
+        bf4_core(xre[xb + q], xim[xb + q], xre[xb + ms + q], xim[xb + ms + q],
+                 xre[xb + 2 * ms + q], xim[xb + 2 * ms + q], xre[xb + 3 * ms + q],
+                 xim[xb + 3 * ms + q], D, y);
+        yre[yb + q] = y[0]; yim[yb + q] = y[1];
+        cmul(w1r, w1i, y[2], y[3], &yre[yb + s + q], &yim[yb + s + q]);
+        cmul(w2r, w2i, y[4], y[5], &yre[yb + 2 * s + q], &yim[yb + 2 * s + q]);
+        cmul(w3r, w3i, y[6], y[7], &yre[yb + 3 * s + q], &yim[yb + 3 * s + q]);
+      }
+    }
+  } else if (r == 8) {
+    const T c = (T)std::sqrt(0.5);
+    for (i64 p = plo; p < phi; ++p) {
+      i64 xb = s * p, yb = 8 * s * p;
+      for (i64 q = qlo; q < qhi; ++q) {
+        T xr[8], xi[8], y[16];
+        for (int k = 0; k < 8; ++k) { xr[k] = xre[xb + k * ms + q]; xi[k] = xim[xb + k * ms + q]; }
+        bf8_core(xr, xi, c, D, y);
+        yre[yb + q] = y[0]; yim[yb + q] = y[1];
+        for (int j = 1; j < 8; ++j)
+          cmul(twr[7 * p + j - 1], twi[7 * p + j - 1], y[2 * j], y[2 * j + 1],
+               &yre[yb + j * s + q], &yim[yb + j * s + q]);
+      }
+    }
+  } else if (r == 2) {
+    for (i64 p = plo; p < phi; ++p) {
+      T wr = twr[p], wi = twi[p];
+      i64 xb = s * p, yb = 2 * s * p;
+      for (i64 q = qlo; q < qhi; ++q) {
+        T ar = xre[xb + q], ai = xim[xb + q], br = xre[xb + ms + q], bi = xim[xb + ms + q];
+        yre[yb + q] = ar + br; yim[yb + q] = ai + bi;
+        cmul(wr, wi, ar - br, ai - bi, &yre[yb + s + q], &yim[yb + s + q]);
+      }
+    }
+  } else {
+    BfpConsts<T> K(r, D);
+    for (i64 p = plo; p < phi; ++p) {
+      i64 xb = s * p, yb = r * s * p;
+      for (i64 q = qlo; q < qhi; ++q) {
+        T xr[13], xi[13], yr[13], yi[13];
+        for (int j = 0; j < r; ++j) { xr[j] = xre[xb + j * ms + q]; xi[j] = xim[xb + j * ms + q]; }
+        bfp(r, xr, xi, K, yr, yi);
+        yre[yb + q] = yr[0]; yim[yb + q] = yi[0];
+        for (int j = 1; j < r; ++j)
+          cmul(twr[(r - 1) * p + j - 1], twi[(r - 1) * p + j - 1], yr[j], yi[j],
+               &yre[yb + j * s + q], &yim[yb + j * s + q]);
+      }
+    }
+  }
+}
+
+// run_stage! / run_stage_par! (src/plan.jl:215-284): split butterflies p when
+// plentiful, else W-aligned lanes q.
+template <typename T>
+static void run_stage(T* yre, T* yim, const T* xre, const T* xim, i64 n, i64 s,
+                      const Stage<T>& st, int D, int nt) {
+  i64 m = n / st.radix;
+  if (nt <= 1) { run_stage_pq(yre, yim, xre, xim, n, s, st, D, 0, m, 0, s); return; }
+  int W = pick_width<T>();
+  if (m >= nt || s < W) {
+    tforeach(m, nt, 1, [&](i64 lo, i64 hi) { run_stage_pq(yre, yim, xre, xim, n, s, st, D, lo, hi, 0, s); });
+  } else {
+    tforeach(s, nt, W, [&](i64 lo, i64 hi) { run_stage_pq(yre, yim, xre, xim, n, s, st, D, 0, m, lo, hi); });
+  }
+}
+
+// run_chain! (src/plan.jl:311-321): ping-pong, effective stride s*B.
+// Returns true when the result sits in (ore, oim).
+template <typename T>
+static bool run_chain(T* cre, T* cim, T* ore, T* oim, const std::vector<Stage<T>>& stages,
+                      size_t from, size_t to, i64 ncur, i64 s, i64 B, int D, int nt) {
+  bool swapped = false;
+  for (size_t k = from; k < to; ++k) {
+    const Stage<T>& st = stages[k];
+    run_stage(ore, oim, cre, cim, ncur, s * B, st, D, nt);
+    std::swap(cre, ore); std::swap(cim, oim);
+    swapped = !swapped;
+    s *= st.radix;
+    ncur /= st.radix;
+  }
+  return swapped;
+}
+
+// ---------------------------------------------------------------------------
+// Plans.
+struct PlanBase {
+  virtual ~PlanBase() {}
+  int route = ORC_FFTPLAN;
+  i64 n = 0;
+  virtual void exec(const void* x, void* y) = 0;
+  virtual void info(std::vector<i64>& v) { v.push_back(route); v.push_back(n); }
+};
+
+template <typename T>
+static T default_scale(i64 n, int D) { return D == -1 ? (T)1 : (T)1 / (T)n; }  // src/plan.jl:97
+
+// FFTPlan (src/plan.jl:48-58, 169-177, 359-396).
+template <typename T>
+struct FFTPlan : PlanBase {
+  int D;
+  T scale;
+  int nt;
+  std::vector<Stage<T>> stages;
+  std::vector<T> are, aim, bre, bim;
+  FFTPlan(i64 n_, int D_, T scale_, int nthreads) : D(D_), scale(scale_) {
+    n = n_;
+    route = ORC_FFTPLAN;
+    stages = build_stages<T>(n, D, true);
+    are.resize(n); aim.resize(n); bre.resize(n); bim.resize(n);
+    nt = plan_tasks(n, nthreads);
+  }
+  // planes in -> planes out (result pointer returned)
+  void exec(const void* xv, void* yv) override {
+    const T* x = (const T*)xv;
+    T* y = (T*)yv;
+    // deinterleave_all! (src/stockham.jl:448-469)
+    tforeach(n, nt, pick_width<T>(), [&](i64 lo, i64 hi) {
+      for (i64 c = lo; c < hi; ++c) { are[c] = x[2 * c]; aim[c] = x[2 * c + 1]; }
+    });
+    bool sw = run_chain(are.data(), aim.data(), bre.data(), bim.data(), stages, 0, stages.size(),
+                        n, 1, 1, D, nt);
+    const T* rr = sw ? bre.data() : are.data();
+    const T* ri = sw ? bim.data() : aim.data();
+    // interleave_all! with scale (src/stockham.jl:486-506)
+    T sc = scale;
+    tforeach(n, nt, pick_width<T>(), [&](i64 lo, i64 hi) {
+      for (i64 c = lo; c < hi; ++c) { y[2 * c] = rr[c] * sc; y[2 * c + 1] = ri[c] * sc; }
+    });
+  }
+  void info(std::vector<i64>& v) override {
+    v.push_back(route); v.push_back(n);
+    for (auto& s : stages) v.push_back(s.radix);
+  }
+};
+
+// ---- four-step (src/fourstep.jl) ------------------------------------------
+static const i64 FS_INNER_MAX = 1 << 19;  // src/fourstep.jl:40
+static const i64 FS_TASK_MIN = 1 << 13;   // src/fourstep.jl:251
+
+// _fs_pick (src/fourstep.jl:184-199)
+static i64 fs_pick(i64 n, i64 S, i64 t) {
+  i64 best = 0, besttile = 0;
+  auto dist = [&](i64 d) { return std::fabs(std::log((double)d / (double)t)); };
+  auto better = [&](i64 d, i64 b) { return b == 0 || dist(d) < dist(b) || (dist(d) == dist(b) && d < b); };
+  i64 rq = (i64)std::sqrt((double)n);
+  while (rq * rq > n) rq--;
+  while ((rq + 1) * (rq + 1) <= n) rq++;
+  for (i64 q = 1; q <= rq; ++q) {
+    if (n % q) continue;
+    i64 ds[2] = {q, n / q};
+    for (i64 d : ds) {
+      if (!(d >= S && n / d >= S)) continue;
+      if (!factor_radices(d).ok || !factor_radices(n / d).ok) continue;
+      if (better(d, best)) best = d;
+      if (d % S == 0 && (n / d) % S == 0 && dist(d) <= std::log(2.0) && better(d, besttile)) besttile = d;
+    }
+  }
+  return besttile != 0 ? besttile : best;
+}
+static i64 isqrt_(i64 n) {
+  i64 r = (i64)std::sqrt((double)n);
+  while (r * r > n) r--;
+  while ((r + 1) * (r + 1) <= n) r++;
+  return r;
+}
+
+// _fourstep_split (src/fourstep.jl:166-180)
+template <typename T>
+static bool fourstep_split(i64 n, int width, i64 N2in, i64* N1o, i64* N2o) {
+  int W = pick_width<T>();
+  if (W <= 1) return false;
+  i64 S = (i64)width * W;
+  i64 N2 = N2in;
+  if (N2 == 0) {
+    i64 r = isqrt_(n);
+    i64 nflat = FS_INNER_MAX / (4 * width * W * (i64)sizeof(T));
+    N2 = fs_pick(n, S, std::max(std::min(r, nflat), r / 2));
+    if (N2 == 0) return false;
+  }
+  i64 N1 = n / N2;
+  bool ok = N1 * N2 == n && N1 >= S && N2 >= S && factor_radices(N1).ok && factor_radices(N2).ok;
+  *N1o = N1; *N2o = N2;
+  return ok;
+}
+template <typename T>
+static bool fs_tiled(i64 N1, i64 N2) { return N1 % pick_width<T>() == 0 && N2 % pick_width<T>() == 0; }
+
+// _fs_width (src/fourstep.jl:259-268)
+template <typename T>
+static int fs_width(i64 N2, i64 N1 = 0) {
+  int W = pick_width<T>();
+  int w = std::max<i64>(1, (256 + 2 * W * (i64)sizeof(T) - 1) / (2 * W * (i64)sizeof(T)));
+  auto fits = [&](int w_) {
+    return 4 * (i64)w_ * W * std::max(N1, N2) * (i64)sizeof(T) <= FS_INNER_MAX &&
+           (N1 == 0 || (N1 % ((i64)w_ * W) == 0 && N2 % ((i64)w_ * W) == 0));
+  };
+  while (w > 1 && !fits(w)) w--;
+  return w;
+}
+// _fs_min_bytes / _use_fourstep (src/fourstep.jl:215-226)
+template <typename T>
+static i64 fs_min_bytes(bool threaded, bool wide) {
+  if (!wide) return threaded ? (1 << 20) : (8 << 20);
+  if (threaded) return 1 << 19;
+  return sizeof(T) >= 8 ? (3 << 20) : (5 << 20);
+}
+template <typename T>
+static bool use_fourstep(i64 n, bool threaded) {
+  i64 N1, N2;
+  if (!fourstep_split<T>(n, 1, 0, &N1, &N2) || !fs_tiled<T>(N1, N2)) return false;
+  bool wide = fs_width<T>(N2, N1) > 1;
+  return 2 * n * (i64)sizeof(T) >= fs_min_bytes<T>(threaded, wide);
+}
+// _use_ragged (src/fourstep.jl:238-247)
+template <typename T>
+static bool use_ragged(i64 n, bool threaded) {
+  i64 a2 = (i64)1 << __builtin_ctzll((unsigned long long)n);
+  i64 W4 = 4 * pick_width<T>();
+  bool ok = (a2 < W4 && n >= (sizeof(T) >= 8 ? 2048 : 1024)) ||
+            (sizeof(T) >= 8 && a2 == W4 && n >= (1 << 14)) || (threaded && n >= (1 << 15));
+  if (!ok) return false;
+  i64 N1, N2;
+  if (!fourstep_split<T>(n, 1, 0, &N1, &N2)) return false;
+  return !fs_tiled<T>(N1, N2);
+}
+// _slow_smooth (src/plan.jl:183-187)
+template <typename T>
+static bool slow_smooth(i64 n) {
+  int a = __builtin_ctzll((unsigned long long)n);
+  return sizeof(T) < 8 && (n >> a) > 1 && 48 <= n && n <= 16384 && ((i64)1 << a) < 4 * pick_width<T>();
+}
+
+// InnerFourStep (src/fourstep.jl:18-113): a length-N lane transform, nested
+// as N = M1*M2 when the lane buffers would outgrow the cache budget.
+template <typename T>
+struct LaneFFT {
+  i64 N, L;
+  int D;
+  bool nested = false;
+  std::vector<Stage<T>> st;    // unnested chain (allow_small = false)
+  i64 M1 = 1, M2 = 1;
+  std::vector<Stage<T>> stA, stB;
+  std::vector<T> twr, twi;     // tw[j1 + M1*k2] = w_N^{j1*k2}
+  LaneFFT(i64 N_, i64 L_, int D_) : N(N_), L(L_), D(D_) {
+    if (4 * L * N * (i64)sizeof(T) > FS_INNER_MAX) {
+      i64 m2 = (i64)1 << (__builtin_ctzll((unsigned long long)N) / 2);
+      if (m2 > 1) {
+        nested = true;
+        M2 = m2; M1 = N / M2;
+        stA = build_stages<T>(M2, D, false);
+        stB = build_stages<T>(M1, D, false);
+        twr.resize(N); twi.resize(N);
+        for (i64 k2 = 0; k2 < M2; ++k2)
+          for (i64 j1 = 0; j1 < M1; ++j1) {
+            double s, c;
+            sincospi((double)(2 * D * j1 * k2) / (double)N, &s, &c);
+            twr[j1 + M1 * k2] = (T)c; twi[j1 + M1 * k2] = (T)s;
+          }
+        return;
+      }
+    }
+    st = build_stages<T>(N, D, false);
+  }
+  // (are, aim): N rows of L lanes (row j at L*j), in natural order; result
+  // in natural order in (are, aim). b*, c*: scratch of N*L each.
+  void run(T* are, T* aim, T* bre, T* bim, T* cre, T* cim) const {
+    if (!nested) {
+      bool sw = run_chain(are, aim, bre, bim, st, 0, st.size(), N, 1, L, D, 1);
+      if (sw) { std::memcpy(are, bre, sizeof(T) * N * L); std::memcpy(aim, bim, sizeof(T) * N * L); }
+      return;
+    }
+    // first transforms over j2 of rows j1 + M1*j2, twiddle, transform over j1
+    for (i64 j1 = 0; j1 < M1; ++j1) {
+      for (i64 j2 = 0; j2 < M2; ++j2)
+        for (i64 l = 0; l < L; ++l) {
+          bre[L * j2 + l] = are[L * (j1 + M1 * j2) + l];
+          bim[L * j2 + l] = aim[L * (j1 + M1 * j2) + l];
+        }
+      bool sw = run_chain(bre, bim, cre, cim, stA, 0, stA.size(), M2, 1, L, D, 1);
+      const T* rr = sw ? cre : bre;
+      const T* ri = sw ? cim : bim;
+      // twiddled rows to slot j1 + M1*k2 (block k2 holds the j1 rows)
+      for (i64 k2 = 0; k2 < M2; ++k2) {
+        T wr = twr[j1 + M1 * k2], wi = twi[j1 + M1 * k2];
+        for (i64 l = 0; l < L; ++l) {
+          T yr = rr[L * k2 + l], yi = ri[L * k2 + l];
+          tmp_re[(size_t)L * (j1 + M1 * k2) + l] = std::fma(yr, wr, -(yi * wi));
+          tmp_im[(size_t)L * (j1 + M1 * k2) + l] = std::fma(yr, wi, yi * wr);
+        }
+      }
+    }
+    // transforms over j1 for each k2; output row k = k2 + M2*k1
+    for (i64 k2 = 0; k2 < M2; ++k2) {
+      T* br = tmp_re.data() + (size_t)L * M1 * k2;
+      T* bi = tmp_im.data() + (size_t)L * M1 * k2;
+      bool sw = run_chain(br, bi, bre, bim, stB, 0, stB.size(), M1, 1, L, D, 1);
+      const T* rr = sw ? bre : br;
+      const T* ri = sw ? bim : bi;
+      for (i64 k1 = 0; k1 < M1; ++k1)
+        for (i64 l = 0; l < L; ++l) {
+          are[L * (k2 + M2 * k1) + l] = rr[L * k1 + l];
+          aim[L * (k2 + M2 * k1) + l] = ri[L * k1 + l];
+        }
+    }
+  }
+  mutable std::vector<T> tmp_re, tmp_im;
+  void alloc_tmp() const {
+    if (nested) { tmp_re.resize((size_t)N * L); tmp_im.resize((size_t)N * L); }
+  }
+};
+
+// FourStepPlan (src/fourstep.jl:130-156, 272-330, 338-495).
+template <typename T>
+struct FourStepPlan : PlanBase {
+  int D;
+  T scale;
+  i64 N1, N2, S, G, Z1, R, K;
+  std::vector<T> b1r, b1i, b2r, b2i, hir, hii, lor, loi;
+  std::vector<T> zre, zim;
+  std::vector<std::unique_ptr<LaneFFT<T>>> innerA, innerB;  // per task
+  std::vector<std::vector<T>> bufs;                          // per task, 6 planes
+  i64 nb;
+  int nt;
+  FourStepPlan(i64 n_, int D_, T scale_, int nthreads, i64 N2req = 0, int width = 0) : D(D_), scale(scale_) {
+    n = n_;
+    route = ORC_FOURSTEP;
+    int W = pick_width<T>();
+    if (!fourstep_split<T>(n, std::max(width, 1), N2req, &N1, &N2))
+      throw std::runtime_error("no four-step split");
+    if (width == 0) width = fs_width<T>(N2, N1);
+    S = G = (i64)width * W;
+    i64 zpad = S;
+    auto om = [&](i64 e, T* c, T* s) {
+      double ss, cc;
+      sincospi((double)(2 * D * e) / (double)n, &ss, &cc);
+      *c = (T)cc; *s = (T)ss;
+    };
+    R = (i64)1 << (__builtin_ctzll((unsigned long long)N2) / 2);
+    i64 ntt = (N2 + R - 1) / R;
+    b1r.resize(S * R); b1i.resize(S * R); b2r.resize(S * ntt); b2i.resize(S * ntt);
+    for (i64 r = 0; r < R; ++r)
+      for (i64 l = 0; l < S; ++l) om(r * l, &b1r[S * r + l], &b1i[S * r + l]);
+    for (i64 t = 0; t < ntt; ++t)
+      for (i64 l = 0; l < S; ++l) om(R * t * l, &b2r[S * t + l], &b2i[S * t + l]);
+    K = isqrt_(n - 1) + 1;
+    i64 nh = (n + K - 1) / K;
+    hir.resize(nh); hii.resize(nh); lor.resize(K); loi.resize(K);
+    for (i64 i = 0; i < nh; ++i) om(i * K, &hir[i], &hii[i]);
+    for (i64 i = 0; i < K; ++i) om(i, &lor[i], &loi[i]);
+    Z1 = N1 + zpad;
+    i64 na = (N1 + S - 1) / S, ng = (N2 + G - 1) / G;
+    nt = (int)std::min<i64>(std::min<i64>(std::max(nthreads, 1), na),
+                            std::min<i64>(ng, std::max<i64>(1, n / FS_TASK_MIN)));
+    for (int i = 0; i < nt; ++i) {
+      innerA.emplace_back(new LaneFFT<T>(N2, S, D));
+      innerB.emplace_back(new LaneFFT<T>(N1, G, D));
+      innerA.back()->alloc_tmp();
+      innerB.back()->alloc_tmp();
+    }
+    nb = std::max(S * N2, G * N1);
+    bufs.resize(nt);
+    for (auto& b : bufs) b.assign(6 * nb, (T)0);
+    i64 nz = Z1 * ng * G;
+    zre.assign(nz, (T)0); zim.assign(nz, (T)0);
+  }
+  // pass A, strips [slo, shi) (src/fourstep.jl:364-428)
+  void pass_a(int ci, const T* x, i64 slo, i64 shi) {
+    T* are = bufs[ci].data();
+    T* aim = are + nb;
+    T* bre = aim + nb;
+    T* bim = bre + nb;
+    T* cre = bim + nb;
+    T* cim = cre + nb;
+    for (i64 sidx = slo; sidx < shi; ++sidx) {
+      i64 c = S * sidx;
+      i64 lim = N1 - c;
+      for (i64 j2 = 0; j2 < N2; ++j2)
+        for (i64 l = 0; l < S; ++l) {
+          if (l < lim) {
+            i64 e = c + N1 * j2 + l;
+            are[S * j2 + l] = x[2 * e]; aim[S * j2 + l] = x[2 * e + 1];
+          } else {
+            are[S * j2 + l] = 0; aim[S * j2 + l] = 0;
+          }
+        }
+      innerA[ci]->run(are, aim, bre, bim, cre, cim);
+      for (i64 k2 = 0; k2 < N2; ++k2) {
+        i64 e = c * k2, hi = e / K, lo = e % K;
+        T ar = hir[hi] * lor[lo] - hii[hi] * loi[lo];
+        T ai = hir[hi] * loi[lo] + hii[hi] * lor[lo];
+        i64 tt = k2 / R, rr = k2 % R;
+        for (i64 l = 0; l < S; ++l) {
+          T b1rv = b1r[S * rr + l], b1iv = b1i[S * rr + l], b2rv = b2r[S * tt + l], b2iv = b2i[S * tt + l];
+          T br = std::fma(b1rv, b2rv, -(b1iv * b2iv));
+          T bi = std::fma(b1rv, b2iv, b1iv * b2rv);
+          T twr = std::fma(ar, br, -(ai * bi));
+          T twi = std::fma(ar, bi, ai * br);
+          T yr = are[S * k2 + l], yi = aim[S * k2 + l];
+          zre[c + Z1 * k2 + l] = std::fma(yr, twr, -(yi * twi));
+          zim[c + Z1 * k2 + l] = std::fma(yr, twi, yi * twr);
+        }
+      }
+    }
+  }
+  // pass B, groups [glo, ghi) (src/fourstep.jl:433-495)
+  void pass_b(int ci, T* y, i64 glo, i64 ghi) {
+    T* are = bufs[ci].data();
+    T* aim = are + nb;
+    T* bre = aim + nb;
+    T* bim = bre + nb;
+    T* cre = bim + nb;
+    T* cim = cre + nb;
+    for (i64 gidx = glo; gidx < ghi; ++gidx) {
+      i64 c2 = G * gidx;
+      i64 lim = N2 - c2;
+      for (i64 g = 0; g < G; ++g) {
+        i64 off = Z1 * (c2 + g);
+        for (i64 j1 = 0; j1 < N1; ++j1) { are[G * j1 + g] = zre[off + j1]; aim[G * j1 + g] = zim[off + j1]; }
+      }
+      innerB[ci]->run(are, aim, bre, bim, cre, cim);
+      for (i64 k1 = 0; k1 < N1; ++k1)
+        for (i64 g = 0; g < G && g < lim; ++g) {
+          i64 e = c2 + N2 * k1 + g;
+          y[2 * e] = are[G * k1 + g] * scale;
+          y[2 * e + 1] = aim[G * k1 + g] * scale;
+        }
+    }
+  }
+  void exec(const void* xv, void* yv) override {
+    const T* x = (const T*)xv;
+    T* y = (T*)yv;
+    i64 na = (N1 + S - 1) / S, ng = (N2 + G - 1) / G;
+    if (nt > 1) {
+      tforeach_chunks(na, nt, 1, [&](int ci, i64 lo, i64 hi) { pass_a(ci, x, lo, hi); });
+      tforeach_chunks(ng, nt, 1, [&](int ci, i64 lo, i64 hi) { pass_b(ci, y, lo, hi); });
+    } else {
+      pass_a(0, x, 0, na);
+      pass_b(0, y, 0, ng);
+    }
+  }
+  void info(std::vector<i64>& v) override {
+    v.push_back(route); v.push_back(n); v.push_back(N1); v.push_back(N2); v.push_back(S);
+    v.push_back(innerA[0]->nested); v.push_back(innerB[0]->nested);
+  }
+};
+
+// ---- resampling (src/resample.jl) -----------------------------------------
+static const int SMOOTH_ODD[7] = {1, 3, 5, 7, 9, 15, 21};
+static int top_set_bit(i64 x) { return x <= 0 ? 0 : 64 - __builtin_clzll((unsigned long long)x); }
+static i64 nextsmooth(i64 N) {  // src/resample.jl:13-21
+  i64 best = INT64_MAX;
+  for (int o : SMOOTH_ODD) {
+    int k = std::max(6, top_set_bit((N + o - 1) / o - 1));
+    i64 c = (i64)o << k;
+    if (c < best) best = c;
+  }
+  return best;
+}
+static i64 nextsmooth7(i64 N) {  // src/resample.jl:25-31
+  i64 m = N;
+  while (!factor_smooth(m)) m++;
+  return m;
+}
+// _gausslegendre (src/resample.jl:33-53)
+static void gausslegendre(int nq, std::vector<double>& z, std::vector<double>& wq) {
+  z.assign(nq, 0); wq.assign(nq, 0);
+  const double eps = 2.220446049250313e-16;
+  for (int i = 1; i <= nq; ++i) {
+    double x = cospi_((i - 0.25) / (nq + 0.5));
+    double dp = 1;
+    for (int it = 0; it < 20; ++it) {
+      double p0 = 1, p1 = x;
+      for (int k = 2; k <= nq; ++k) {
+        double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+        p0 = p1; p1 = p2;
+      }
+      dp = nq * (x * p1 - p0) / (x * x - 1);
+      double dx = p1 / dp;
+      x -= dx;
+      if (std::fabs(dx) < 4 * eps) break;
+    }
+    z[i - 1] = x;
+    wq[i - 1] = 2 / ((1 - x * x) * dp * dp);
+  }
+}
+static inline double es_(double z, double beta) {  // src/resample.jl:55
+  return std::fabs(z) >= 1 ? 0.0 : std::exp(beta * (std::sqrt(1 - z * z) - 1));
+}
+
+// Plan-independent resampling parts (src/resample.jl:202-256), table weights.
+template <typename T>
+struct RsParts {
+  i64 n, m, w, h;
+  double beta;
+  std::vector<T> corr, wt;
+  std::vector<int32_t> l0;
+  RsParts(i64 n_, int D, T scale, i64 m_ = 0) : n(n_) {
+    (void)D;
+    const double epsT = sizeof(T) >= 8 ? 2.220446049250313e-16 : 1.1920928955078125e-07;
+    double tol = 10 * epsT;
+    m = m_ ? m_ : nextsmooth((i64)std::ceil(2.0 * n));
+    double ratio = std::max((double)n / m, 0.5);
+    i64 wc = (i64)std::ceil(std::log(1 / tol) / (M_PI * std::sqrt(1 - ratio)));
+    w = 4 * ((wc + 3) / 4);
+    beta = 0.97 * M_PI * w * (1 - (double)n / (2.0 * m));
+    h = w / 2;
+    std::vector<double> zq, wq;
+    gausslegendre((int)(2 * w + 20), zq, wq);
+    corr.resize(n);
+    i64 hp = (n + 1) / 2;
+    for (i64 j = 0; j < n; ++j) {
+      i64 jp = j < hp ? j : j - n;
+      double nu = (double)jp / m;
+      double Phi = 0;
+      for (size_t q = 0; q < zq.size(); ++q) {
+        if (!(zq[q] > 0)) continue;
+        Phi += wq[q] * es_(zq[q], beta) * cospi_(nu * w * zq[q]);
+      }
+      corr[j] = (T)((double)scale / (w * Phi));
+    }
+    wt.resize(n * w);
+    l0.resize(n);
+    for (i64 k = 0; k < n; ++k) {
+      __int128 km = (__int128)k * m;
+      i64 q = (i64)(km / n), r = (i64)(km % n);
+      l0[k] = (int32_t)(q - h + 1);
+      double delta = (double)r / n;
+      for (i64 i = 0; i < w; ++i) wt[k * w + i] = (T)es_((delta + h - 1 - i) / h, beta);
+    }
+  }
+};
+
+// ResamplePlan (src/resample.jl:175-194, 258-276, 392-424).
+template <typename T>
+struct ResamplePlan : PlanBase {
+  int D;
+  T scale;
+  RsParts<T> parts;
+  std::unique_ptr<FFTPlan<T>> p;
+  ResamplePlan(i64 n_, int D_, T scale_) : D(D_), scale(scale_), parts(n_, D_, scale_) {
+    n = n_;
+    route = ORC_RESAMPLE;
+    p.reset(new FFTPlan<T>(parts.m, D, (T)1, 1));
+  }
+  void exec(const void* xv, void* yv) override {
+    const T* x = (const T*)xv;
+    T* y = (T*)yv;
+    i64 m = parts.m, hp = (n + 1) / 2;
+    T* are = p->are.data();
+    T* aim = p->aim.data();
+    // _deconv! x2 (src/resample.jl:281-301) and zero fill
+    for (i64 c = 0; c < hp; ++c) { are[c] = x[2 * c] * parts.corr[c]; aim[c] = x[2 * c + 1] * parts.corr[c]; }
+    for (i64 c = 0; c < n - hp; ++c) {
+      i64 j = hp + c;
+      are[m - n + hp + c] = x[2 * j] * parts.corr[j];
+      aim[m - n + hp + c] = x[2 * j + 1] * parts.corr[j];
+    }
+    for (i64 j = hp; j < m - n + hp; ++j) { are[j] = 0; aim[j] = 0; }
+    bool sw = run_chain(are, aim, p->bre.data(), p->bim.data(), p->stages, 0, p->stages.size(), m, 1, 1, D, 1);
+    const T* gre = sw ? p->bre.data() : are;
+    const T* gim = sw ? p->bim.data() : aim;
+    // _interp! (src/resample.jl:392-424)
+    i64 w = parts.w;
+    for (i64 k = 0; k < n; ++k) {
+      i64 lk = parts.l0[k];
+      const T* wv = &parts.wt[k * w];
+      T re = 0, im = 0;
+      for (i64 i = 0; i < w; ++i) {
+        i64 l = lk + i;
+        l %= m;
+        if (l < 0) l += m;
+        re += wv[i] * gre[l];
+        im += wv[i] * gim[l];
+      }
+      y[2 * k] = re; y[2 * k + 1] = im;
+    }
+  }
+  void info(std::vector<i64>& v) override {
+    v.push_back(route); v.push_back(n); v.push_back(parts.m); v.push_back(parts.w);
+  }
+};
+
+// _anyplan routing (src/plan.jl:192-206). Composite/split are not restated;
+// HvdH-routed lengths fall back to the resampling restatement.
+template <typename T>
+static PlanBase* anyplan(i64 n, int D, T scale, int nthreads) {
+  if (n < 1) throw std::runtime_error("transform length must be positive");
+  if (!factor_radices(n).ok) return new ResamplePlan<T>(n, D, scale);
+  if (use_ragged<T>(n, nthreads > 1)) return new FourStepPlan<T>(n, D, scale, nthreads);
+  if (slow_smooth<T>(n)) return new ResamplePlan<T>(n, D, scale);
+  if (use_fourstep<T>(n, nthreads > 1 && n >= 2 * FS_TASK_MIN)) return new FourStepPlan<T>(n, D, scale, nthreads);
+  return new FFTPlan<T>(n, D, scale, nthreads);
+}
+
+// ---- real transforms (src/real.jl) ----------------------------------------
+template <typename T>
+struct RfftPlan {
+  i64 n;
+  std::unique_ptr<PlanBase> inner;
+  std::vector<T> twr, twi, buf, buf2;
+  RfftPlan(i64 n_, int nthreads) : n(n_) {
+    bool even = n % 2 == 0;
+    i64 len = even ? n / 2 : n;
+    inner.reset(anyplan<T>(len, -1, (T)1, nthreads));
+    if (even) {
+      twr.resize(len + 1); twi.resize(len + 1);
+      for (i64 k = 0; k <= len; ++k) {  // real_twiddles (src/real.jl:26-39)
+        double s, c;
+        sincospi(-1 * ((double)(2 * k) / n), &s, &c);
+        twr[k] = (T)c; twi[k] = (T)s;
+      }
+    }
+    buf.resize(2 * len);
+    buf2.resize(even ? 0 : 2 * n);
+  }
+  void exec(const T* x, T* y) {  // src/real.jl:80-142
+    if (n % 2 == 0) {
+      i64 h = n / 2;
+      inner->exec(x, buf.data());
+      const T* Z = buf.data();
+      y[0] = Z[0] + Z[1]; y[1] = 0;
+      y[2 * h] = Z[0] - Z[1]; y[2 * h + 1] = 0;
+      const T half = (T)0.5;
+      for (i64 k = 1; k < h; ++k) {
+        T ar = Z[2 * k], ai = Z[2 * k + 1];
+        T br = Z[2 * (h - k)], bi = -Z[2 * (h - k) + 1];
+        T xer = (ar + br) * half, xei = (ai + bi) * half;
+        T xor_ = (ar - br) * half, xoi = (ai - bi) * half;
+        T wr = twr[k], wi = twi[k];
+        y[2 * k] = xer + std::fma(wr, xoi, wi * xor_);
+        y[2 * k + 1] = xei + std::fma(wi, xoi, -(wr * xor_));
+      }
+    } else {
+      for (i64 j = 0; j < n; ++j) { buf[2 * j] = x[j]; buf[2 * j + 1] = 0; }
+      inner->exec(buf.data(), buf2.data());
+      std::memcpy(y, buf2.data(), sizeof(T) * 2 * (n / 2 + 1));
+    }
+  }
+};
+
+template <typename T>
+struct IrfftPlan {
+  i64 n;
+  T pre;
+  std::unique_ptr<PlanBase> inner;
+  std::vector<T> twr, twi, buf, buf2;
+  IrfftPlan(i64 n_, bool normalized, int nthreads) : n(n_) {
+    pre = normalized ? (T)0.5 : (T)1;
+    bool even = n % 2 == 0;
+    i64 len = even ? n / 2 : n;
+    inner.reset(anyplan<T>(len, +1, normalized ? default_scale<T>(len, +1) : (T)1, nthreads));
+    if (even) {
+      twr.resize(len); twi.resize(len);
+      for (i64 k = 0; k < len; ++k) {
+        double s, c;
+        sincospi(+1 * ((double)(2 * k) / n), &s, &c);
+        twr[k] = (T)c; twi[k] = (T)s;
+      }
+    }
+    buf.resize(2 * len);
+    buf2.resize(even ? 0 : 2 * n);
+  }
+  void exec(const T* X, T* y) {  // src/real.jl:144-211
+    if (n % 2 == 0) {
+      i64 h = n / 2;
+      T* Z = buf.data();
+      for (i64 k = 0; k < h; ++k) {
+        T ar = X[2 * k], ai = X[2 * k + 1];
+        T br = X[2 * (h - k)], bi = -X[2 * (h - k) + 1];
+        T xer = (ar + br) * pre, xei = (ai + bi) * pre;
+        T xdr = (ar - br) * pre, xdi = (ai - bi) * pre;
+        T wr = twr[k], wi = twi[k];
+        T tr = std::fma(wr, xdr, -(wi * xdi));
+        T ti = std::fma(wr, xdi, wi * xdr);
+        Z[2 * k] = xer - ti;
+        Z[2 * k + 1] = xei + tr;
+      }
+      inner->exec(Z, y);
+    } else {
+      i64 h = n / 2;
+      T* b = buf.data();
+      for (i64 k = 0; k <= h; ++k) { b[2 * k] = X[2 * k]; b[2 * k + 1] = X[2 * k + 1]; }
+      for (i64 k = 1; k <= h; ++k) { b[2 * (n - k)] = X[2 * k]; b[2 * (n - k) + 1] = -X[2 * k + 1]; }
+      inner->exec(b, buf2.data());
+      for (i64 j = 0; j < n; ++j) y[j] = buf2[2 * j];
+    }
+  }
+};
+
+// ---- N-d (src/ndplan.jl) ---------------------------------------------------
+// Batched resampling along one dim (RsPass, src/resample.jl:434-588).
+template <typename T>
+struct RsPass {
+  i64 n, m, w, B;
+  RsParts<T> parts;
+  std::vector<Stage<T>> stages;
+  RsPass(i64 n_, int D, i64 B_) : n(n_), B(B_), parts(n_, D, (T)1, nextsmooth7(2 * n_)) {
+    m = parts.m; w = parts.w;
+    stages = build_stages<T>(m, D, B == 1);
+  }
+  // rows of B lanes at xre/xim + off (row j lane i at off + B*j + i), in place
+  void run(T* xre, T* xim, i64 off, int D) {
+    std::vector<T> pre(m * B), pim(m * B), qre(m * B), qim(m * B);
+    i64 hp = (n + 1) / 2;
+    for (i64 j = 0; j < n; ++j) {
+      i64 jj = j < hp ? j : m - n + j;
+      T c = parts.corr[j];
+      for (i64 i = 0; i < B; ++i) { pre[B * jj + i] = xre[off + B * j + i] * c; pim[B * jj + i] = xim[off + B * j + i] * c; }
+    }
+    for (i64 j = hp; j < m - n + hp; ++j)
+      for (i64 i = 0; i < B; ++i) { pre[B * j + i] = 0; pim[B * j + i] = 0; }
+    bool sw = run_chain(pre.data(), pim.data(), qre.data(), qim.data(), stages, 0, stages.size(), m, 1, B, D, 1);
+    const T* gre = sw ? qre.data() : pre.data();
+    const T* gim = sw ? qim.data() : pim.data();
+    for (i64 k = 0; k < n; ++k) {
+      i64 l = parts.l0[k];
+      for (i64 i = 0; i < B; ++i) {
+        T ar = 0, ai = 0;
+        for (i64 t = 0; t < w; ++t) {
+          i64 g = l + t;
+          if (g < 0) g += m;
+          if (g >= m) g -= m;
+          ar = std::fma(parts.wt[w * k + t], gre[B * g + i], ar);
+          ai = std::fma(parts.wt[w * k + t], gim[B * g + i], ai);
+        }
+        xre[off + B * k + i] = ar;
+        xim[off + B * k + i] = ai;
+      }
+    }
+  }
+};
+
+template <typename T>
+struct DimPass {
+  i64 nd, Bi, Bo;
+  std::vector<Stage<T>> stages;
+  std::unique_ptr<RsPass<T>> fb;
+};
+
+template <typename T>
+struct NdPlan : PlanBase {
+  int D;
+  T scale;
+  std::vector<i64> dims;
+  i64 len;
+  int nt;
+  std::vector<std::unique_ptr<DimPass<T>>> passes;
+  std::vector<T> are, aim, bre, bim;
+  // _ndplan (src/ndplan.jl:57-118); dims before first_dim are pure batch
+  NdPlan(const std::vector<i64>& dims_, int D_, T scale_, int nthreads, int first_dim = 0)
+      : D(D_), scale(scale_), dims(dims_) {
+    route = -1;
+    len = 1;
+    for (i64 d : dims) { if (d < 1) throw std::runtime_error("dimensions must be positive"); len *= d; }
+    n = len;
+    nt = plan_tasks(len, nthreads);
+    int W = pick_width<T>();
+    for (size_t d = first_dim; d < dims.size(); ++d) {
+      i64 nd = dims[d];
+      if (nd == 1) continue;
+      i64 Bi = 1, Bo = 1;
+      for (size_t e = 0; e < d; ++e) Bi *= dims[e];
+      for (size_t e = d + 1; e < dims.size(); ++e) Bo *= dims[e];
+      std::unique_ptr<DimPass<T>> ps(new DimPass<T>());
+      ps->nd = nd; ps->Bi = Bi; ps->Bo = Bo;
+      if (factor_radices(nd).ok) {
+        ps->stages = build_stages<T>(nd, D, Bi == 1);
+        (void)W;
+      } else {
+        ps->fb.reset(new RsPass<T>(nd, D, Bi == 1 ? Bo : Bi));
+      }
+      passes.push_back(std::move(ps));
+    }
+    are.resize(len); aim.resize(len); bre.resize(len); bim.resize(len);
+  }
+  // split planes in (cre, cim); returns the plane pair holding the result
+  void core(T*& cre, T*& cim, T*& ore, T*& oim) {
+    for (auto& pp : passes) {
+      DimPass<T>& ps = *pp;
+      if (ps.fb) {
+        if (ps.Bi == 1 && ps.Bo > 1) {
+          // dim 1: transpose so pencils become lanes (src/ndplan.jl:137-151)
+          for (i64 o = 0; o < ps.Bo; ++o)
+            for (i64 j = 0; j < ps.nd; ++j) { ore[ps.Bo * j + o] = cre[ps.nd * o + j]; oim[ps.Bo * j + o] = cim[ps.nd * o + j]; }
+          ps.fb->run(ore, oim, 0, D);
+          for (i64 o = 0; o < ps.Bo; ++o)
+            for (i64 j = 0; j < ps.nd; ++j) { cre[ps.nd * o + j] = ore[ps.Bo * j + o]; cim[ps.nd * o + j] = oim[ps.Bo * j + o]; }
+        } else {
+          for (i64 o = 0; o < ps.Bo; ++o) ps.fb->run(cre, cim, o * ps.Bi * ps.nd, D);
+        }
+        continue;
+      }
+      i64 block = ps.Bi * ps.nd;
+      bool sw = false;
+      for (i64 o = 0; o < ps.Bo; ++o)
+        sw = run_chain(cre + o * block, cim + o * block, ore + o * block, oim + o * block, ps.stages, 0,
+                       ps.stages.size(), ps.nd, 1, ps.Bi, D, nt);
+      if (sw) { std::swap(cre, ore); std::swap(cim, oim); }
+    }
+  }
+  void exec(const void* xv, void* yv) override {
+    const T* x = (const T*)xv;
+    T* y = (T*)yv;
+    T *cre = are.data(), *cim = aim.data(), *ore = bre.data(), *oim = bim.data();
+    for (i64 c = 0; c < len; ++c) { cre[c] = x[2 * c]; cim[c] = x[2 * c + 1]; }
+    core(cre, cim, ore, oim);
+    for (i64 c = 0; c < len; ++c) { y[2 * c] = cre[c] * scale; y[2 * c + 1] = cim[c] * scale; }
+  }
+};
+
+// RfftNdPlan / IrfftNdPlan (src/ndplan.jl:355-519), per-pencil real edge.
+template <typename T>
+struct RfftNd {
+  std::vector<i64> rdims, cdims;
+  i64 B;
+  std::unique_ptr<RfftPlan<T>> r1;
+  std::unique_ptr<NdPlan<T>> rest;
+  std::vector<T> C;
+  RfftNd(const std::vector<i64>& dims, int nthreads) : rdims(dims) {
+    cdims = dims;
+    cdims[0] = dims[0] / 2 + 1;
+    B = 1;
+    for (size_t d = 1; d < dims.size(); ++d) B *= dims[d];
+    r1.reset(new RfftPlan<T>(dims[0], nthreads));
+    rest.reset(new NdPlan<T>(cdims, -1, (T)1, nthreads, 1));
+    C.resize(2 * cdims[0] * B);
+  }
+  void exec(const T* X, T* Y) {
+    i64 n1 = rdims[0], h1p = cdims[0];
+    for (i64 o = 0; o < B; ++o) r1->exec(X + o * n1, C.data() + 2 * o * h1p);
+    rest->exec(C.data(), Y);
+  }
+};
+template <typename T>
+struct IrfftNd {
+  std::vector<i64> rdims, cdims;
+  i64 B;
+  std::unique_ptr<IrfftPlan<T>> r1;
+  std::unique_ptr<NdPlan<T>> rest;
+  std::vector<T> C;
+  IrfftNd(const std::vector<i64>& dims, bool normalized, int nthreads) : rdims(dims) {
+    cdims = dims;
+    cdims[0] = dims[0] / 2 + 1;
+    B = 1;
+    for (size_t d = 1; d < dims.size(); ++d) B *= dims[d];
+    T restscale = normalized ? (T)1 / (T)B : (T)1;
+    r1.reset(new IrfftPlan<T>(dims[0], normalized, nthreads));
+    rest.reset(new NdPlan<T>(cdims, +1, restscale, nthreads, 1));
+    C.resize(2 * cdims[0] * B);
+  }
+  void exec(const T* X, T* y) {
+    i64 n1 = rdims[0], h1p = cdims[0];
+    rest->exec(X, C.data());
+    for (i64 o = 0; o < B; ++o) r1->exec(C.data() + 2 * o * h1p, y + o * n1);
+  }
+};
+
+// ---- FP64 direct DFT with double-double accumulation -----------------------
+static inline void two_sum(double a, double b, double* s, double* e) {
+  *s = a + b;
+  double bb = *s - a;
+  *e = (a - (*s - bb)) + (b - bb);
+}
+static void dft_f64(i64 n, const double* x, double* y, int sign) {
+  std::vector<double> cr(n), ci(n);
+  for (i64 k = 0; k < n; ++k) {
+    double s, c;
+    sincospi((double)(2 * k) / (double)n, &s, &c);
+    cr[k] = c; ci[k] = sign * s;
+  }
+  for (i64 k = 0; k < n; ++k) {
+    double sr = 0, er = 0, si = 0, ei = 0;
+    for (i64 j = 0; j < n; ++j) {
+      i64 e = (i64)(((__int128)j * k) % n);
+      double wr = cr[e], wi = ci[e];
+      double xr = x[2 * j], xi = x[2 * j + 1];
+      // products with their rounding errors (fma), then compensated sums
+      double p1 = wr * xr, p1e = std::fma(wr, xr, -p1);
+      double p2 = -(wi * xi), p2e = -std::fma(wi, xi, -(wi * xi));
+      double p3 = wr * xi, p3e = std::fma(wr, xi, -p3);
+      double p4 = wi * xr, p4e = std::fma(wi, xr, -p4);
+      double t, te;
+      two_sum(sr, p1, &t, &te); sr = t; er += te + p1e;
+      two_sum(sr, p2, &t, &te); sr = t; er += te + p2e;
+      two_sum(si, p3, &t, &te); si = t; ei += te + p3e;
+      two_sum(si, p4, &t, &te); si = t; ei += te + p4e;
+    }
+    y[2 * k] = sr + er;
+    y[2 * k + 1] = si + ei;
+  }
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+// ---------------------------------------------------------------------------
+// C ABI of the oracle.
+namespace {
+struct Handle {
+  int dtype = 0;
+  int kind = 0;  // 0 c2c, 1 rfft, 2 irfft, 3 nd, 4 rfft nd, 5 irfft nd
+  std::unique_ptr<PlanBase> p32, p64;
+  std::unique_ptr<RfftPlan<float>> r32;
+  std::unique_ptr<RfftPlan<double>> r64;
+  std::unique_ptr<IrfftPlan<float>> i32;
+  std::unique_ptr<IrfftPlan<double>> i64_;
+  std::unique_ptr<RfftNd<float>> rn32;
+  std::unique_ptr<RfftNd<double>> rn64;
+  std::unique_ptr<IrfftNd<float>> in32;
+  std::unique_ptr<IrfftNd<double>> in64;
+  int64_t n = 0, nin = 0, nout = 0;  // element counts (T) per transform
+};
+}  // namespace
+
+extern "C" {
+
+void orc_set_vector_bits(int bits) { g_vector_bits = bits; }
+int orc_get_vector_bits(void) { return g_vector_bits; }
+int orc_max_threads(void) { return Pool::get().size(); }
+
+void* orc_plan_c2c(int dtype, int64_t n, int D, int scale_mode, int nthreads) {
+  try {
+    Handle* h = new Handle();
+    h->dtype = dtype; h->kind = 0; h->n = n; h->nin = 2 * n; h->nout = 2 * n;
+    if (dtype == 0) h->p32.reset(anyplan<float>(n, D, scale_mode ? 1.0f : default_scale<float>(n, D), nthreads));
+    else h->p64.reset(anyplan<double>(n, D, scale_mode ? 1.0 : default_scale<double>(n, D), nthreads));
+    return h;
+  } catch (...) { return nullptr; }
+}
+int orc_plan_route(void* p) {
+  Handle* h = (Handle*)p;
+  return h->dtype == 0 ? h->p32->route : h->p64->route;
+}
+int64_t orc_plan_info(void* p, int64_t* out, int64_t cap) {
+  Handle* h = (Handle*)p;
+  std::vector<i64> v;
+  if (h->dtype == 0) h->p32->info(v); else h->p64->info(v);
+  for (int64_t i = 0; i < (int64_t)v.size() && i < cap; ++i) out[i] = v[i];
+  return (int64_t)v.size();
+}
+int orc_execute_c2c(void* p, const void* x, void* y, int64_t batch) {
+  Handle* h = (Handle*)p;
+  for (int64_t b = 0; b < batch; ++b) {
+    if (h->dtype == 0) h->p32->exec((const float*)x + b * h->nin, (float*)y + b * h->nout);
+    else h->p64->exec((const double*)x + b * h->nin, (double*)y + b * h->nout);
+  }
+  return 0;
+}
+void orc_destroy(void* p) { delete (Handle*)p; }
+
+void* orc_plan_rfft(int dtype, int64_t n, int nthreads) {
+  try {
+    Handle* h = new Handle();
+    h->dtype = dtype; h->kind = 1; h->n = n; h->nin = n; h->nout = 2 * (n / 2 + 1);
+    if (dtype == 0) h->r32.reset(new RfftPlan<float>(n, nthreads));
+    else h->r64.reset(new RfftPlan<double>(n, nthreads));
+    return h;
+  } catch (...) { return nullptr; }
+}
+void* orc_plan_irfft(int dtype, int64_t n, int normalized, int nthreads) {
+  try {
+    Handle* h = new Handle();
+    h->dtype = dtype; h->kind = 2; h->n = n; h->nin = 2 * (n / 2 + 1); h->nout = n;
+    if (dtype == 0) h->i32.reset(new IrfftPlan<float>(n, normalized != 0, nthreads));
+    else h->i64_.reset(new IrfftPlan<double>(n, normalized != 0, nthreads));
+    return h;
+  } catch (...) { return nullptr; }
+}
+int orc_execute_rfft(void* p, const void* x, void* y, int64_t batch) {
+  Handle* h = (Handle*)p;
+  for (int64_t b = 0; b < batch; ++b) {
+    if (h->dtype == 0) h->r32->exec((const float*)x + b * h->nin, (float*)y + b * h->nout);
+    else h->r64->exec((const double*)x + b * h->nin, (double*)y + b * h->nout);
+  }
+  return 0;
+}
+int orc_execute_irfft(void* p, const void* x, void* y, int64_t batch) {
+  Handle* h = (Handle*)p;
+  for (int64_t b = 0; b < batch; ++b) {
+    if (h->dtype == 0) h->i32->exec((const float*)x + b * h->nin, (float*)y + b * h->nout);
+    else h->i64_->exec((const double*)x + b * h->nin, (double*)y + b * h->nout);
+  }
+  return 0;
+}
+
+void* orc_plan_nd(int dtype, int rank, const int64_t* dims, int kind, int nthreads) {
+  try {
+    std::vector<i64> d(dims, dims + rank);
+    i64 len = 1;
+    for (i64 v : d) len *= v;
+    Handle* h = new Handle();
+    h->dtype = dtype; h->kind = 3; h->n = len;
+    int D = kind == 0 ? -1 : +1;
+    if (dtype == 0) h->p32.reset(new NdPlan<float>(d, D, kind == 1 ? 1.0f / (float)len : 1.0f, nthreads));
+    else h->p64.reset(new NdPlan<double>(d, D, kind == 1 ? 1.0 / (double)len : 1.0, nthreads));
+    return h;
+  } catch (...) { return nullptr; }
+}
+int orc_execute_nd(void* p, const void* x, void* y) {
+  Handle* h = (Handle*)p;
+  if (h->dtype == 0) h->p32->exec(x, y); else h->p64->exec(x, y);
+  return 0;
+}
+void* orc_plan_rfft_nd(int dtype, int rank, const int64_t* dims, int nthreads) {
+  try {
+    std::vector<i64> d(dims, dims + rank);
+    Handle* h = new Handle();
+    h->dtype = dtype; h->kind = 4;
+    if (dtype == 0) h->rn32.reset(new RfftNd<float>(d, nthreads));
+    else h->rn64.reset(new RfftNd<double>(d, nthreads));
+    return h;
+  } catch (...) { return nullptr; }
+}
+void* orc_plan_irfft_nd(int dtype, int rank, const int64_t* dims, int normalized, int nthreads) {
+  try {
+    std::vector<i64> d(dims, dims + rank);
+    Handle* h = new Handle();
+    h->dtype = dtype; h->kind = 5;
+    if (dtype == 0) h->in32.reset(new IrfftNd<float>(d, normalized != 0, nthreads));
+    else h->in64.reset(new IrfftNd<double>(d, normalized != 0, nthreads));
+    return h;
+  } catch (...) { return nullptr; }
+}
+int orc_execute_rfft_nd(void* p, const void* x, void* y) {
+  Handle* h = (Handle*)p;
+  if (h->dtype == 0) h->rn32->exec((const float*)x, (float*)y); else h->rn64->exec((const double*)x, (double*)y);
+  return 0;
+}
+int orc_execute_irfft_nd(void* p, const void* x, void* y) {
+  Handle* h = (Handle*)p;
+  if (h->dtype == 0) h->in32->exec((const float*)x, (float*)y); else h->in64->exec((const double*)x, (double*)y);
+  return 0;
+}
+
+void orc_dft_f64(int64_t n, const double* x, double* y, int sign) { dft_f64(n, x, y, sign); }
+
+int orc_factor_radices(int64_t n, int64_t* a, int64_t* primes, int64_t* counts, int64_t cap) {
+  Fac f = factor_radices(n);
+  if (!f.ok) return -1;
+  *a = f.a;
+  int64_t k = 0;
+  for (auto& pc : f.ps) { if (k < cap) { primes[k] = pc.first; counts[k] = pc.second; } k++; }
+  return (int)k;
+}
+int64_t orc_nextsmooth(int64_t n) { return nextsmooth(n); }
+int64_t orc_nextsmooth7(int64_t n) { return nextsmooth7(n); }
+int64_t orc_resample_params(int dtype, int64_t n, int64_t* w, double* beta) {
+  if (dtype == 0) { RsParts<float> p(n, -1, 1.0f); *w = p.w; *beta = p.beta; return p.m; }
+  RsParts<double> p(n, -1, 1.0); *w = p.w; *beta = p.beta; return p.m;
+}
+}

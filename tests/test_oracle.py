@@ -1,0 +1,144 @@
+"""The oracle (CPU restatement of FFTJ.jl) pinned against the golden vectors,
+an FP64 direct DFT and the reference test suite's identities and routing.
+CPU only."""
+import numpy as np
+import pytest
+
+from conftest import EPS, rel_l2
+
+# tolerance classes of test/runtests.jl: 50 eps (smooth, four-step), 100 eps
+# (resampling, real), 200 eps (N-d)
+T_LIST = [np.float32, np.float64]
+
+
+def _golden_sizes(golden, prefix):
+    return sorted(int(k[len(prefix):]) for k in golden.files if k.startswith(prefix))
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_c2c_matches_golden(golden, orc, T):
+    for n in _golden_sizes(golden, "c2c_x_"):
+        x = golden["c2c_x_%d" % n]
+        ref = golden["c2c_y_%d" % n]
+        p = orc.Plan1D(T, n, "fft")
+        y = p(x)
+        k = 100 if p.route == "ResamplePlan" else 50
+        assert rel_l2(y, ref) <= k * EPS[T], (n, p.route, rel_l2(y, ref) / EPS[T])
+        # round trip (runtests.jl:23) and bfft = n * ifft (runtests.jl:76)
+        xi = orc.Plan1D(T, n, "ifft")(y)
+        assert rel_l2(xi, x) <= 2 * k * EPS[T], n
+        xb = orc.Plan1D(T, n, "bfft")(ref.astype(np.complex128))
+        assert rel_l2(xb, n * x) <= 2 * k * EPS[T], n
+
+
+def test_direct_dft_matches_golden(golden, orc):
+    for n in _golden_sizes(golden, "c2c_x_"):
+        if n > 1100:
+            continue
+        x = golden["c2c_x_%d" % n]
+        assert rel_l2(orc.dft_f64(x), golden["c2c_y_%d" % n]) <= 4 * EPS[np.float64], n
+
+
+def test_known_answers(golden, orc):
+    for key in golden.files:
+        if not key.startswith("kat_"):
+            continue
+        n = int(key.rsplit("_", 1)[1])
+        x = golden[key]
+        for T in T_LIST:
+            y = orc.Plan1D(T, n, "fft")(x)
+            if "impulse" in key:
+                assert np.allclose(y, np.ones(n), atol=10 * EPS[T])
+            elif n > 3:
+                exp = np.zeros(n, dtype=np.complex128)
+                exp[3] = n
+                assert rel_l2(y, exp) <= 50 * EPS[T] * max(np.log2(n), 1), key
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_rfft_matches_golden(golden, orc, T):
+    for n in _golden_sizes(golden, "r2c_x_"):
+        x = golden["r2c_x_%d" % n]
+        ref = golden["r2c_y_%d" % n]
+        y = orc.PlanReal(T, n, "rfft")(x)
+        assert y.shape == (n // 2 + 1,)
+        assert rel_l2(y, ref) <= 100 * EPS[T], n
+        xr = orc.PlanReal(T, n, "irfft")(ref)
+        assert rel_l2(xr, x) <= 100 * EPS[T], n
+        xb = orc.PlanReal(T, n, "brfft")(ref)
+        assert rel_l2(xb, n * x) <= 100 * EPS[T], n
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_nd_matches_golden(golden, orc, T):
+    for key in golden.files:
+        if not key.startswith("nd_x_"):
+            continue
+        dims = [int(v) for v in key[5:].split("x")]
+        x = golden[key]
+        ref = golden["nd_y_" + key[5:]]
+        y = orc.PlanND(T, dims, "fft")(x)
+        assert rel_l2(y, ref) <= 200 * EPS[T], dims
+        assert rel_l2(orc.PlanND(T, dims, "ifft")(ref), x) <= 200 * EPS[T], dims
+        xr = golden["ndr_x_" + key[5:]]
+        rref = golden["ndr_y_" + key[5:]]
+        Y = orc.PlanND(T, dims, "rfft")(xr)
+        assert Y.shape == rref.shape and rel_l2(Y, rref) <= 200 * EPS[T], dims
+        assert rel_l2(orc.PlanND(T, dims, "irfft")(rref), xr) <= 200 * EPS[T], dims
+        assert rel_l2(orc.PlanND(T, dims, "brfft")(rref), np.prod(dims) * xr) <= 200 * EPS[T], dims
+
+
+def test_routing_matches_reference_table(orc):
+    """Plan types asserted by the reference's routing tests
+    (test/runtests.jl:391-419). Those assertions hold for a 512-bit (AVX-512)
+    host only (e.g. F32 40000 threaded is four-step only when W = 16), so the
+    oracle is pinned at 512 bits here; the config splits below hold on the
+    128-bit NEON host of the GPU machine as well."""
+    orc.set_vector_bits(512)
+    r = lambda T, n, nt=1: orc.Plan1D(T, n, "fft", nthreads=nt).route
+    for n in (405, 11 * 1024, 4000):
+        assert r(np.float64, n) == "FFTPlan"
+    assert r(np.float32, 8000) == "FFTPlan"
+    for n in (2835, 3 ** 8, 2 * 3 ** 6 * 5 ** 2 * 7 ** 2, 13 ** 3):
+        assert r(np.float64, n) == "FourStepPlan", n
+    assert r(np.float64, 12000) == "FFTPlan"
+    assert r(np.float32, 40000) == "FFTPlan"
+    assert r(np.float32, 40000, 4) == "FourStepPlan"
+    assert r(np.float64, 2 ** 17) == "FFTPlan"
+    assert r(np.float64, 2 ** 18) == "FourStepPlan"
+    assert r(np.float64, 2 ** 15, 4) == "FourStepPlan"
+    assert r(np.float64, 2 ** 14, 4) == "FFTPlan"
+    assert r(np.float64, 10006) == "ResamplePlan"
+    assert r(np.float32, 10007) == "ResamplePlan"
+    assert r(np.float32, 729) == "ResamplePlan"
+    assert r(np.float32, 2187) == "FourStepPlan"
+    assert r(np.float32, 3 ** 12) == "FourStepPlan"
+    # the config sizes (four-step splits of the reference's planner)
+    orc.set_vector_bits(128)
+    assert orc.Plan1D(np.float32, 42525, "fft").info()[2:4] == [225, 189]
+    assert orc.Plan1D(np.float64, 2 ** 18, "fft").info()[2:4] == [512, 512]
+    m, w, _ = orc.resample_params(np.float32, 10007)
+    assert (m, w) == (20480, 8)
+    m, w, _ = orc.resample_params(np.float64, 10007)
+    assert (m, w) == (20480, 16)
+    orc.set_vector_bits(512)
+    assert orc.Plan1D(np.float32, 42525, "fft").info()[2:4] == [225, 189]
+    orc.set_vector_bits(128)
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_threaded_bitwise_serial(orc, T):
+    """test/threading.jl: threaded plans are bitwise equal to serial ones of
+    the same algorithm (deterministic tforeach chunking)."""
+    rng = np.random.default_rng(5)
+    for n in (2 ** 17, 3 * 2 ** 16, 42525):
+        x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        p4 = orc.Plan1D(T, n, "fft", nthreads=4)
+        info = p4.info()
+        y4 = p4(x)
+        if p4.route == "FourStepPlan":
+            # same split, one task: the serial plan of FFTJ's _serial_copy
+            y1 = orc.Plan1D(T, n, "fft", nthreads=1)(x)
+            if orc.Plan1D(T, n, "fft", nthreads=1).info()[2:4] == info[2:4]:
+                assert np.array_equal(y1, y4), n
+        assert rel_l2(y4, np.fft.fft(x)) <= 50 * EPS[T]
