@@ -72,6 +72,10 @@ struct PassParams {
   double scale;            // applied on store when != 1
   int smem_elems;          // padded elements per buffer
   int threads;
+  int Tf;                  // threads per tile column (threads = NB * Tf)
+  int ept;                 // elements per thread per column (ceil(R / Tf))
+  int load_rows;           // 1: lanes walk j (contiguous input rows), 0: lanes walk columns
+  int store_rows;          // 1: lanes walk j (contiguous output rows), 0: lanes walk columns
   // fused load op parameters
   int load_op;
   int64_t ld_n, ld_m, ld_hp;     // DECONV: n, m, ceil(n/2); C2R_PRE: h = ld_n
@@ -101,8 +105,21 @@ struct CopyParams {
   int64_t nc;  // complex length per batch (mode 1/3)
 };
 
+// A pass kernel specialised at compile time for one radix sequence.
+struct RecipeEntry {
+  int f64, dir, load_op;
+  int mode;      // 0 row load + row store, 1 fused load + row store, 2 fused both
+  int radix[6];  // zero-terminated
+  int Tf;        // threads per tile column the kernel was built for
+  const void* fn;
+};
+template <typename T, int DIR>
+const RecipeEntry* recipe_table(int* count);
+
+// fn: a recipe kernel (RecipeEntry::fn) or nullptr for the generic kernel.
 template <typename T>
-cudaError_t launch_pass(const PassParams& pp, int dir, const void* in, void* out, cudaStream_t st);
+cudaError_t launch_pass(const PassParams& pp, int dir, const void* fn, const void* in, void* out,
+                        cudaStream_t st);
 template <typename T>
 cudaError_t launch_interp(const InterpParams& ip, const void* g, void* y, cudaStream_t st);
 template <typename T>
@@ -111,6 +128,6 @@ template <typename T>
 cudaError_t launch_copy(const CopyParams& cp, const void* in, void* out, cudaStream_t st);
 // Opt a pass configuration into the dynamic shared memory it needs.
 template <typename T>
-cudaError_t prepare_pass(const PassParams& pp, int dir);
+cudaError_t prepare_pass(const PassParams& pp, int dir, const void* fn);
 
 }  // namespace fftj

@@ -1,0 +1,769 @@
+// Device building blocks of the pass kernels, shared by kernels.cu (the
+// generic pass) and recipes.cu (passes specialised at compile time).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "bfly_consts.h"
+#include "fftj_internal.h"
+
+namespace fftj {
+
+template <typename T>
+struct CT;
+template <>
+struct CT<float> { using t = float2; };
+template <>
+struct CT<double> { using t = double2; };
+
+template <typename T>
+using Cx = typename CT<T>::t;
+
+template <typename T>
+__device__ __forceinline__ Cx<T> mk(T x, T y) { Cx<T> c; c.x = x; c.y = y; return c; }
+template <typename C>
+__device__ __forceinline__ C add(C a, C b) { C c; c.x = a.x + b.x; c.y = a.y + b.y; return c; }
+template <typename C>
+__device__ __forceinline__ C sub(C a, C b) { C c; c.x = a.x - b.x; c.y = a.y - b.y; return c; }
+// a * w (complex)
+template <typename C>
+__device__ __forceinline__ C cmul(C a, C w) {
+  C c;
+  c.x = fma(w.x, a.x, -(w.y * a.y));
+  c.y = fma(w.x, a.y, w.y * a.x);
+  return c;
+}
+// (DIR * i) * z
+template <int DIR, typename C>
+__device__ __forceinline__ C mul_di(C z) {
+  C c;
+  if (DIR < 0) { c.x = z.y; c.y = -z.x; } else { c.x = -z.y; c.y = z.x; }
+  return c;
+}
+
+// Shared-memory padding: one element per 16 (8-byte) or 8 (16-byte) elements,
+// so power-of-two strides spread over the banks.
+template <typename T>
+__device__ __forceinline__ int pidx(int i) { return i + (i >> (sizeof(T) == 4 ? 4 : 3)); }
+
+// ---------------------------------------------------------------------------
+// Register DFTs (FFTJ src/kernels.jl:93-239: bf2, bf4_core, bf8_core, bfp).
+template <typename T, int DIR>
+__device__ __forceinline__ void dft4(Cx<T>& a, Cx<T>& b, Cx<T>& c, Cx<T>& d) {
+  Cx<T> apc = add(a, c), amc = sub(a, c), bpd = add(b, d), bmd = mul_di<DIR>(sub(b, d));
+  a = add(apc, bpd);
+  c = sub(apc, bpd);
+  b = add(amc, bmd);
+  d = sub(amc, bmd);
+}
+
+template <typename T, int DIR, int R>
+struct Dft;
+
+template <typename T, int DIR>
+struct Dft<T, DIR, 2> {
+  __device__ __forceinline__ static void run(Cx<T>* v) {
+    Cx<T> a = v[0];
+    v[0] = add(a, v[1]);
+    v[1] = sub(a, v[1]);
+  }
+};
+template <typename T, int DIR>
+struct Dft<T, DIR, 4> {
+  __device__ __forceinline__ static void run(Cx<T>* v) { dft4<T, DIR>(v[0], v[1], v[2], v[3]); }
+};
+template <typename T, int DIR>
+struct Dft<T, DIR, 8> {
+  __device__ __forceinline__ static void run(Cx<T>* v) {
+    Cx<T> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    Cx<T> o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<T, DIR>(e0, e1, e2, e3);
+    dft4<T, DIR>(o0, o1, o2, o3);
+    const T c = (T)0.70710678118654752440;
+    Cx<T> t1, t3;
+    if (DIR < 0) {
+      t1 = mk<T>(c * (o1.x + o1.y), c * (o1.y - o1.x));
+      t3 = mk<T>(c * (o3.y - o3.x), -c * (o3.x + o3.y));
+    } else {
+      t1 = mk<T>(c * (o1.x - o1.y), c * (o1.y + o1.x));
+      t3 = mk<T>(-c * (o3.x + o3.y), c * (o3.x - o3.y));
+    }
+    Cx<T> t2 = mul_di<DIR>(o2);
+    v[0] = add(e0, o0); v[4] = sub(e0, o0);
+    v[1] = add(e1, t1); v[5] = sub(e1, t1);
+    v[2] = add(e2, t2); v[6] = sub(e2, t2);
+    v[3] = add(e3, t3); v[7] = sub(e3, t3);
+  }
+};
+template <typename T, int DIR>
+struct Dft<T, DIR, 16> {
+  __device__ __forceinline__ static void run(Cx<T>* v) {
+    // 4 x 4: x[4 n1 + n2], X[k1 + 4 k2]
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) dft4<T, DIR>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
+    // now v[4*k1 + n2] holds a_{n2}[k1]; twiddle by w16^(n2*k1)
+#pragma unroll
+    for (int k1 = 1; k1 < 4; ++k1)
+#pragma unroll
+      for (int n2 = 1; n2 < 4; ++n2) {
+        const int t = n2 * k1;
+        Cx<T> w = mk<T>((T)kCos16(t), (T)(DIR * kSin16(t)));
+        v[4 * k1 + n2] = cmul(v[4 * k1 + n2], w);
+      }
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) dft4<T, DIR>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+    // v[4*k1 + k2] holds X[k1 + 4 k2]: transpose to natural order
+    Cx<T> o[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 4; ++k2) o[k1 + 4 * k2] = v[4 * k1 + k2];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = o[i];
+  }
+};
+
+template <int P>
+struct PrimeTab;
+template <>
+struct PrimeTab<3> { __device__ static constexpr double c(int i) { return kCos3(i); } __device__ static constexpr double s(int i) { return kSin3(i); } };
+template <>
+struct PrimeTab<5> { __device__ static constexpr double c(int i) { return kCos5(i); } __device__ static constexpr double s(int i) { return kSin5(i); } };
+template <>
+struct PrimeTab<7> { __device__ static constexpr double c(int i) { return kCos7(i); } __device__ static constexpr double s(int i) { return kSin7(i); } };
+template <>
+struct PrimeTab<11> { __device__ static constexpr double c(int i) { return kCos11(i); } __device__ static constexpr double s(int i) { return kSin11(i); } };
+template <>
+struct PrimeTab<13> { __device__ static constexpr double c(int i) { return kCos13(i); } __device__ static constexpr double s(int i) { return kSin13(i); } };
+
+// odd prime P by conjugate pairs (FFTJ bfp, src/kernels.jl:146-228)
+template <typename T, int DIR, int P>
+struct DftPrime {
+  __device__ __forceinline__ static void run(Cx<T>* v) {
+    constexpr int h = (P - 1) / 2;
+    Cx<T> t[h], d[h];
+#pragma unroll
+    for (int j = 1; j <= h; ++j) {
+      t[j - 1] = add(v[j], v[P - j]);
+      d[j - 1] = sub(v[j], v[P - j]);
+    }
+    Cx<T> x0 = v[0];
+    Cx<T> sum = t[0];
+#pragma unroll
+    for (int j = 2; j <= h; ++j) sum = add(sum, t[j - 1]);
+    v[0] = add(x0, sum);
+#pragma unroll
+    for (int k = 1; k <= h; ++k) {
+      Cx<T> u = x0, w = mk<T>(0, 0);
+#pragma unroll
+      for (int j = h; j >= 1; --j) {
+        const T c = (T)PrimeTab<P>::c((k - 1) * h + j - 1);
+        const T s = (T)(DIR * PrimeTab<P>::s((k - 1) * h + j - 1));
+        u.x = fma(c, t[j - 1].x, u.x);
+        u.y = fma(c, t[j - 1].y, u.y);
+        w.x = fma(s, d[j - 1].x, w.x);
+        w.y = fma(s, d[j - 1].y, w.y);
+      }
+      v[k] = mk<T>(u.x - w.y, u.y + w.x);      // u + i w
+      v[P - k] = mk<T>(u.x + w.y, u.y - w.x);  // u - i w
+    }
+  }
+};
+template <typename T, int DIR>
+struct Dft<T, DIR, 3> { __device__ __forceinline__ static void run(Cx<T>* v) { DftPrime<T, DIR, 3>::run(v); } };
+template <typename T, int DIR>
+struct Dft<T, DIR, 5> { __device__ __forceinline__ static void run(Cx<T>* v) { DftPrime<T, DIR, 5>::run(v); } };
+template <typename T, int DIR>
+struct Dft<T, DIR, 7> { __device__ __forceinline__ static void run(Cx<T>* v) { DftPrime<T, DIR, 7>::run(v); } };
+template <typename T, int DIR>
+struct Dft<T, DIR, 11> { __device__ __forceinline__ static void run(Cx<T>* v) { DftPrime<T, DIR, 11>::run(v); } };
+template <typename T, int DIR>
+struct Dft<T, DIR, 13> { __device__ __forceinline__ static void run(Cx<T>* v) { DftPrime<T, DIR, 13>::run(v); } };
+
+// ---------------------------------------------------------------------------
+// One radix-r Stockham sub-stage on all NB columns of the tile, in place.
+// Element j of sub-butterfly k (= p*S + q) is read at position k + j*R/r and
+// written at r*S*p + j*S + q, twiddled by w_L^(p*j) = w_R^(p*j*S). Thread
+// (b, kg) owns column b and butterflies k = kg + i*Tf; it loads all of them
+// into registers before the barrier, so one shared buffer suffices. The host
+// sizes Tf so that no thread holds more than max(1, 16/r) butterflies.
+template <typename T, int DIR, int r>
+__device__ __noinline__ void substage(Cx<T>* __restrict__ buf, const int b, const int kg, const int Tf,
+                                         const int NB, const int Rr, const int S, const FastDiv fS,
+                                         const Cx<T>* __restrict__ twR) {
+  constexpr int IPT = (16 / r) > 0 ? (16 / r) : 1;
+  const int jstride_in = Rr * NB;
+  const int jstride_out = S * NB;
+  Cx<T> v[IPT][r];
+#pragma unroll
+  for (int i = 0; i < IPT; ++i) {
+    const int k = kg + i * Tf;
+    if (k < Rr) {
+      const int a = k * NB + b;
+#pragma unroll
+      for (int j = 0; j < r; ++j) v[i][j] = buf[pidx<T>(a + j * jstride_in)];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < IPT; ++i) {
+    const int k = kg + i * Tf;
+    if (k < Rr) {
+      const int p = (int)fS.div((uint32_t)k);
+      const int q = k - p * S;
+      Dft<T, DIR, r>::run(v[i]);
+      const int a = (r * S * p + q) * NB + b;
+      buf[pidx<T>(a)] = v[i][0];
+      if (p == 0) {
+#pragma unroll
+        for (int j = 1; j < r; ++j) buf[pidx<T>(a + j * jstride_out)] = v[i][j];
+      } else {
+        const int tstep = p * S;
+#pragma unroll
+        for (int j = 1; j < r; ++j) {
+          const Cx<T> w = __ldg(&twR[j * tstep]);
+          buf[pidx<T>(a + j * jstride_out)] = cmul(v[i][j], w);
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int LOADOP>
+__device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in, int64_t b, int64_t g) {
+  if (LOADOP == LOAD_PLAIN) {
+    return __ldg(reinterpret_cast<const Cx<T>*>(in) + b * pp.in_bstride + g);
+  } else if (LOADOP == LOAD_DECONV) {
+    // grid position g of the length-m zero-padded deconvolved input
+    // (FFTJ _deconv! + zero fill, src/resample.jl:258-301)
+    const int64_t n = pp.ld_n, m = pp.ld_m, hp = pp.ld_hp;
+    int64_t j;
+    if (g < hp) j = g;
+    else if (g >= m - n + hp) j = g - (m - n);
+    else return mk<T>(0, 0);
+    const Cx<T> x = __ldg(reinterpret_cast<const Cx<T>*>(in) + b * pp.ld_stride + j);
+    const T c = __ldg(reinterpret_cast<const T*>(pp.ld_tab) + j);
+    return mk<T>(x.x * c, x.y * c);
+  } else if (LOADOP == LOAD_C2R_PRE) {
+    // irfft pre-pass (FFTJ src/real.jl:149-192): Z[k] = xe + i (w xd)
+    const int64_t h = pp.ld_n;
+    const Cx<T>* X = reinterpret_cast<const Cx<T>*>(in) + b * pp.ld_stride;
+    const Cx<T> a = __ldg(X + g);
+    Cx<T> bb = __ldg(X + (h - g));
+    bb.y = -bb.y;
+    const T pre = (T)pp.ld_pre;
+    const Cx<T> xe = mk<T>((a.x + bb.x) * pre, (a.y + bb.y) * pre);
+    const Cx<T> xd = mk<T>((a.x - bb.x) * pre, (a.y - bb.y) * pre);
+    const Cx<T> w = __ldg(reinterpret_cast<const Cx<T>*>(pp.ld_tab) + g);
+    const T tr = fma(w.x, xd.x, -(w.y * xd.y));
+    const T ti = fma(w.x, xd.y, w.y * xd.x);
+    return mk<T>(xe.x - ti, xe.y + tr);
+  } else {  // LOAD_REAL
+    const T x = __ldg(reinterpret_cast<const T*>(in) + b * pp.ld_stride + g);
+    return mk<T>(x, 0);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ Cx<T> outer_tw(const PassParams& pp, int64_t e) {
+  if (pp.tw_mode == 1) return __ldg(reinterpret_cast<const Cx<T>*>(pp.tw_full) + e);
+  const Cx<T> hi = __ldg(reinterpret_cast<const Cx<T>*>(pp.tw_hi) + (e >> pp.tw_shift));
+  const Cx<T> lo = __ldg(reinterpret_cast<const Cx<T>*>(pp.tw_lo) + (e & ((1ll << pp.tw_shift) - 1)));
+  return cmul(hi, lo);
+}
+
+// ---------------------------------------------------------------------------
+// Passes specialised at compile time: the radix sequence of the pass's
+// R-point DFT is a template parameter pack, so R, the sub-stage strides S and
+// the threads per column are constants and every index is strength-reduced.
+struct RuntimeRecipe {
+  static constexpr bool kConst = false;
+  static constexpr int R = 1;
+  static constexpr int Tf = 1;
+};
+
+template <int... Rs>
+struct Recipe {
+  static constexpr bool kConst = true;
+  static constexpr int n = sizeof...(Rs);
+  static constexpr int R = (Rs * ... * 1);
+  // threads per column: the smallest count with <= 16 elements per thread and
+  // <= max(1, 16/r) butterflies per thread in every sub-stage (the host
+  // planner applies the same rule)
+  static constexpr int tf() {
+    constexpr int a[] = {Rs...};
+    for (int t = 1; t <= R; ++t) {
+      bool ok = (R + t - 1) / t <= 16;
+      for (int i = 0; i < n && ok; ++i) {
+        const int cap = 16 / a[i] > 0 ? 16 / a[i] : 1;
+        if ((R / a[i] + t - 1) / t > cap) ok = false;
+      }
+      if (ok) return t;
+    }
+    return R;
+  }
+  static constexpr int Tf = tf();
+};
+
+// compile-time sub-stage: the maps of substage<> with constant r, S, R/r, Tf
+template <typename T, int DIR, int r, int S, int Rr, int TF>
+__device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b, const int kg, const int NB,
+                                            const Cx<T>* __restrict__ twR) {
+  constexpr int IPT = (Rr + TF - 1) / TF;
+  const int jstride_in = Rr * NB;
+  const int jstride_out = S * NB;
+  Cx<T> v[IPT][r];
+#pragma unroll
+  for (int i = 0; i < IPT; ++i) {
+    const int k = kg + i * TF;
+    if ((i + 1) * TF <= Rr || k < Rr) {
+      const int a = k * NB + b;
+#pragma unroll
+      for (int j = 0; j < r; ++j) v[i][j] = buf[pidx<T>(a + j * jstride_in)];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < IPT; ++i) {
+    const int k = kg + i * TF;
+    if ((i + 1) * TF <= Rr || k < Rr) {
+      const int p = k / S;
+      const int q = k - p * S;
+      Dft<T, DIR, r>::run(v[i]);
+      const int a = (r * S * p + q) * NB + b;
+      buf[pidx<T>(a)] = v[i][0];
+      if (Rr == S) {
+        // last sub-stage of the pass (L = r): no twiddle
+#pragma unroll
+        for (int j = 1; j < r; ++j) buf[pidx<T>(a + j * jstride_out)] = v[i][j];
+      } else {
+        const int tstep = p * S;
+#pragma unroll
+        for (int j = 1; j < r; ++j) {
+          Cx<T> w = v[i][j];
+          if (p != 0) w = cmul(w, __ldg(&twR[j * tstep]));
+          buf[pidx<T>(a + j * jstride_out)] = w;
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int DIR, int TF, int R, int S, int r, int... rest>
+__device__ __forceinline__ void run_subs_ct(Cx<T>* buf, const int b, const int kg, const int NB,
+                                            const Cx<T>* twR) {
+  substage_ct<T, DIR, r, S, R / r, TF>(buf, b, kg, NB, twR);
+  if constexpr (sizeof...(rest) > 0) run_subs_ct<T, DIR, TF, R, S * r, rest...>(buf, b, kg, NB, twR);
+}
+template <typename T, int DIR, int... Rs>
+__device__ __forceinline__ void run_recipe(Recipe<Rs...>*, Cx<T>* buf, const int b, const int kg, const int NB,
+                                           const Cx<T>* twR) {
+  run_subs_ct<T, DIR, Recipe<Rs...>::Tf, Recipe<Rs...>::R, 1, Rs...>(buf, b, kg, NB, twR);
+}
+
+// ---------------------------------------------------------------------------
+// One Stockham pass over one tile (the kernel comment in kernels.cu gives
+// the maps). Rec is RuntimeRecipe (radix sequence read from pp.sub) or a
+// Recipe<r...> fixed at compile time.
+template <typename T, int DIR, int LOADOP, class Rec>
+__device__ __forceinline__ void pass_body(const PassParams& pp, const void* __restrict__ in,
+                                          Cx<T>* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Cx<T>* buf = reinterpret_cast<Cx<T>*>(smem_raw);
+  constexpr int EPT = Rec::kConst ? (Rec::R + Rec::Tf - 1) / Rec::Tf : 16;
+  const uint32_t tile = blockIdx.x;
+  const uint32_t t1 = pp.ftq.div(tile);
+  const uint32_t tq = tile - t1 * pp.tiles_q;
+  const uint32_t tb = pp.ftp.div(t1);
+  const uint32_t tp = t1 - tb * pp.tiles_p;
+  const int64_t q0 = (int64_t)tq * pp.Q, p0 = (int64_t)tp * pp.P, b0 = (int64_t)tb * pp.NBt;
+  const int R = Rec::kConst ? Rec::R : pp.R;
+  const int Tf = Rec::kConst ? Rec::Tf : pp.Tf;
+  const int P = pp.P, Q = pp.Q, NB = pp.NB;
+  const int E = NB * R;
+  const int64_t ms = pp.m * pp.s;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+
+  // this thread's column b = (bt, pl, ql) and first butterfly row kg
+  const int kg = (int)pp.fNB.div((uint32_t)tid);
+  const int b = tid - kg * NB;
+  const int cq = (int)pp.fQ.div((uint32_t)b);
+  const int ql = b - cq * Q;
+  const int cbt = (int)pp.fP.div((uint32_t)cq);
+  const int pl = cq - cbt * P;
+  const int64_t batch = b0 + cbt;
+  const int64_t pcol = p0 + pl;
+
+  // ---- load: HBM -> shared. All of a thread's loads are issued before its
+  // first shared store; indices are recomputed rather than kept in registers.
+  {
+    Cx<T> v[EPT];
+    if (pp.load_rows) {
+      // transforms contiguous along j (one pass over whole transforms)
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        const int e = tid + i * nthr;
+        if (e < E) {
+          const int c = Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e);
+          const int64_t bb = b0 + c;
+          v[i] = bb < pp.nbatch ? load_elem<T, LOADOP>(pp, in, bb, e - c * R) : mk<T>(0, 0);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        const int e = tid + i * nthr;
+        if (e < E) {
+          const int c = Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e);
+          buf[pidx<T>((e - c * R) * NB + c)] = v[i];
+        }
+      }
+    } else {
+      // lanes walk the tile's columns (contiguous p or q runs)
+      const int64_t gcol = pp.s * pcol + q0 + ql;
+      const bool ok = batch < pp.nbatch;
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        const int j = kg + i * Tf;
+        if (j < R) v[i] = ok ? load_elem<T, LOADOP>(pp, in, batch, gcol + (int64_t)j * ms) : mk<T>(0, 0);
+      }
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        const int j = kg + i * Tf;
+        if (j < R) buf[pidx<T>(j * NB + b)] = v[i];
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- the pass's R-point DFTs: radix sub-stages in shared memory
+  const Cx<T>* twR = reinterpret_cast<const Cx<T>*>(pp.twR);
+  if constexpr (Rec::kConst) {
+    run_recipe<T, DIR>((Rec*)nullptr, buf, b, kg, NB, twR);
+  } else {
+#pragma unroll 1
+    for (int si = 0; si < pp.nsub; ++si) {
+      const SubStage& ss = pp.sub[si];
+      switch (ss.r) {
+        case 2: substage<T, DIR, 2>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
+        case 3: substage<T, DIR, 3>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
+        case 4: substage<T, DIR, 4>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
+        case 5: substage<T, DIR, 5>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
+        case 7: substage<T, DIR, 7>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
+        case 8: substage<T, DIR, 8>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
+        case 11: substage<T, DIR, 11>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
+        case 13: substage<T, DIR, 13>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
+        case 16: substage<T, DIR, 16>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
+        default: break;
+      }
+    }
+  }
+
+  // ---- store: shared -> HBM with the outer twiddle w_ncur^(p*j) and scale.
+  // The twiddle loads of all of a thread's elements are issued first.
+  const bool scaled = pp.scale != 1.0;
+  const T sc = (T)pp.scale;
+  const bool tw = pp.tw_mode != 0;
+  Cx<T> w[EPT];
+  if (pp.store_rows) {
+    // outputs contiguous along j (s == 1): lanes walk j
+#pragma unroll
+    for (int i = 0; i < EPT; ++i) {
+      const int e = tid + i * nthr;
+      w[i] = mk<T>(1, 0);
+      if (e < E && tw) {
+        const int c = Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e);
+        const int j = e - c * R;
+        const int cbt2 = (int)pp.fP.div((uint32_t)c);
+        const int64_t p = p0 + (c - cbt2 * P);
+        if (p * j != 0) w[i] = outer_tw<T>(pp, p * (int64_t)j);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < EPT; ++i) {
+      const int e = tid + i * nthr;
+      if (e < E) {
+        const int c = Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e);
+        const int j = e - c * R;
+        const int cbt2 = (int)pp.fP.div((uint32_t)c);
+        const int64_t bb = b0 + cbt2;
+        if (bb < pp.nbatch) {
+          Cx<T> v = buf[pidx<T>(j * NB + c)];
+          if (tw) v = cmul(v, w[i]);
+          if (scaled) { v.x *= sc; v.y *= sc; }
+          out[bb * pp.out_bstride + (int64_t)R * (p0 + (c - cbt2 * P)) + j] = v;
+        }
+      }
+    }
+  } else {
+    const bool ok = batch < pp.nbatch;
+#pragma unroll
+    for (int i = 0; i < EPT; ++i) {
+      const int j = kg + i * Tf;
+      w[i] = mk<T>(1, 0);
+      if (j < R && tw && pcol * j != 0) w[i] = outer_tw<T>(pp, pcol * (int64_t)j);
+    }
+    if (ok) {
+      Cx<T>* ob = out + batch * pp.out_bstride + (int64_t)R * pp.s * pcol + q0 + ql;
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        const int j = kg + i * Tf;
+        if (j < R) {
+          Cx<T> v = buf[pidx<T>(j * NB + b)];
+          if (tw) v = cmul(v, w[i]);
+          if (scaled) { v.x *= sc; v.y *= sc; }
+          ob[(int64_t)j * pp.s] = v;
+        }
+      }
+    }
+  }
+}
+
+// load_elem with the batch offset already applied (boff = batch * stride)
+template <typename T, int LOADOP>
+__device__ __forceinline__ Cx<T> load_elem_off(const PassParams& pp, const void* in, int64_t boff, int64_t g) {
+  if (LOADOP == LOAD_PLAIN) {
+    return __ldg(reinterpret_cast<const Cx<T>*>(in) + boff + g);
+  } else if (LOADOP == LOAD_DECONV) {
+    const int64_t n = pp.ld_n, m = pp.ld_m, hp = pp.ld_hp;
+    int64_t j;
+    if (g < hp) j = g;
+    else if (g >= m - n + hp) j = g - (m - n);
+    else return mk<T>(0, 0);
+    const Cx<T> x = __ldg(reinterpret_cast<const Cx<T>*>(in) + boff + j);
+    const T c = __ldg(reinterpret_cast<const T*>(pp.ld_tab) + j);
+    return mk<T>(x.x * c, x.y * c);
+  } else if (LOADOP == LOAD_C2R_PRE) {
+    const int64_t h = pp.ld_n;
+    const Cx<T>* X = reinterpret_cast<const Cx<T>*>(in) + boff;
+    const Cx<T> a = __ldg(X + g);
+    Cx<T> bb = __ldg(X + (h - g));
+    bb.y = -bb.y;
+    const T pre = (T)pp.ld_pre;
+    const Cx<T> xe = mk<T>((a.x + bb.x) * pre, (a.y + bb.y) * pre);
+    const Cx<T> xd = mk<T>((a.x - bb.x) * pre, (a.y - bb.y) * pre);
+    const Cx<T> w = __ldg(reinterpret_cast<const Cx<T>*>(pp.ld_tab) + g);
+    const T tr = fma(w.x, xd.x, -(w.y * xd.y));
+    const T ti = fma(w.x, xd.y, w.y * xd.x);
+    return mk<T>(xe.x - ti, xe.y + tr);
+  } else {
+    const T x = __ldg(reinterpret_cast<const T*>(in) + boff + g);
+    return mk<T>(x, 0);
+  }
+}
+
+// sub-stages 2 .. NS-DROP of a recipe (the first ran fused with the load;
+// DROP = 1 leaves the last one to the fused store)
+template <typename T, int DIR, int TF, int R, int S, int DROP, int r, int... rest>
+__device__ __forceinline__ void run_mid_skip(Cx<T>* buf, const int b, const int kg, const int NB,
+                                             const Cx<T>* twR) {
+  if constexpr (sizeof...(rest) >= DROP) {
+    if constexpr (sizeof...(rest) == 0) {
+      substage_ct<T, DIR, r, S, R / r, TF>(buf, b, kg, NB, twR);
+    } else {
+      substage_ct<T, DIR, r, S, R / r, TF>(buf, b, kg, NB, twR);
+      run_mid_skip<T, DIR, TF, R, S * r, DROP, rest...>(buf, b, kg, NB, twR);
+    }
+  }
+}
+template <typename T, int DIR, int TF, int R, int S1, int DROP, int r0, int... rest>
+__device__ __forceinline__ void run_mid_ct(Cx<T>* buf, const int b, const int kg, const int NB,
+                                           const Cx<T>* twR) {
+  if constexpr (sizeof...(rest) > 0) run_mid_skip<T, DIR, TF, R, S1, DROP, rest...>(buf, b, kg, NB, twR);
+}
+
+// ---------------------------------------------------------------------------
+// Recipe pass with the first sub-stage fused into the HBM load and/or the last
+// sub-stage fused into the HBM store. MODE 0: lanes walk j on both sides (one
+// pass over whole contiguous transforms); MODE 1: fused load, row store (the
+// first pass of a multi-pass transform, s == 1); MODE 2: fused load and store
+// (later passes: lanes walk the contiguous q columns on both sides).
+// No per-element 64-bit multiply or multiply-high: addresses and (column,
+// row) counters advance by additions.
+template <typename T, int DIR, int LOADOP, int MODE, int... Rs>
+__device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __restrict__ in,
+                                           Cx<T>* __restrict__ out) {
+  using Rec = Recipe<Rs...>;
+  constexpr int R = Rec::R, TF = Rec::Tf, NS = Rec::n;
+  constexpr int rad[] = {Rs...};
+  constexpr int r0 = rad[0], rL = rad[NS - 1];
+  constexpr int EPT = (R + TF - 1) / TF;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Cx<T>* buf = reinterpret_cast<Cx<T>*>(smem_raw);
+  const uint32_t tile = blockIdx.x;
+  const uint32_t t1 = pp.ftq.div(tile);
+  const uint32_t tq = tile - t1 * pp.tiles_q;
+  const uint32_t tb = pp.ftp.div(t1);
+  const uint32_t tp = t1 - tb * pp.tiles_p;
+  const int64_t q0 = (int64_t)tq * pp.Q, p0 = (int64_t)tp * pp.P, b0 = (int64_t)tb * pp.NBt;
+  const int P = pp.P, Q = pp.Q, NB = pp.NB;
+  const int E = NB * R;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int kg = (int)pp.fNB.div((uint32_t)tid);
+  const int b = tid - kg * NB;
+  const int cq = (int)pp.fQ.div((uint32_t)b);
+  const int ql = b - cq * Q;
+  const int cbt = (int)pp.fP.div((uint32_t)cq);
+  const int pl = cq - cbt * P;
+  const int64_t batch = b0 + cbt;
+  const int64_t pcol = p0 + pl;
+  const bool colok = batch < pp.nbatch;
+  const Cx<T>* twR = reinterpret_cast<const Cx<T>*>(pp.twR);
+
+  if constexpr (MODE == 0) {
+    // ---- row load (lanes walk j): e = tid + i*nthr -> (c, j), c = column
+    Cx<T> v[EPT];
+    const int dc = nthr / R, dj = nthr - (nthr / R) * R;
+    {
+      int c = tid / R, j = tid - (tid / R) * R;
+      const int64_t bstr = LOADOP == LOAD_PLAIN ? pp.in_bstride : pp.ld_stride;
+      int64_t boff = (b0 + c) * bstr;
+      const int64_t dstep = (int64_t)dc * bstr;
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        if (tid + i * nthr < E) {
+          v[i] = b0 + c < pp.nbatch ? load_elem_off<T, LOADOP>(pp, in, boff, j) : mk<T>(0, 0);
+        }
+        j += dj; c += dc; boff += dstep;
+        if (j >= R) { j -= R; c++; boff += bstr; }
+      }
+    }
+    {
+      int c = tid / R, j = tid - (tid / R) * R;
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        if (tid + i * nthr < E) buf[pidx<T>(j * NB + c)] = v[i];
+        j += dj; c += dc;
+        if (j >= R) { j -= R; c++; }
+      }
+    }
+    __syncthreads();
+    run_subs_ct<T, DIR, TF, R, 1, Rs...>(buf, b, kg, NB, twR);
+  } else {
+    // ---- fused load + first sub-stage (radix r0, S = 1): butterfly k reads
+    // column positions k + j*R/r0 straight from HBM
+    constexpr int Rr = R / r0;
+    constexpr int IPT = (Rr + TF - 1) / TF;
+    const int64_t ms = pp.m * pp.s;
+    const int64_t bstr = LOADOP == LOAD_PLAIN ? pp.in_bstride : pp.ld_stride;
+    const int64_t boff = batch * bstr;
+    const int64_t gcol = pp.s * pcol + q0 + ql;
+    Cx<T> v[IPT][r0];
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) {
+      const int k = kg + i * TF;
+      if ((i + 1) * TF <= Rr || k < Rr) {
+        int64_t g = gcol + (int64_t)k * ms;
+        const int64_t gstep = (int64_t)Rr * ms;
+#pragma unroll
+        for (int j = 0; j < r0; ++j) {
+          v[i][j] = colok ? load_elem_off<T, LOADOP>(pp, in, boff, g) : mk<T>(0, 0);
+          g += gstep;
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) {
+      const int k = kg + i * TF;
+      if ((i + 1) * TF <= Rr || k < Rr) {
+        Dft<T, DIR, r0>::run(v[i]);
+        const int a = r0 * k * NB + b;
+        buf[pidx<T>(a)] = v[i][0];
+#pragma unroll
+        for (int j = 1; j < r0; ++j) {
+          Cx<T> w = v[i][j];
+          if (NS > 1 && k != 0) w = cmul(w, __ldg(&twR[j * k]));
+          buf[pidx<T>(a + j * NB)] = w;
+        }
+      }
+    }
+    __syncthreads();
+    if constexpr (NS > 2 || (NS == 2 && MODE == 1)) {
+      // middle sub-stages (all but the last when the store is fused)
+      run_mid_ct<T, DIR, TF, R, r0, (MODE == 2 ? 1 : 0), Rs...>(buf, b, kg, NB, twR);
+    }
+  }
+
+  const bool scaled = pp.scale != 1.0;
+  const T sc = (T)pp.scale;
+  const bool tw = pp.tw_mode != 0;
+  if constexpr (MODE <= 1) {
+    // ---- row store (lanes walk j): outputs contiguous along j (s == 1)
+    const int dc = nthr / R, dj = nthr - (nthr / R) * R;
+    int c = tid / R, j = tid - (tid / R) * R;
+    Cx<T> w[EPT];
+#pragma unroll
+    for (int i = 0; i < EPT; ++i) {
+      w[i] = mk<T>(1, 0);
+      if (tid + i * nthr < E && tw) {
+        const uint32_t e = (uint32_t)(p0 + c) * (uint32_t)j;  // NBt == 1 whenever m > 1
+        if (e != 0) w[i] = outer_tw<T>(pp, e);
+      }
+      j += dj; c += dc;
+      if (j >= R) { j -= R; c++; }
+    }
+    c = tid / R; j = tid - (tid / R) * R;
+    Cx<T>* ob = out + b0 * pp.out_bstride + (int64_t)R * p0;
+#pragma unroll
+    for (int i = 0; i < EPT; ++i) {
+      const int e = tid + i * nthr;
+      // MODE 0: column c is a batch entry; MODE 1: a butterfly p of batch b0
+      if (e < E && b0 + (MODE == 0 ? c : 0) < pp.nbatch) {
+        Cx<T> v = buf[pidx<T>(j * NB + c)];
+        if (tw) v = cmul(v, w[i]);
+        if (scaled) { v.x *= sc; v.y *= sc; }
+        ob[e] = v;
+      }
+      j += dj; c += dc;
+      if (j >= R) { j -= R; c++; }
+    }
+  } else {
+    // ---- fused last sub-stage (radix rL, L = rL, no inner twiddle) + store:
+    // butterfly k (< S = R/rL) writes positions j*S + k of its column
+    constexpr int S = R / rL;
+    constexpr int IPT = (S + TF - 1) / TF;
+    Cx<T> v[IPT][rL];
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) {
+      const int k = kg + i * TF;
+      if ((i + 1) * TF <= S || k < S) {
+#pragma unroll
+        for (int j = 0; j < rL; ++j) v[i][j] = buf[pidx<T>((k + j * S) * NB + b)];
+      }
+    }
+    if (colok) {
+      Cx<T>* ob = out + batch * pp.out_bstride + (int64_t)R * pp.s * pcol + q0 + ql;
+      const int64_t jstep = (int64_t)S * pp.s;
+#pragma unroll
+      for (int i = 0; i < IPT; ++i) {
+        const int k = kg + i * TF;
+        if ((i + 1) * TF <= S || k < S) {
+          Dft<T, DIR, rL>::run(v[i]);
+          Cx<T>* o = ob + (int64_t)k * pp.s;
+          uint32_t e = (uint32_t)pcol * (uint32_t)k;
+          const uint32_t estep = (uint32_t)pcol * (uint32_t)S;
+#pragma unroll
+          for (int j = 0; j < rL; ++j) {
+            Cx<T> x = v[i][j];
+            if (tw && e != 0) x = cmul(x, outer_tw<T>(pp, e));
+            if (scaled) { x.x *= sc; x.y *= sc; }
+            *o = x;
+            o += jstep;
+            e += estep;
+          }
+        }
+      }
+    }
+  }
+}
+
+template <typename T, int DIR, int LOADOP, int MODE, class Rec>
+struct FusedLaunch;
+template <typename T, int DIR, int LOADOP, int MODE, int... Rs>
+struct FusedLaunch<T, DIR, LOADOP, MODE, Recipe<Rs...>> {
+  __device__ __forceinline__ static void run(const PassParams& pp, const void* in, Cx<T>* out) {
+    pass_fused<T, DIR, LOADOP, MODE, Rs...>(pp, in, out);
+  }
+};
+
+}  // namespace fftj

@@ -241,6 +241,7 @@ struct Op {
   OpKind kind;
   int src, dst;
   int dir = -1;
+  const void* kfn = nullptr;  // recipe kernel for OP_PASS (nullptr: generic)
   PassParams pp;
   InterpParams ip;
   RealPostParams rp;
@@ -345,15 +346,30 @@ int build_axis_passes(fftj_plan_s* P, i64 n, i64 Bi, i64 nbatch, i64 ibs, i64 ob
     }
     const i64 m = ncur / R;
     const i64 s = s1 * Bi;  // effective stride
+    if (ncur >= ((i64)1 << 31)) return fail(FFTJ_ERR_UNSUPPORTED, "transform length must be below 2^31");
     pp.m = m;
     pp.s = s;
     pp.ncur = ncur;
     pp.in_bstride = ibs;
     pp.out_bstride = obs;
     pp.nbatch = nbatch;
-    // tile: columns (batch, p, q)
+    // threads per tile column: every sub-stage's butterflies fit the
+    // per-thread register budget (max(1, 16/r) butterflies, <= 16 elements)
+    auto tf_ok = [&](i64 tf) {
+      if ((R + tf - 1) / tf > 16) return false;
+      for (int i = 0; i < pp.nsub; ++i) {
+        const int r = pp.sub[i].r;
+        const i64 cap = std::max(1, 16 / r);
+        if ((pp.sub[i].Rr + tf - 1) / tf > cap) return false;
+      }
+      return true;
+    };
+    i64 Tf = 1;
+    while (!tf_ok(Tf)) Tf++;
+    // tile: columns (batch, p, q); NB * Tf threads
     const i64 tmax = std::max<i64>(cfg.tile_max, R);
-    const i64 cols = std::max<i64>(1, tmax / R);
+    i64 cols = std::max<i64>(1, std::min<i64>(tmax / R, cfg.threads_max / Tf));
+    if (Tf > cfg.threads_max) return fail(FFTJ_ERR_UNSUPPORTED, "pass radix needs too many threads");
     i64 Pt = 1, Qt = 1, NBt = 1;
     if (s == 1) {
       Pt = largest_divisor_le(m, cols);
@@ -370,6 +386,8 @@ int build_axis_passes(fftj_plan_s* P, i64 n, i64 Bi, i64 nbatch, i64 ibs, i64 ob
     pp.Q = (int)Qt;
     pp.NBt = (int)NBt;
     pp.NB = (int)(Pt * Qt * NBt);
+    pp.Tf = (int)Tf;
+    pp.ept = (int)((R + Tf - 1) / Tf);
     pp.fQ = FastDiv((uint32_t)Qt);
     pp.fP = FastDiv((uint32_t)Pt);
     pp.fR = FastDiv((uint32_t)R);
@@ -382,18 +400,12 @@ int build_axis_passes(fftj_plan_s* P, i64 n, i64 Bi, i64 nbatch, i64 ibs, i64 ob
     const double ntiles = (double)pp.tiles_q * pp.tiles_p * pp.tiles_b;
     if (ntiles >= 2147483647.0) return fail(FFTJ_ERR_UNSUPPORTED, "grid too large");
     const i64 E = (i64)pp.NB * R;
-    // threads: enough that each sub-stage's butterflies fit IPT(r) per thread
-    i64 th = 32;
-    for (int i = 0; i < pp.nsub; ++i) {
-      const int r = pp.sub[i].r;
-      const int ipt = std::max(1, 16 / r);
-      const i64 need = (E / r + ipt - 1) / ipt;
-      th = std::max(th, need);
-    }
-    th = std::max<i64>(th, std::min<i64>(E, 128));
-    th = (th + 31) / 32 * 32;
-    if (th > cfg.threads_max) return fail(FFTJ_ERR_UNSUPPORTED, "tile needs too many threads");
-    pp.threads = (int)th;
+    pp.threads = (int)(pp.NB * Tf);
+    // lanes walk j where the transform axis is contiguous in HBM
+    pp.load_rows = (m == 1 && s == 1) ? 1 : 0;
+    pp.store_rows = (s == 1) ? 1 : 0;
+    if ((pp.load_rows || pp.store_rows) && (E + pp.threads - 1) / pp.threads > 16)
+      return fail(FFTJ_ERR_UNSUPPORTED, "tile exceeds 16 elements per thread");
     const int padsh = f64 ? 3 : 4;
     pp.smem_elems = (int)(E + (E >> padsh) + 2);
     // inner twiddles w_R^t
@@ -420,7 +432,6 @@ int build_axis_passes(fftj_plan_s* P, i64 n, i64 Bi, i64 nbatch, i64 ibs, i64 ob
     }
     pp.scale = (pi + 1 == Rs.size()) ? scale : 1.0;
     pp.load_op = LOAD_PLAIN;
-    if (prepare_pass<T>(pp, dir) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
     op.dst_bytes = (size_t)(nbatch * obs) * sizeof(T) * 2;
     out_ops->push_back(op);
     P->pass_R.push_back((int)R);
@@ -492,7 +503,6 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
     f.ld_tab = upload_raw(P, c.data(), c.size() * sizeof(T));
     if (!f.ld_tab) return fail(FFTJ_ERR_CUDA, "table upload failed");
   }
-  if (prepare_pass<T>(f, dir) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
   Op ip;
   ip.kind = OP_INTERP;
   ip.ip.n = n;
@@ -622,7 +632,6 @@ int build_c2r_1d(fftj_plan_s* P, i64 n, i64 nb, i64 idist, i64 odist, bool norma
       f.ld_stride = idist;
       f.ld_tab = twd;
       f.ld_pre = normalized ? 0.5 : 1.0;
-      if (prepare_pass<T>(f, +1) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
       for (auto& o : inner) ops->push_back(o);
       return FFTJ_OK;
     }
@@ -731,7 +740,40 @@ int check_dims(int rank, const int64_t* dims, std::vector<i64>* out) {
   return FFTJ_OK;
 }
 
+// Pick the compile-time recipe kernel matching a pass (same radix sequence,
+// load op, direction and threads per column), else the generic kernel, and
+// opt it into its shared memory.
+template <typename T>
+int finalize_passes(fftj_plan_s* P) {
+  for (auto& op : P->ops) {
+    if (op.kind != OP_PASS) continue;
+    const PassParams& pp = op.pp;
+    op.kfn = nullptr;
+    int count = 0;
+    const RecipeEntry* tab = op.dir < 0 ? recipe_table<T, -1>(&count) : recipe_table<T, 1>(&count);
+    // the kernel mode this pass needs (see pass_fused in pass_common.cuh)
+    int mode = -1;
+    if (pp.load_rows && pp.store_rows && (pp.NBt == 1 || pp.out_bstride == (int64_t)pp.R)) mode = 0;
+    else if (!pp.load_rows && pp.store_rows && pp.NBt == 1) mode = 1;
+    else if (!pp.load_rows && !pp.store_rows) mode = 2;
+    for (int i = 0; i < count && mode >= 0; ++i) {
+      const RecipeEntry& e = tab[i];
+      if (e.mode != mode || e.load_op != pp.load_op || e.Tf != pp.Tf) continue;
+      int n = 0;
+      while (n < 6 && e.radix[n]) n++;
+      if (n != pp.nsub) continue;
+      bool same = true;
+      for (int j = 0; j < n; ++j) same = same && e.radix[j] == pp.sub[j].r;
+      if (same) { op.kfn = e.fn; break; }
+    }
+    if (prepare_pass<T>(pp, op.dir, op.kfn) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
+  }
+  return FFTJ_OK;
+}
+
 int finish(fftj_plan_s* P, fftj_plan* out) {
+  int frc = P->dtype == FFTJ_F32 ? finalize_passes<float>(P) : finalize_passes<double>(P);
+  if (frc) return frc;
   wire(P->ops);
   int rc = alloc_workspace(P);
   if (rc) return rc;
@@ -846,14 +888,14 @@ int fftj_execute(fftj_plan plan, const void* d_in, void* d_out, void* stream) {
     cudaError_t e = cudaSuccess;
     if (P->dtype == FFTJ_F32) {
       switch (op.kind) {
-        case OP_PASS: e = launch_pass<float>(op.pp, op.dir, src, dst, st); break;
+        case OP_PASS: e = launch_pass<float>(op.pp, op.dir, op.kfn, src, dst, st); break;
         case OP_INTERP: e = launch_interp<float>(op.ip, src, dst, st); break;
         case OP_RPOST: e = launch_real_post<float>(op.rp, src, dst, st); break;
         case OP_COPY: e = launch_copy<float>(op.cp, src, dst, st); break;
       }
     } else {
       switch (op.kind) {
-        case OP_PASS: e = launch_pass<double>(op.pp, op.dir, src, dst, st); break;
+        case OP_PASS: e = launch_pass<double>(op.pp, op.dir, op.kfn, src, dst, st); break;
         case OP_INTERP: e = launch_interp<double>(op.ip, src, dst, st); break;
         case OP_RPOST: e = launch_real_post<double>(op.rp, src, dst, st); break;
         case OP_COPY: e = launch_copy<double>(op.cp, src, dst, st); break;
@@ -881,6 +923,8 @@ int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info) {
   for (size_t i = 0; i < plan->pass_R.size() && i < 8; ++i) info->pass_radix[i] = plan->pass_R[i];
   info->workspace_bytes = plan->ws[0].bytes + plan->ws[1].bytes;
   info->table_bytes = plan->table_bytes;
+  for (auto& op : plan->ops)
+    if (op.kind == OP_PASS && op.kfn) info->specialized_passes++;
   return FFTJ_OK;
 }
 

@@ -1,0 +1,3 @@
+#define FFTJ_T float
+#define FFTJ_DIR 1
+#include "recipes.inc"

@@ -49,7 +49,7 @@ class PlanInfo(ctypes.Structure):
         ("route", ctypes.c_int), ("npasses", ctypes.c_int), ("n", ctypes.c_int64),
         ("batch", ctypes.c_int64), ("resample_m", ctypes.c_int64), ("resample_w", ctypes.c_int64),
         ("pass_radix", ctypes.c_int * 8), ("workspace_bytes", ctypes.c_size_t),
-        ("table_bytes", ctypes.c_size_t),
+        ("table_bytes", ctypes.c_size_t), ("specialized_passes", ctypes.c_int),
     ]
 
 

@@ -13,7 +13,8 @@ PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD = os.path.join(PKG_DIR, "_build")
 LIB = os.path.join(PKG_DIR, "libfftj_gb300.so")
-SOURCES = ["kernels.cu", "planner.cpp"]
+SOURCES = ["kernels.cu", "recipes_f32_fwd.cu", "recipes_f32_bwd.cu", "recipes_f64_fwd.cu",
+           "recipes_f64_bwd.cu", "planner.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

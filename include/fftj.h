@@ -64,6 +64,7 @@ typedef struct {
   int pass_radix[8];    /* points per butterfly of each pass */
   size_t workspace_bytes;
   size_t table_bytes;
+  int specialized_passes; /* passes run by compile-time specialised kernels */
 } fftj_plan_info_t;
 
 /*
