@@ -1,0 +1,367 @@
+"""Benchmark of the FFTJ GB300 transform path.
+
+Workload (one step): the mixed-radix and prime-size configuration — forward
+ComplexF32 and ComplexF64 1-D FFTs at N = 42525 (3^5 5^2 7), N = 10007
+(prime, resampled onto 20480) and N = 2^18, batch 128 each, inputs iid
+standard complex normal from a fixed seed, resident in HBM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line. `value` is whole-job GFLOP/s in the 5 N log2 N
+convention with inputs on the device; `e2e` is the same metric through the
+public plan API with pinned host buffers copied in and out every step. Under
+torchrun every rank runs the full workload on its own GPU (replicas: the
+transforms are independent, no collective on the data path) and `value` sums
+the ranks. `--impl reference` times the reference's algorithm on the host
+cores instead: FFTJ restated in C++ (the oracle; Julia is not available), all
+host threads, on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "fftj.jl_gb300"))
+sys.path.insert(0, ROOT)
+
+PARTS = [("c32", 42525), ("c32", 10007), ("c32", 1 << 18),
+         ("c64", 42525), ("c64", 10007), ("c64", 1 << 18)]
+BATCH = 128
+METRIC = "FFT GFLOP/s (5N·log2N)"
+WORKLOAD = ("mixed-radix and prime sizes: forward C32 and C64 1-D FFTs at N=42525 (3^5*5^2*7), "
+            "N=10007 (prime, resampled) and N=2^18, batch 128 each")
+
+
+def flops(n, batch):
+    return 5.0 * n * math.log2(n) * batch
+
+
+STEP_FLOPS = sum(flops(n, BATCH) for _, n in PARTS)
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# part's pass kernels, averaged over its launches, from one ncu capture of
+# this workload on a GB300 (the launch list and the capture command are kept
+# with the profile summaries).
+NCU_TRAFFIC_PER_LAUNCH = {}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([v.strip() for v in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# ---------------------------------------------------------------------------
+# reference arm: FFTJ's algorithm on the host cores (oracle restatement)
+
+def cpu_sample(steps_hint=1, max_seconds=20.0):
+    """Time the FFTJ-restated CPU plans (all host threads, threads inside each
+    transform as FFTJ runs them) on a bounded sample of the workload: `nb`
+    transforms of every part. Returns (GFLOP/s, cores, sample description)."""
+    from oracle import oracle as O
+    O.build()
+    nt = O.max_threads()
+    rng = np.random.default_rng(1)
+    plans, xs = [], []
+    for dt, n in PARTS:
+        T = np.float32 if dt == "c32" else np.float64
+        plans.append(O.Plan1D(T, n, "fft", nthreads=nt))
+        xs.append(((rng.standard_normal(n) + 1j * rng.standard_normal(n)) / math.sqrt(2)).astype(
+            np.complex64 if dt == "c32" else np.complex128))
+    for p, x in zip(plans, xs):  # warm plans
+        p(x)
+    # size the sample: per-part transforms so the total stays within budget
+    t0 = time.perf_counter()
+    for p, x in zip(plans, xs):
+        p(x)
+    one = time.perf_counter() - t0
+    nb = int(max(1, min(BATCH, max_seconds / max(one, 1e-6) / max(steps_hint, 1))))
+    t0 = time.perf_counter()
+    for p, x in zip(plans, xs):
+        xb = np.broadcast_to(x, (nb, x.size)).copy()
+        p(xb)
+    dt = time.perf_counter() - t0
+    fl = sum(flops(n, nb) for _, n in PARTS)
+    return fl / dt / 1e9, nt, "%d of %d transforms of each of the 6 parts (FFTJ-restated C++ plans, %d threads)" % (
+        nb, BATCH, nt)
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(1, max_seconds=2.0)
+    for _ in range(args.steps):
+        v, cores, desc = cpu_sample(1, max_seconds=5.0)
+        vals.append(v)
+    value = float(np.median(vals))
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic: iid standard complex normal, seeded",
+        "config": {"workload": WORKLOAD, "sample": desc},
+        "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": cores, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+    import fftj
+
+    world, rank, local = dist_setup()
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU (there is no CPU path)")
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+    fftj.build()
+    dev = torch.device("cuda", local)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0xF17 + rank)
+    plans, xs, ys = [], [], []
+    for dt, n in PARTS:
+        T = np.float32 if dt == "c32" else np.float64
+        ct = torch.complex64 if dt == "c32" else torch.complex128
+        p = fftj.plan_fft(T, n, batch=BATCH)
+        x = torch.randn((BATCH, n), dtype=ct, device=dev, generator=gen)
+        plans.append(p)
+        xs.append(x)
+        ys.append(torch.empty_like(x))
+    launches_per_step = sum(p.info.npasses for p in plans)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        for p, x, y in zip(plans, xs, ys):
+            p(y, x)
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    if pg is not None:
+        t = torch.tensor([ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    value = STEP_FLOPS * world / (ms * 1e-3) / 1e9
+
+    # ---- per-part breakdown and the dominant kernel's roofline (live, CUDA
+    # events on the launching stream)
+    parts = {}
+    reps = 5
+    for (dt, n), p, x, y in zip(PARTS, plans, xs, ys):
+        p(y, x)
+        torch.cuda.synchronize(dev)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            p(y, x)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        pms = a.elapsed_time(b) / reps
+        inf = p.info
+        bytes_alg = 2.0 * x.numel() * x.element_size()
+        parts["%s_%d" % (dt, n)] = {
+            "ms": round(pms, 4), "gflops": round(flops(n, BATCH) / pms / 1e6, 1),
+            "alg_gbs": round(bytes_alg / pms / 1e6, 1), "route": p.route,
+            "passes": [int(v) for v in inf.pass_radix[:inf.npasses]], "launches": int(inf.npasses),
+            "specialized_passes": int(inf.specialized_passes)}
+    dom_key = max(parts, key=lambda k: parts[k]["ms"])
+    dom = parts[dom_key]
+    idx = list(parts).index(dom_key)
+    dx = xs[idx]
+    per_launch_ms = dom["ms"] / max(dom["launches"], 1)
+    bytes_launch = 2.0 * dx.numel() * dx.element_size()
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_launch / (per_launch_ms * 1e-3) / 1e9
+    dn = PARTS[idx][1]
+    fp64 = PARTS[idx][0] == "c64"
+    roofline = {
+        "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+        "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+        "kernel": "k_fused pass of %s N=%d x%d (%d launches/step)" % (PARTS[idx][0], dn, BATCH, dom["launches"]),
+    }
+    if fp64:
+        # ComplexF64 passes are limited by the FP64 pipe (1.19 TFLOP/s measured
+        # with an FMA loop on this GPU), not by HBM
+        roofline["fp64_gflops_5nlogn"] = round(flops(dn, BATCH) / dom["ms"] / 1e6, 1)
+        roofline["fp64_peak_gflops_measured"] = 1193.0
+        roofline["fp64_frac"] = round(roofline["fp64_gflops_5nlogn"] / 1193.0, 4)
+        roofline["note"] = "FP64-pipe bound on GB300 (FP64 is 1/62 of FP32); frac is the HBM fraction"
+    if dom_key in NCU_TRAFFIC_PER_LAUNCH:
+        roofline["traffic"] = NCU_TRAFFIC_PER_LAUNCH[dom_key]
+
+    # ---- e2e: through the public plan API with pinned host buffers
+    hx = [x.cpu().pin_memory() for x in xs]
+    hy = [torch.empty_like(h).pin_memory() for h in hx]
+    h2d = sum(h.numel() * h.element_size() for h in hx)
+    d2h = h2d
+
+    def e2e_step():
+        for p, h_in, h_out, x, y in zip(plans, hx, hy, xs, ys):
+            x.copy_(h_in, non_blocking=True)
+            p(y, x)
+            h_out.copy_(y, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    e2e_steps = max(2, min(args.steps, 5))
+    a.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    b.record(stream)
+    barrier()
+    e2e_ms = a.elapsed_time(b) / e2e_steps
+    if pg is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = STEP_FLOPS * world / (e2e_ms * 1e-3) / 1e9
+
+    # ---- accuracy of this run's outputs vs FP64 (two batches per part)
+    errs = {}
+    for (dt, n), x, y in zip(PARTS, xs, ys):
+        xr = x[:2].cpu().numpy().astype(np.complex128)
+        ref = np.fft.fft(xr, axis=-1)
+        got = y[:2].cpu().numpy().astype(np.complex128)
+        errs["%s_%d" % (dt, n)] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, cores, desc = cpu_sample(1, max_seconds=15.0)
+        cpu = {"value": round(v, 2), "unit": "GFLOP/s", "cores": cores, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        in_bytes = sum(x.numel() * x.element_size() for x in xs)
+        out = {
+            "metric": METRIC, "value": round(value, 1), "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic: iid standard complex normal (seeded torch generator)",
+            "config": {"workload": WORKLOAD, "parts": [f"{d}:{n}x{BATCH}" for d, n in PARTS],
+                       "l2": "inputs larger than L2: %.2f GB of input per step (L2 129 MB)" % (in_bytes / 1e9),
+                       "rel_l2_vs_fp64": {k: float("%.3g" % v) for k, v in errs.items()},
+                       "breakdown": parts},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_value, 1), "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 4)},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(out))
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--only", default=None,
+                    help="run one part only, e.g. c32:262144 (profiling a single plan)")
+    args = ap.parse_args()
+    if args.only:
+        dt, n = args.only.split(":")
+        global PARTS, STEP_FLOPS
+        PARTS = [(dt, int(n))]
+        STEP_FLOPS = sum(flops(nn, BATCH) for _, nn in PARTS)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -101,8 +101,12 @@ struct RealPostParams {
 // Generic elementwise helpers for odd-length real transforms.
 struct CopyParams {
   int64_t n, nbatch, in_bstride, out_bstride;
-  int mode;  // 0: real -> complex, 1: hermitian expand (n real), 2: complex -> real, 3: truncate h+1
-  int64_t nc;  // complex length per batch (mode 1/3)
+  // 0: real -> complex, 1: hermitian expand (n real), 2: complex -> real,
+  // 3: complex copy of n entries, 4: irfft pre-pass Z[k], k < n = h
+  int mode;
+  int64_t nc;          // complex length per batch (mode 1)
+  const void* tab;     // mode 4: e^{+2 pi i k / 2h}
+  double pre;          // mode 4: pair factor (1/2 irfft, 1 brfft)
 };
 
 // A pass kernel specialised at compile time for one radix sequence.

@@ -87,9 +87,22 @@ __global__ void k_copy(const CopyParams cp, const void* __restrict__ in, void* _
   } else if (cp.mode == 2) {  // complex -> real part
     const Cx<T> v = reinterpret_cast<const Cx<T>*>(in)[b * cp.in_bstride + j];
     reinterpret_cast<T*>(out)[b * cp.out_bstride + j] = v.x;
-  } else {  // complex copy of the first n entries
+  } else if (cp.mode == 3) {  // complex copy of the first n entries
     reinterpret_cast<Cx<T>*>(out)[b * cp.out_bstride + j] =
         reinterpret_cast<const Cx<T>*>(in)[b * cp.in_bstride + j];
+  } else {  // irfft pre-pass (FFTJ src/real.jl:149-192) for a resampled inner transform
+    const Cx<T>* X = reinterpret_cast<const Cx<T>*>(in) + b * cp.in_bstride;
+    const int64_t h = cp.n;
+    const Cx<T> a = X[j];
+    Cx<T> bb = X[h - j];
+    bb.y = -bb.y;
+    const T pre = (T)cp.pre;
+    const T xer = (a.x + bb.x) * pre, xei = (a.y + bb.y) * pre;
+    const T xdr = (a.x - bb.x) * pre, xdi = (a.y - bb.y) * pre;
+    const Cx<T> w = reinterpret_cast<const Cx<T>*>(cp.tab)[j];
+    const T tr = fma(w.x, xdr, -(w.y * xdi));
+    const T ti = fma(w.x, xdi, w.y * xdr);
+    reinterpret_cast<Cx<T>*>(out)[b * cp.out_bstride + j] = mk<T>(xer - ti, xei + tr);
   }
 }
 

@@ -627,6 +627,7 @@ int build_c2r_1d(fftj_plan_s* P, i64 n, i64 nb, i64 idist, i64 odist, bool norma
     if (!twd) return fail(FFTJ_ERR_CUDA, "table upload failed");
     PassParams& f = inner.front().pp;
     if (inner.front().kind == OP_PASS && f.load_op == LOAD_PLAIN) {
+      // the pre-pass rides on the first pass's loads
       f.load_op = LOAD_C2R_PRE;
       f.ld_n = h;
       f.ld_stride = idist;
@@ -635,7 +636,23 @@ int build_c2r_1d(fftj_plan_s* P, i64 n, i64 nb, i64 idist, i64 odist, bool norma
       for (auto& o : inner) ops->push_back(o);
       return FFTJ_OK;
     }
-    return fail(FFTJ_ERR_UNSUPPORTED, "irfft of a length whose half is not 13-smooth is not supported yet");
+    // resampled half length: a separate pre-pass feeds the inner transform
+    std::vector<Op> inner2;
+    rc = build_c2c_1d<T>(P, h, nb, h, odist / 2, +1, sc, &inner2, route);
+    if (rc) return rc;
+    Op pre;
+    pre.kind = OP_COPY;
+    pre.cp.mode = 4;
+    pre.cp.n = h;
+    pre.cp.nbatch = nb;
+    pre.cp.in_bstride = idist;
+    pre.cp.out_bstride = h;
+    pre.cp.tab = twd;
+    pre.cp.pre = normalized ? 0.5 : 1.0;
+    pre.dst_bytes = (size_t)(nb * h) * sizeof(T) * 2;
+    ops->push_back(pre);
+    for (auto& o : inner2) ops->push_back(o);
+    return FFTJ_OK;
   }
   // odd n: Hermitian expansion, full complex inverse, real part
   Op ex;

@@ -1,0 +1,378 @@
+"""GPU parity: the sm_103a path (through the C ABI) against the oracle (the
+FFTJ CPU restatement in the config dtype) and FP64 references.
+
+Bar: relative L2 error <= 5 * log2(N) * eps(T) against both the oracle and
+the FP64 reference (the parity bar of the task; tighter than the reference
+suite's 50/100/200 eps classes for N >= 2^10). Full-size configs are checked
+on sampled batches against the oracle and on every batch through
+size-independent properties (inverse round trip, Parseval, exact FP64 bins).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import EPS, parity_tol, rel_l2
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+T_LIST = [np.float32, np.float64]
+CT = {np.float32: torch.complex64, np.float64: torch.complex128}
+RT = {np.float32: torch.float32, np.float64: torch.float64}
+
+
+@pytest.fixture(scope="module")
+def fftj():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    import fftj as F
+    F.build()
+    return F
+
+
+def dev(x, T):
+    t = torch.from_numpy(np.ascontiguousarray(x))
+    t = t.to(CT[T] if np.iscomplexobj(x) else RT[T])
+    return t.cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+def cn(rng, shape):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / np.sqrt(2)
+
+
+def _sizes(golden, prefix):
+    return sorted(int(k[len(prefix):]) for k in golden.files if k.startswith(prefix))
+
+
+# --------------------------------------------------------------------------
+# reference test-suite sizes (test/runtests.jl) against golden and oracle
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_c2c_reference_sizes(fftj, golden, orc, T):
+    for n in _sizes(golden, "c2c_x_"):
+        x = golden["c2c_x_%d" % n]
+        ref = golden["c2c_y_%d" % n]
+        xd = dev(x, T)
+        y = host(fftj.plan_fft(T, n)(xd))
+        tol = parity_tol(T, n)
+        assert rel_l2(y, ref) <= tol, (n, rel_l2(y, ref) / EPS[T])
+        yo = orc.Plan1D(T, n, "fft")(x)
+        assert rel_l2(y, yo) <= tol, (n, "vs oracle", rel_l2(y, yo) / EPS[T])
+        # inverse round trip (runtests.jl:23) and bfft = n * ifft (:76)
+        xi = host(fftj.plan_ifft(T, n)(dev(y, T)))
+        assert rel_l2(xi, x) <= 2 * tol, n
+        xb = host(fftj.plan_bfft(T, n)(dev(ref, T)))
+        assert rel_l2(xb, n * x) <= 2 * tol, n
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_known_answers(fftj, golden, T):
+    for key in golden.files:
+        if not key.startswith("kat_"):
+            continue
+        n = int(key.rsplit("_", 1)[1])
+        y = host(fftj.plan_fft(T, n)(dev(golden[key], T)))
+        if "impulse" in key:
+            assert np.allclose(y, np.ones(n), atol=10 * EPS[T])
+        elif n > 3:
+            exp = np.zeros(n, dtype=np.complex128)
+            exp[3] = n
+            assert rel_l2(y, exp) <= parity_tol(T, n), key
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_real_reference_sizes(fftj, golden, orc, T):
+    for n in _sizes(golden, "r2c_x_"):
+        x = golden["r2c_x_%d" % n]
+        ref = golden["r2c_y_%d" % n]
+        Y = fftj.plan_rfft(T, n)(dev(x, T))
+        assert tuple(Y.shape) == (n // 2 + 1,)
+        tol = max(parity_tol(T, n), 5 * EPS[T])
+        assert rel_l2(host(Y), ref) <= tol, n
+        yo = orc.PlanReal(T, n, "rfft")(x)
+        assert rel_l2(host(Y), yo) <= 2 * tol, (n, "vs oracle")
+        xr = host(fftj.plan_irfft(T, n)(dev(ref, T)))
+        assert rel_l2(xr, x) <= 2 * tol, n
+        xb = host(fftj.plan_brfft(T, n)(dev(ref, T)))
+        assert rel_l2(xb, n * x) <= 2 * tol, n
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_nd_reference_shapes(fftj, golden, orc, T):
+    for key in golden.files:
+        if not key.startswith("nd_x_"):
+            continue
+        dims = [int(v) for v in key[5:].split("x")]
+        if any(not _smooth13(d) for d in dims):
+            continue  # non-smooth N-d dims: covered by test_nd_nonsmooth_dim_rejected
+        n = int(np.prod(dims))
+        tol = 200 * EPS[T]
+        x = golden[key]
+        ref = golden["nd_y_" + key[5:]]
+        y = host(fftj.fft(dev(x, T)))
+        assert rel_l2(y, ref) <= tol, dims
+        assert rel_l2(y, orc.PlanND(T, dims, "fft")(x)) <= tol, dims
+        assert rel_l2(host(fftj.ifft(dev(ref, T))), x) <= tol, dims
+        xr = golden["ndr_x_" + key[5:]]
+        rref = golden["ndr_y_" + key[5:]]
+        Y = fftj.rfft(dev(xr, T))
+        assert tuple(Y.shape) == rref.shape and rel_l2(host(Y), rref) <= tol, dims
+        assert rel_l2(host(fftj.irfft(dev(rref, T), dims[0])), xr) <= tol, dims
+        assert rel_l2(host(fftj.brfft(dev(rref, T), dims[0])), n * xr) <= tol, dims
+
+
+def _smooth13(n):
+    for p in (2, 3, 5, 7, 11, 13):
+        while n % p == 0:
+            n //= p
+    return n == 1
+
+
+def test_nd_nonsmooth_dim_rejected(fftj):
+    x = torch.zeros((17, 16), dtype=torch.complex64, device="cuda")
+    with pytest.raises(fftj.FFTJError):
+        fftj.fft(x)
+
+
+# --------------------------------------------------------------------------
+# BASELINE configs at full size
+
+
+def test_config_c64_2e16_batch64(fftj, orc):
+    """Plain 1-D forward ComplexF64 FFT, N=2^16, batch 64, U[-1,1) re/im,
+    compared to the FFTJ CPU plan (oracle) and FP64 pocketfft."""
+    n, B = 1 << 16, 64
+    rng = np.random.default_rng(0xF17)
+    x = rng.uniform(-1, 1, (B, n)) + 1j * rng.uniform(-1, 1, (B, n))
+    y = host(fftj.plan_fft(np.float64, n, batch=B)(dev(x, np.float64)))
+    tol = parity_tol(np.float64, n)
+    assert rel_l2(y, orc.Plan1D(np.float64, n, "fft")(x)) <= tol
+    assert rel_l2(y, np.fft.fft(x, axis=-1)) <= tol
+
+
+@pytest.mark.parametrize("T", T_LIST)
+@pytest.mark.parametrize("n", [42525, 10007, 1 << 18])
+def test_config_mixed_prime_batch128(fftj, orc, T, n):
+    """ComplexF32/F64 at N = 42525 (3^5 5^2 7), 10007 (prime: resampled) and
+    2^18, batch 128, iid standard complex normal: all batches against FP64,
+    four sampled batches against the oracle, forward+inverse round trip."""
+    B = 128
+    rng = np.random.default_rng([0xC0F1, n])
+    x = cn(rng, (B, n))
+    xd = dev(x, T)
+    y = fftj.plan_fft(T, n, batch=B)(xd)
+    yh = host(y)
+    tol = parity_tol(T, n)
+    assert rel_l2(yh, np.fft.fft(x, axis=-1)) <= tol
+    pick = [0, 1, 63, 127]
+    assert rel_l2(yh[pick], orc.Plan1D(T, n, "fft")(x[pick])) <= tol
+    xi = host(fftj.plan_ifft(T, n, batch=B)(y))
+    assert rel_l2(xi, x) <= 2 * tol
+
+
+def _dft_bins(x, ks, sign=-1):
+    """Exact-ish FP64 DFT bins X[k] of a long vector (numpy, float64)."""
+    n = x.shape[-1]
+    j = np.arange(n, dtype=np.int64)
+    out = []
+    for k in ks:
+        e = (j * int(k)) % n
+        w = np.exp(sign * 2j * np.pi * e / n)
+        out.append(np.dot(x.astype(np.complex128), w))
+    return np.array(out)
+
+
+@pytest.mark.parametrize("T,logn", [(np.float32, 26), (np.float64, 24)])
+def test_config_large_single(fftj, T, logn):
+    """Single ComplexF32 2^26 / ComplexF64 2^24 (U[-1,1)): sampled FP64 bins,
+    Parseval, inverse round trip."""
+    n = 1 << logn
+    rng = np.random.default_rng(logn)
+    x = (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)).astype(np.complex64 if T == np.float32 else np.complex128)
+    xd = dev(x, T)
+    y = fftj.plan_fft(T, n)(xd)
+    yh = host(y)
+    ks = [0, 1, 7, n // 3, n // 2, n - 1, 12345, n // 2 + 17]
+    ref = _dft_bins(x, ks)
+    # per-bin error relative to the rms bin magnitude (sqrt(n) * rms(x))
+    scale = np.sqrt(n) * np.sqrt(np.mean(np.abs(x.astype(np.complex128)) ** 2))
+    assert np.max(np.abs(yh[ks] - ref)) / scale <= 4 * parity_tol(T, n)
+    # Parseval
+    px = np.sum(np.abs(x.astype(np.complex128)) ** 2) * n
+    py = np.sum(np.abs(yh.astype(np.complex128)) ** 2)
+    assert abs(py - px) / px <= parity_tol(T, n)
+    xi = host(fftj.plan_ifft(T, n)(y))
+    assert rel_l2(xi, x) <= 2 * parity_tol(T, n)
+
+
+def test_config_rfft_2e25_batch4(fftj):
+    """Float32 rfft / irfft N=2^25, batch 4, U[-1,1)."""
+    n, B = 1 << 25, 4
+    rng = np.random.default_rng(25)
+    x = rng.uniform(-1, 1, (B, n)).astype(np.float32)
+    Y = fftj.plan_rfft(np.float32, n, batch=B)(dev(x, np.float32))
+    assert tuple(Y.shape) == (B, n // 2 + 1)
+    Yh = host(Y)
+    tol = parity_tol(np.float32, n)
+    ks = [0, 1, 5, n // 4, n // 2, 999]
+    for b in (0, 3):
+        ref = _dft_bins(x[b], ks)
+        scale = np.sqrt(n) * np.sqrt(np.mean(x[b].astype(np.float64) ** 2))
+        assert np.max(np.abs(Yh[b, ks] - ref)) / scale <= 4 * tol
+    xr = host(fftj.plan_irfft(np.float32, n, batch=B)(Y))
+    assert rel_l2(xr, x) <= 2 * tol
+
+
+def _stress(rng, shape):
+    x = cn(rng, shape)
+    flat = x.reshape(-1)
+    idx = rng.choice(flat.size, size=flat.size // 100, replace=False)
+    flat[idx] *= 1e3
+    return x
+
+
+def test_config_precision_2e20_batch64(fftj):
+    """ComplexF32 2^20, batch 64, standard complex normal with 1% of entries
+    x1e3: plain FP32 form against the FP64 reference."""
+    n, B = 1 << 20, 64
+    rng = np.random.default_rng(20)
+    x = _stress(rng, (B, n)).astype(np.complex64)
+    y = host(fftj.plan_fft(np.float32, n, batch=B)(dev(x, np.float32)))
+    pick = [0, 31, 63]
+    ref = np.fft.fft(x[pick].astype(np.complex128), axis=-1)
+    assert rel_l2(y[pick], ref) <= parity_tol(np.float32, n)
+
+
+def test_config_precision_2d_4096(fftj, orc):
+    """ComplexF32 2-D 4096x4096 with the 1% x1e3 stress entries."""
+    rng = np.random.default_rng(4096)
+    x = _stress(rng, (4096, 4096)).astype(np.complex64)
+    y = host(fftj.fft(dev(x, np.float32)))
+    ref = np.fft.fft2(x.astype(np.complex128))
+    assert rel_l2(y, ref) <= parity_tol(np.float32, 4096 * 4096)
+
+
+def test_config_rfft3d_256(fftj):
+    """Float32 256^3 3-D rfft (and its irfft) against FP64 numpy."""
+    rng = np.random.default_rng(256)
+    x = rng.standard_normal((256, 256, 256)).astype(np.float32)
+    Y = fftj.rfft(dev(x, np.float32))
+    assert tuple(Y.shape) == (256, 256, 129)
+    ref = np.fft.rfftn(x.astype(np.float64))
+    tol = parity_tol(np.float32, 256 ** 3)
+    assert rel_l2(host(Y), ref) <= tol
+    assert rel_l2(host(fftj.irfft(Y, 256)), x) <= 2 * tol
+
+
+# --------------------------------------------------------------------------
+# API idioms (test/runtests.jl:264-328), in-place, strides, streams
+
+
+@pytest.mark.parametrize("T", T_LIST)
+@pytest.mark.parametrize("n", [96, 11])
+def test_api_idioms(fftj, T, n):
+    rng = np.random.default_rng(0xC0A7)
+    x = cn(rng, n)
+    xr = rng.standard_normal(n)
+    tol = 100 * EPS[T]
+    xd = dev(x, T)
+    p = fftj.plan_fft(xd, flags="ignored")
+    assert rel_l2(host(p * xd), np.fft.fft(x)) <= tol
+    y = torch.empty_like(xd)
+    assert fftj.mul_(y, p, xd) is y
+    assert rel_l2(host(y), np.fft.fft(x)) <= tol
+    assert rel_l2(host(fftj.plan_bfft(xd) * xd), n * np.fft.ifft(x)) <= tol
+    # in place: DSP's p! * buf; inv(p!).p
+    pin = fftj.plan_fft_(xd)
+    z = xd.clone()
+    assert (pin * z) is z
+    assert rel_l2(host(z), np.fft.fft(x)) <= tol
+    ip = fftj.inv(pin).p
+    assert (ip * z) is z
+    assert rel_l2(host(z), n * x) <= tol
+    z2 = xd.clone()
+    pin * z2
+    fftj.inv(pin) * z2
+    assert rel_l2(host(z2), x) <= tol
+    # rfft / brfft (DSP _fftfilt!)
+    xrd = dev(xr, T)
+    pr = fftj.plan_rfft(xrd)
+    X = pr * xrd
+    assert rel_l2(host(X), np.fft.rfft(xr)) <= tol
+    pbr = fftj.plan_brfft(X, n)
+    assert rel_l2(host(pbr * X), n * np.fft.irfft(np.fft.rfft(xr), n)) <= tol
+    # one-shots
+    assert rel_l2(host(fftj.fft(xd)), np.fft.fft(x)) <= tol
+    assert rel_l2(host(fftj.ifft(xd)), np.fft.ifft(x)) <= tol
+    assert rel_l2(host(fftj.bfft(xd)), n * np.fft.ifft(x)) <= tol
+    assert rel_l2(host(fftj.rfft(xrd)), np.fft.rfft(xr)) <= tol
+    assert rel_l2(host(fftj.irfft(X, n)), xr) <= tol
+    assert rel_l2(host(fftj.fft_(xd.clone())), np.fft.fft(x)) <= tol
+    assert fftj.size(p) == (n,) and fftj.size(pbr) == (n // 2 + 1,)
+    # region validation and DimensionMismatch (runtests.jl:327, 426)
+    with pytest.raises(fftj.ArgumentError):
+        fftj.plan_fft(xd, 2)
+    with pytest.raises(fftj.DimensionMismatch):
+        p(torch.zeros(n + 1, dtype=CT[T], device="cuda"))
+    with pytest.raises(fftj.ArgumentError):
+        p(torch.zeros(n, dtype=CT[T]))  # host tensor: there is no CPU path
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_inplace_and_determinism(fftj, T):
+    rng = np.random.default_rng(7)
+    for n, B in ((4096, 8), (42525, 3), (1 << 18, 2), (10007, 4)):
+        x = dev(cn(rng, (B, n)), T)
+        p = fftj.plan_fft(T, n, batch=B)
+        y1 = p(x)
+        y2 = p(x)
+        assert torch.equal(y1, y2), n  # bitwise run-to-run
+        z = x.clone()
+        p(z, z)
+        assert torch.equal(z, y1), n   # in == out
+
+
+def test_strided_batches_c_abi(fftj):
+    """idist/odist > n through the C ABI (padded rows)."""
+    L = fftj.lib()
+    n, B, idist, odist = 1000, 5, 1024, 1100
+    rng = np.random.default_rng(3)
+    x = cn(rng, (B, idist)).astype(np.complex64)
+    xd = dev(x, np.float32)
+    yd = torch.zeros((B, odist), dtype=torch.complex64, device="cuda")
+    h = ctypes.c_void_p()
+    dims = (ctypes.c_int64 * 1)(n)
+    assert L.fftj_plan_c2c(ctypes.byref(h), 0, 1, dims, B, idist, odist, -1, 1.0) == 0
+    try:
+        assert L.fftj_execute(h, ctypes.c_void_p(xd.data_ptr()), ctypes.c_void_p(yd.data_ptr()), None) == 0
+        torch.cuda.synchronize()
+        y = host(yd)
+        assert rel_l2(y[:, :n], np.fft.fft(x[:, :n], axis=-1)) <= parity_tol(np.float32, n)
+        assert np.all(y[:, n:] == 0)
+    finally:
+        L.fftj_plan_destroy(h)
+
+
+def test_nondefault_stream(fftj):
+    rng = np.random.default_rng(11)
+    n, B = 1 << 16, 16
+    x = dev(cn(rng, (B, n)), np.float32)
+    p = fftj.plan_fft(np.float32, n, batch=B)
+    ref = p(x)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        y = p(x)
+    s.synchronize()
+    assert torch.equal(y, ref)
+
+
+def test_library_loaded_from_tree(fftj):
+    import os
+    assert os.path.dirname(fftj._build.LIB).endswith("fftj.jl_gb300")
+    assert fftj.lib()._name == fftj._build.LIB
