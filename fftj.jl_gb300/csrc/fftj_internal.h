@@ -121,6 +121,25 @@ template <typename T, int DIR>
 const RecipeEntry* recipe_table(int* count);
 
 // fn: a recipe kernel (RecipeEntry::fn) or nullptr for the generic kernel.
+// Planner pieces shared by the plan builder and the allocation-free entry
+// point (all heap-free).
+struct DtypeCfg {
+  int esize;        // bytes per complex element
+  int tile_max;     // preferred elements per CTA tile (one shared buffer)
+  int tile_cap;     // largest tile (shared memory / 16 elements per thread)
+  int threads_max;  // CTA size bound of the kernel
+  int rmax_multi;   // largest per-pass radix when more than one pass
+  int min_run;      // minimum contiguous elements per tile row (coalescing)
+};
+DtypeCfg dtype_cfg(bool f64);
+int pass_radices(int64_t n, bool f64, bool strided, int64_t* Rs, int cap);
+int sub_radices(int64_t R, int* out, int cap);
+int pass_geometry(PassParams& pp, bool f64, int64_t R, int64_t m, int64_t s, int64_t ncur, int64_t nbatch,
+                  int64_t ibs, int64_t obs);
+void outer_twiddle_layout(PassParams& pp, bool f64);
+const void* pick_pass_kernel(bool f64, int dir, const PassParams& pp);
+void set_error(const char* msg);
+
 template <typename T>
 cudaError_t launch_pass(const PassParams& pp, int dir, const void* fn, const void* in, void* out,
                         cudaStream_t st);

@@ -156,15 +156,30 @@ Resample resample_parts(i64 n, bool f64, double scale) {
   return r;
 }
 
-// ---- pass decomposition ----------------------------------------------------
-struct DtypeCfg {
-  int esize;        // bytes per complex element
-  int tile_max;     // preferred elements per CTA tile (one shared buffer)
-  int tile_cap;     // largest tile (shared memory / 16 elements per thread)
-  int threads_max;  // CTA size bound of the kernel
-  int rmax_multi;   // largest per-pass radix when more than one pass
-  int min_run;      // minimum contiguous elements per tile row (coalescing)
-};
+// split the prime multiset into k bins with every bin <= rmax (LPT on logs);
+// bins sorted descending. Heap-free.
+bool split_bins(const int* primes, int np, int k, i64 rmax, i64* bins) {
+  int ps[64];
+  for (int i = 0; i < np; ++i) ps[i] = primes[i];
+  std::sort(ps, ps + np, [](int x, int y) { return x > y; });
+  for (int i = 0; i < k; ++i) bins[i] = 1;
+  for (int i = 0; i < np; ++i) {
+    int best = 0;
+    for (int j = 1; j < k; ++j)
+      if (bins[j] < bins[best]) best = j;
+    bins[best] *= ps[i];
+  }
+  for (int i = 0; i < k; ++i)
+    if (bins[i] > rmax) return false;
+  std::sort(bins, bins + k, [](i64 x, i64 y) { return x > y; });
+  return true;
+}
+
+}  // namespace
+
+namespace fftj {
+
+// ---- pass decomposition ----
 int env_int(const char* name, int dflt) {
   const char* v = std::getenv(name);
   return v && *v ? std::atoi(v) : dflt;
@@ -176,56 +191,6 @@ DtypeCfg dtype_cfg(bool f64) {
   return DtypeCfg{8, env_int("FFTJ_TILE_F32", 4096), 8192, 512, 1024, 8};
 }
 
-// split the prime multiset into k bins with every bin <= rmax (LPT on logs)
-bool split_bins(const std::vector<int>& primes, int k, i64 rmax, std::vector<i64>* bins) {
-  std::vector<int> ps(primes);
-  std::sort(ps.rbegin(), ps.rend());
-  std::vector<i64> b(k, 1);
-  for (int p : ps) {
-    int best = 0;
-    for (int i = 1; i < k; ++i)
-      if (b[i] < b[best]) best = i;
-    b[best] *= p;
-  }
-  for (i64 v : b)
-    if (v > rmax) return false;
-  std::sort(b.rbegin(), b.rend());
-  *bins = b;
-  return true;
-}
-
-// Passes of a length-n axis: one pass when the whole transform fits a tile
-// and the axis is contiguous; otherwise the fewest passes whose radices keep
-// >= min_run contiguous elements per tile row.
-std::vector<i64> pass_radices(i64 n, const DtypeCfg& cfg, bool strided) {
-  std::vector<int> primes;
-  smooth13(n, &primes);
-  if (!strided && n <= cfg.tile_cap) return {n};
-  if (n <= cfg.rmax_multi) return {n};
-  for (int k = 1; k < 16; ++k) {
-    std::vector<i64> bins;
-    if (split_bins(primes, k, cfg.rmax_multi, &bins)) return bins;
-  }
-  return {};
-}
-
-// sub-radix sequence of one pass: odd primes first, then the power-of-two
-// part as balanced radix-16/8/4/2 sub-stages
-std::vector<int> sub_radices(i64 R) {
-  std::vector<int> out;
-  i64 r = R;
-  int a = 0;
-  while (r % 2 == 0) { r /= 2; a++; }
-  for (int p : {3, 5, 7, 11, 13})
-    while (r % p == 0) { r /= p; out.push_back(p); }
-  if (a > 0) {
-    int k = (a + 3) / 4;
-    int base = a / k, extra = a % k;
-    for (int i = 0; i < k; ++i) out.push_back(1 << (base + (i < extra ? 1 : 0)));
-  }
-  if (out.empty()) out.push_back(1);
-  return out;
-}
 
 i64 largest_divisor_le(i64 n, i64 cap) {
   if (cap >= n) return n;
@@ -233,6 +198,184 @@ i64 largest_divisor_le(i64 n, i64 cap) {
     if (n % d == 0) return d;
   return 1;
 }
+
+// Passes of a length-n axis: one pass when the whole transform fits a tile
+// and the axis is contiguous; otherwise the fewest passes whose radices keep
+// >= min_run contiguous elements per tile row. Heap-free; returns the pass
+// count (0: no decomposition within cap passes).
+int pass_radices(i64 n, bool f64, bool strided, i64* Rs, int cap) {
+  const DtypeCfg cfg = dtype_cfg(f64);
+  int primes[64];
+  int np = 0;
+  i64 r = n;
+  for (int p : {2, 3, 5, 7, 11, 13})
+    while (r % p == 0 && np < 64) { r /= p; primes[np++] = p; }
+  if (r != 1 || n < 1) return 0;
+  if ((!strided && n <= cfg.tile_cap) || n <= cfg.rmax_multi) { Rs[0] = n; return 1; }
+  for (int k = 1; k <= cap && k < 16; ++k)
+    if (split_bins(primes, np, k, cfg.rmax_multi, Rs)) return k;
+  return 0;
+}
+
+// sub-radix sequence of one pass: odd primes first, then the power-of-two
+// part as balanced radix-16/8/4/2 sub-stages (larger first). Returns the count.
+int sub_radices(i64 R, int* out, int cap) {
+  int k = 0;
+  i64 r = R;
+  int a = 0;
+  while (r % 2 == 0) { r /= 2; a++; }
+  for (int p : {3, 5, 7, 11, 13})
+    while (r % p == 0 && k < cap) { r /= p; out[k++] = p; }
+  if (a > 0) {
+    const int parts = (a + 3) / 4;
+    const int base = a / parts, extra = a % parts;
+    for (int i = 0; i < parts && k < cap; ++i) out[k++] = 1 << (base + (i < extra ? 1 : 0));
+  }
+  if (k == 0) out[k++] = 1;
+  return k;
+}
+
+// Everything of a pass but its tables, scale and load op: sub-stages, tile
+// (columns of batch x p x q), threads per column, kernel mappings and
+// shared memory. Heap-free.
+int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 nbatch, i64 ibs, i64 obs) {
+  const DtypeCfg cfg = dtype_cfg(f64);
+  if (ncur >= ((i64)1 << 31)) return fail(FFTJ_ERR_UNSUPPORTED, "transform length must be below 2^31");
+  pp.R = (int)R;
+  int subs[kMaxSub + 4];
+  const int ns = sub_radices(R, subs, kMaxSub + 4);
+  if (ns > kMaxSub) return fail(FFTJ_ERR_UNSUPPORTED, "too many sub-stages");
+  pp.nsub = 0;
+  i64 S = 1;
+  for (int i = 0; i < ns; ++i) {
+    const int r = subs[i];
+    if (r == 1) continue;
+    SubStage& ss = pp.sub[pp.nsub++];
+    ss.r = r;
+    ss.S = (int)S;
+    ss.fS = FastDiv((uint32_t)S);
+    ss.Rr = (int)(R / r);
+    S *= r;
+  }
+  pp.m = m;
+  pp.s = s;
+  pp.ncur = ncur;
+  pp.in_bstride = ibs;
+  pp.out_bstride = obs;
+  pp.nbatch = nbatch;
+    // threads per tile column: every sub-stage's butterflies fit the
+    // per-thread register budget (max(1, 16/r) butterflies, <= 16 elements)
+    auto tf_ok = [&](i64 tf) {
+      if ((R + tf - 1) / tf > 16) return false;
+      for (int i = 0; i < pp.nsub; ++i) {
+        const int r = pp.sub[i].r;
+        const i64 cap = std::max(1, 16 / r);
+        if ((pp.sub[i].Rr + tf - 1) / tf > cap) return false;
+      }
+      return true;
+    };
+    i64 Tf = 1;
+    while (!tf_ok(Tf)) Tf++;
+    // tile: columns (batch, p, q); NB * Tf threads. Passes over strided
+    // data keep >= min_run columns (contiguous elements per HBM run).
+    const bool one_pass = (m == 1 && s == 1);
+    i64 tmax = std::max<i64>(cfg.tile_max, R);
+    if (!one_pass) tmax = std::min<i64>(std::max<i64>(tmax, R * cfg.min_run), std::max<i64>(cfg.tile_cap, R));
+    i64 cols = std::max<i64>(1, std::min<i64>(tmax / R, cfg.threads_max / Tf));
+    if (Tf > cfg.threads_max) return fail(FFTJ_ERR_UNSUPPORTED, "pass radix needs too many threads");
+    i64 Pt = 1, Qt = 1, NBt = 1;
+    if (s == 1) {
+      Pt = largest_divisor_le(m, cols);
+      if (Pt == m) NBt = std::max<i64>(1, cols / m);
+    } else {
+      Qt = largest_divisor_le(s, cols);
+      if (Qt == s) {
+        Pt = largest_divisor_le(m, cols / Qt);
+        if (Pt == m) NBt = std::max<i64>(1, cols / (m * s));
+      }
+    }
+    NBt = std::min(NBt, nbatch);
+    pp.P = (int)Pt;
+    pp.Q = (int)Qt;
+    pp.NBt = (int)NBt;
+    pp.NB = (int)(Pt * Qt * NBt);
+    pp.Tf = (int)Tf;
+    pp.ept = (int)((R + Tf - 1) / Tf);
+    pp.fQ = FastDiv((uint32_t)Qt);
+    pp.fP = FastDiv((uint32_t)Pt);
+    pp.fR = FastDiv((uint32_t)R);
+    pp.fNB = FastDiv((uint32_t)pp.NB);
+    pp.tiles_q = (uint32_t)(s / Qt);
+    pp.tiles_p = (uint32_t)(m / Pt);
+    pp.tiles_b = (uint32_t)((nbatch + NBt - 1) / NBt);
+    pp.ftq = FastDiv(pp.tiles_q);
+    pp.ftp = FastDiv(pp.tiles_p);
+    const double ntiles = (double)pp.tiles_q * pp.tiles_p * pp.tiles_b;
+    if (ntiles >= 2147483647.0) return fail(FFTJ_ERR_UNSUPPORTED, "grid too large");
+    const i64 E = (i64)pp.NB * R;
+    pp.threads = (int)(pp.NB * Tf);
+    // lanes walk j where the transform axis is contiguous in HBM
+    pp.load_rows = (m == 1 && s == 1) ? 1 : 0;
+    pp.store_rows = (s == 1) ? 1 : 0;
+    if ((pp.load_rows || pp.store_rows) && (E + pp.threads - 1) / pp.threads > 16)
+      return fail(FFTJ_ERR_UNSUPPORTED, "tile exceeds 16 elements per thread");
+    const int padsh = f64 ? 3 : 4;
+    pp.smem_elems = (int)(E + (E >> padsh) + 2);
+  return FFTJ_OK;
+}
+
+// outer twiddle table layout of a pass: none (last pass), full table
+// w_ncur^e, or two-level hi[e >> sh] * lo[e & (2^sh - 1)]
+void outer_twiddle_layout(PassParams& pp, bool f64) {
+  pp.tw_mode = 0;
+  if (pp.m <= 1) return;
+  const i64 ncur = pp.ncur;
+  // first passes (s == 1) store along j, so their twiddle exponents p*j
+  // scatter: F32 reads the small two-level tables (L1-resident) there
+  const i64 full_max = f64 ? (1 << 21) : (pp.s == 1 && env_int("FFTJ_TW_FIRST_FULL", 0) == 0 ? 0 : (1 << 22));
+  if (ncur <= full_max) {
+    pp.tw_mode = 1;
+    return;
+  }
+  int sh = 0;
+  while (((i64)1 << (2 * sh)) < ncur) sh++;
+  pp.tw_mode = 2;
+  pp.tw_shift = sh;
+}
+
+// The compile-time recipe kernel matching a pass (same radix sequence, load
+// op, direction, threads per column and mapping mode), else nullptr (the
+// generic kernel). Heap-free.
+template <typename T>
+const void* pick_pass_kernel_t(int dir, const PassParams& pp) {
+  int count = 0;
+  const RecipeEntry* tab = dir < 0 ? recipe_table<T, -1>(&count) : recipe_table<T, 1>(&count);
+  int mode = -1;
+  if (pp.load_rows && pp.store_rows && (pp.NBt == 1 || pp.out_bstride == (int64_t)pp.R)) mode = 0;
+  else if (!pp.load_rows && pp.store_rows && pp.NBt == 1) mode = 1;
+  else if (!pp.load_rows && !pp.store_rows) mode = 2;
+  for (int i = 0; i < count && mode >= 0; ++i) {
+    const RecipeEntry& e = tab[i];
+    if (e.mode != mode || e.load_op != pp.load_op || e.Tf != pp.Tf) continue;
+    int n = 0;
+    while (n < 6 && e.radix[n]) n++;
+    if (n != pp.nsub) continue;
+    bool same = true;
+    for (int j = 0; j < n; ++j) same = same && e.radix[j] == pp.sub[j].r;
+    if (same) return e.fn;
+  }
+  return nullptr;
+}
+const void* pick_pass_kernel(bool f64, int dir, const PassParams& pp) {
+  return f64 ? pick_pass_kernel_t<double>(dir, pp) : pick_pass_kernel_t<float>(dir, pp);
+}
+
+void set_error(const char* msg) { g_err = msg; }
+
+}  // namespace fftj
+
+namespace {
+
 
 }  // namespace
 
@@ -326,9 +469,10 @@ template <typename T>
 int build_axis_passes(fftj_plan_s* P, i64 n, i64 Bi, i64 nbatch, i64 ibs, i64 obs, int dir, double scale,
                       std::vector<Op>* out_ops) {
   const bool f64 = sizeof(T) == 8;
-  const DtypeCfg cfg = dtype_cfg(f64);
-  std::vector<i64> Rs = pass_radices(n, cfg, Bi > 1);
-  if (Rs.empty()) return fail(FFTJ_ERR_UNSUPPORTED, "no pass decomposition for length " + std::to_string(n));
+  i64 Rbuf[16];
+  const int npass = pass_radices(n, f64, Bi > 1, Rbuf, 16);
+  if (npass == 0) return fail(FFTJ_ERR_UNSUPPORTED, "no pass decomposition for length " + std::to_string(n));
+  std::vector<i64> Rs(Rbuf, Rbuf + npass);
   i64 s1 = 1;  // 1-D stride before this pass
   i64 ncur = n;
   for (size_t pi = 0; pi < Rs.size(); ++pi) {
@@ -339,109 +483,25 @@ int build_axis_passes(fftj_plan_s* P, i64 n, i64 Bi, i64 nbatch, i64 ibs, i64 ob
     PassParams& pp = op.pp;
     std::memset(&pp, 0, sizeof(pp));
     pp.R = (int)R;
-    std::vector<int> subs = sub_radices(R);
-    if ((int)subs.size() > kMaxSub) return fail(FFTJ_ERR_UNSUPPORTED, "too many sub-stages");
-    pp.nsub = 0;
-    i64 S = 1;
-    for (int r : subs) {
-      if (r == 1) continue;
-      SubStage& ss = pp.sub[pp.nsub++];
-      ss.r = r;
-      ss.S = (int)S;
-      ss.fS = FastDiv((uint32_t)S);
-      ss.Rr = (int)(R / r);
-      S *= r;
-    }
     const i64 m = ncur / R;
     const i64 s = s1 * Bi;  // effective stride
-    if (ncur >= ((i64)1 << 31)) return fail(FFTJ_ERR_UNSUPPORTED, "transform length must be below 2^31");
-    pp.m = m;
-    pp.s = s;
-    pp.ncur = ncur;
-    pp.in_bstride = ibs;
-    pp.out_bstride = obs;
-    pp.nbatch = nbatch;
-    // threads per tile column: every sub-stage's butterflies fit the
-    // per-thread register budget (max(1, 16/r) butterflies, <= 16 elements)
-    auto tf_ok = [&](i64 tf) {
-      if ((R + tf - 1) / tf > 16) return false;
-      for (int i = 0; i < pp.nsub; ++i) {
-        const int r = pp.sub[i].r;
-        const i64 cap = std::max(1, 16 / r);
-        if ((pp.sub[i].Rr + tf - 1) / tf > cap) return false;
-      }
-      return true;
-    };
-    i64 Tf = 1;
-    while (!tf_ok(Tf)) Tf++;
-    // tile: columns (batch, p, q); NB * Tf threads. Passes over strided
-    // data keep >= min_run columns (contiguous elements per HBM run).
-    const bool one_pass = (m == 1 && s == 1);
-    i64 tmax = std::max<i64>(cfg.tile_max, R);
-    if (!one_pass) tmax = std::min<i64>(std::max<i64>(tmax, R * cfg.min_run), std::max<i64>(cfg.tile_cap, R));
-    i64 cols = std::max<i64>(1, std::min<i64>(tmax / R, cfg.threads_max / Tf));
-    if (Tf > cfg.threads_max) return fail(FFTJ_ERR_UNSUPPORTED, "pass radix needs too many threads");
-    i64 Pt = 1, Qt = 1, NBt = 1;
-    if (s == 1) {
-      Pt = largest_divisor_le(m, cols);
-      if (Pt == m) NBt = std::max<i64>(1, cols / m);
-    } else {
-      Qt = largest_divisor_le(s, cols);
-      if (Qt == s) {
-        Pt = largest_divisor_le(m, cols / Qt);
-        if (Pt == m) NBt = std::max<i64>(1, cols / (m * s));
-      }
+    {
+      int grc = pass_geometry(pp, f64, R, m, s, ncur, nbatch, ibs, obs);
+      if (grc) return grc;
     }
-    NBt = std::min(NBt, nbatch);
-    pp.P = (int)Pt;
-    pp.Q = (int)Qt;
-    pp.NBt = (int)NBt;
-    pp.NB = (int)(Pt * Qt * NBt);
-    pp.Tf = (int)Tf;
-    pp.ept = (int)((R + Tf - 1) / Tf);
-    pp.fQ = FastDiv((uint32_t)Qt);
-    pp.fP = FastDiv((uint32_t)Pt);
-    pp.fR = FastDiv((uint32_t)R);
-    pp.fNB = FastDiv((uint32_t)pp.NB);
-    pp.tiles_q = (uint32_t)(s / Qt);
-    pp.tiles_p = (uint32_t)(m / Pt);
-    pp.tiles_b = (uint32_t)((nbatch + NBt - 1) / NBt);
-    pp.ftq = FastDiv(pp.tiles_q);
-    pp.ftp = FastDiv(pp.tiles_p);
-    const double ntiles = (double)pp.tiles_q * pp.tiles_p * pp.tiles_b;
-    if (ntiles >= 2147483647.0) return fail(FFTJ_ERR_UNSUPPORTED, "grid too large");
-    const i64 E = (i64)pp.NB * R;
-    pp.threads = (int)(pp.NB * Tf);
-    // lanes walk j where the transform axis is contiguous in HBM
-    pp.load_rows = (m == 1 && s == 1) ? 1 : 0;
-    pp.store_rows = (s == 1) ? 1 : 0;
-    if ((pp.load_rows || pp.store_rows) && (E + pp.threads - 1) / pp.threads > 16)
-      return fail(FFTJ_ERR_UNSUPPORTED, "tile exceeds 16 elements per thread");
-    const int padsh = f64 ? 3 : 4;
-    pp.smem_elems = (int)(E + (E >> padsh) + 2);
     // inner twiddles w_R^t
     pp.twR = omega_table<T>(P, R, R, 1, dir);
     if (!pp.twR) return fail(FFTJ_ERR_CUDA, "table upload failed");
     // outer twiddles w_ncur^(p*j), p*j < ncur
-    if (m > 1) {
-      // first passes (s == 1) store along j, so their twiddle exponents p*j
-      // scatter: F32 reads the small two-level tables (L1-resident) there
-      const i64 full_max = f64 ? (1 << 21) : (s == 1 && env_int("FFTJ_TW_FIRST_FULL", 0) == 0 ? 0 : (1 << 22));
-      if (ncur <= full_max) {
-        pp.tw_mode = 1;
-        pp.tw_full = omega_table<T>(P, ncur, ncur, 1, dir);
-        if (!pp.tw_full) return fail(FFTJ_ERR_CUDA, "table upload failed");
-      } else {
-        int sh = 0;
-        while (((i64)1 << (2 * sh)) < ncur) sh++;
-        const i64 K = (i64)1 << sh;
-        const i64 nh = (ncur + K - 1) / K;
-        pp.tw_mode = 2;
-        pp.tw_shift = sh;
-        pp.tw_hi = omega_table<T>(P, ncur, nh, K, dir);
-        pp.tw_lo = omega_table<T>(P, ncur, K, 1, dir);
-        if (!pp.tw_hi || !pp.tw_lo) return fail(FFTJ_ERR_CUDA, "table upload failed");
-      }
+    outer_twiddle_layout(pp, f64);
+    if (pp.tw_mode == 1) {
+      pp.tw_full = omega_table<T>(P, ncur, ncur, 1, dir);
+      if (!pp.tw_full) return fail(FFTJ_ERR_CUDA, "table upload failed");
+    } else if (pp.tw_mode == 2) {
+      const i64 K = (i64)1 << pp.tw_shift;
+      pp.tw_hi = omega_table<T>(P, ncur, (ncur + K - 1) / K, K, dir);
+      pp.tw_lo = omega_table<T>(P, ncur, K, 1, dir);
+      if (!pp.tw_hi || !pp.tw_lo) return fail(FFTJ_ERR_CUDA, "table upload failed");
     }
     pp.scale = (pi + 1 == Rs.size()) ? scale : 1.0;
     pp.load_op = LOAD_PLAIN;
@@ -773,30 +833,14 @@ int check_dims(int rank, const int64_t* dims, std::vector<i64>* out) {
 // Pick the compile-time recipe kernel matching a pass (same radix sequence,
 // load op, direction and threads per column), else the generic kernel, and
 // opt it into its shared memory.
+// Pick each pass's kernel (compile-time recipe or generic) and opt it into
+// its shared memory.
 template <typename T>
 int finalize_passes(fftj_plan_s* P) {
   for (auto& op : P->ops) {
     if (op.kind != OP_PASS) continue;
-    const PassParams& pp = op.pp;
-    op.kfn = nullptr;
-    int count = 0;
-    const RecipeEntry* tab = op.dir < 0 ? recipe_table<T, -1>(&count) : recipe_table<T, 1>(&count);
-    // the kernel mode this pass needs (see pass_fused in pass_common.cuh)
-    int mode = -1;
-    if (pp.load_rows && pp.store_rows && (pp.NBt == 1 || pp.out_bstride == (int64_t)pp.R)) mode = 0;
-    else if (!pp.load_rows && pp.store_rows && pp.NBt == 1) mode = 1;
-    else if (!pp.load_rows && !pp.store_rows) mode = 2;
-    for (int i = 0; i < count && mode >= 0; ++i) {
-      const RecipeEntry& e = tab[i];
-      if (e.mode != mode || e.load_op != pp.load_op || e.Tf != pp.Tf) continue;
-      int n = 0;
-      while (n < 6 && e.radix[n]) n++;
-      if (n != pp.nsub) continue;
-      bool same = true;
-      for (int j = 0; j < n; ++j) same = same && e.radix[j] == pp.sub[j].r;
-      if (same) { op.kfn = e.fn; break; }
-    }
-    if (prepare_pass<T>(pp, op.dir, op.kfn) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
+    op.kfn = pick_pass_kernel(sizeof(T) == 8, op.dir, op.pp);
+    if (prepare_pass<T>(op.pp, op.dir, op.kfn) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
   }
   return FFTJ_OK;
 }

@@ -57,6 +57,7 @@ _lib = None
 EXPORTS = [
     "fftj_plan_c2c", "fftj_plan_r2c", "fftj_plan_c2r", "fftj_execute", "fftj_plan_get_info",
     "fftj_plan_workspace_bytes", "fftj_plan_destroy", "fftj_last_error_string", "fftj_version",
+    "fftj_execute_noalloc_c2c",
 ]
 
 
@@ -82,6 +83,7 @@ def lib():
         L.fftj_plan_get_info.argtypes = [vp, ctypes.POINTER(PlanInfo)]
         L.fftj_plan_workspace_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
         L.fftj_plan_destroy.argtypes = [vp]
+        L.fftj_execute_noalloc_c2c.argtypes = [i32, i64, i64, i32, ctypes.c_double, vp, vp, vp]
         L.fftj_last_error_string.restype = ctypes.c_char_p
         L.fftj_version.restype = ctypes.c_char_p
         for name in EXPORTS:

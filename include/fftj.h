@@ -120,6 +120,28 @@ const char* fftj_last_error_string(void);
 /* Library version string. */
 const char* fftj_version(void);
 
+/*
+ * Allocation-free complex transform. No counterpart in the reference: it is
+ * for callers that cannot allocate device memory when they transform, such
+ * as code recording a CUDA stream capture (cudaMalloc cannot be captured),
+ * real-time loops that forbid allocation after start-up, and hosts that own
+ * all device memory through their own pool. It creates no plan and calls no
+ * cudaMalloc, cudaFree or other allocating routine: its scratch is a
+ * file-scope static device array of 64 MiB (1 MiB of twiddle tables,
+ * regenerated on the device on every call, and 63 MiB for the intermediate
+ * of a two-pass transform) that every GPU loading the library holds until
+ * exit. Limits: n 13-smooth and done in one or two passes (n <= 2^20), and
+ * for two passes batch * n * sizeof(complex) <= 63 MiB; larger requests
+ * return FFTJ_ERR_ARG / FFTJ_ERR_UNSUPPORTED with a message. d_in/d_out hold
+ * batch dense transforms; in == out is allowed. The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) and should
+ * come before any stream capture. All calls share the one array: calls that
+ * overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller. Nothing in the array needs to start at zero.
+ */
+int fftj_execute_noalloc_c2c(int dtype, int64_t n, int64_t batch, int dir, double scale, const void* d_in,
+                             void* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
