@@ -71,6 +71,7 @@ struct PassParams {
   const void* twR;         // w_R^t, t < R (inner twiddles, sign of the pass)
   double scale;            // applied on store when != 1
   int smem_elems;          // padded elements per buffer
+  int smem_tw_elems;       // extra shared elements (recipe kernels stage w_R^t there)
   int threads;
   int Tf;                  // threads per tile column (threads = NB * Tf)
   int ept;                 // elements per thread per column (ceil(R / Tf))

@@ -138,7 +138,7 @@ cudaError_t prepare_pass(const PassParams& pp, int dir, const void* fn) {
   if (e != cudaSuccess) return e;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const size_t need = (size_t)pp.smem_elems * sizeof(Cx<T>);
+  const size_t need = (size_t)(pp.smem_elems + pp.smem_tw_elems) * sizeof(Cx<T>);
   if (need > (size_t)optin) return cudaErrorInvalidValue;
   const void* f = fn ? fn : (const void*)pass_fn<T>(dir, pp.load_op);
   return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -147,7 +147,7 @@ cudaError_t prepare_pass(const PassParams& pp, int dir, const void* fn) {
 template <typename T>
 cudaError_t launch_pass(const PassParams& pp, int dir, const void* fn, const void* in, void* out,
                         cudaStream_t st) {
-  const size_t smem = (size_t)pp.smem_elems * sizeof(Cx<T>);
+  const size_t smem = (size_t)(pp.smem_elems + pp.smem_tw_elems) * sizeof(Cx<T>);
   const uint32_t grid = pp.tiles_q * pp.tiles_p * pp.tiles_b;
   const void* f = fn ? fn : (const void*)pass_fn<T>(dir, pp.load_op);
   void* args[3] = {const_cast<PassParams*>(&pp), const_cast<void**>(&in), &out};

@@ -341,7 +341,7 @@ __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b
 #pragma unroll
         for (int j = 1; j < r; ++j) {
           Cx<T> w = v[i][j];
-          if (p != 0) w = cmul(w, __ldg(&twR[j * tstep]));
+          if (p != 0) w = cmul(w, twR[j * tstep]);
           buf[pidx<T>(a + j * jstride_out)] = w;
         }
       }
@@ -608,7 +608,15 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
   const int64_t batch = b0 + cbt;
   const int64_t pcol = p0 + pl;
   const bool colok = batch < pp.nbatch;
-  const Cx<T>* twR = reinterpret_cast<const Cx<T>*>(pp.twR);
+  // the pass's inner twiddles w_R^t are staged in shared memory right after
+  // the tile (smem_elems), so sub-stages read them with 32-bit shared
+  // addresses: no per-element global index arithmetic
+  Cx<T>* twS = buf + pp.smem_elems;
+  {
+    const Cx<T>* twG = reinterpret_cast<const Cx<T>*>(pp.twR) + tid;
+    for (int t = tid; t < R; t += nthr, twG += nthr) twS[t] = __ldg(twG);
+  }
+  const Cx<T>* twR = twS;
 
   if constexpr (MODE == 0) {
     // ---- row load (lanes walk j): e = tid + i*nthr -> (c, j), c = column
@@ -662,6 +670,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
         }
       }
     }
+    __syncthreads();  // staged twiddles visible (the loads above stay in flight)
 #pragma unroll
     for (int i = 0; i < IPT; ++i) {
       const int k = kg + i * TF;
@@ -672,7 +681,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
 #pragma unroll
         for (int j = 1; j < r0; ++j) {
           Cx<T> w = v[i][j];
-          if (NS > 1 && k != 0) w = cmul(w, __ldg(&twR[j * k]));
+          if (NS > 1 && k != 0) w = cmul(w, twR[j * k]);
           buf[pidx<T>(a + j * NB)] = w;
         }
       }
@@ -703,7 +712,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
       if (j >= R) { j -= R; c++; }
     }
     c = tid / R; j = tid - (tid / R) * R;
-    Cx<T>* ob = out + b0 * pp.out_bstride + (int64_t)R * p0;
+    Cx<T>* op = out + b0 * pp.out_bstride + (int64_t)R * p0 + tid;
 #pragma unroll
     for (int i = 0; i < EPT; ++i) {
       const int e = tid + i * nthr;
@@ -712,8 +721,9 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
         Cx<T> v = buf[pidx<T>(j * NB + c)];
         if (tw) v = cmul(v, w[i]);
         if (scaled) { v.x *= sc; v.y *= sc; }
-        ob[e] = v;
+        *op = v;
       }
+      op += nthr;
       j += dj; c += dc;
       if (j >= R) { j -= R; c++; }
     }

@@ -840,6 +840,7 @@ int finalize_passes(fftj_plan_s* P) {
   for (auto& op : P->ops) {
     if (op.kind != OP_PASS) continue;
     op.kfn = pick_pass_kernel(sizeof(T) == 8, op.dir, op.pp);
+    op.pp.smem_tw_elems = op.kfn ? op.pp.R : 0;
     if (prepare_pass<T>(op.pp, op.dir, op.kfn) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
   }
   return FFTJ_OK;
