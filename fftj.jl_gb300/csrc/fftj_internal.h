@@ -81,6 +81,7 @@ struct PassParams {
   int load_op;
   int64_t ld_n, ld_m, ld_hp;     // DECONV: n, m, ceil(n/2); C2R_PRE: h = ld_n
   int64_t ld_stride;             // input batch stride of the raw input
+  int64_t ld_inner;              // DECONV along a strided axis: inner stride (1 = contiguous)
   const void* ld_tab;            // DECONV: corr[n]; C2R_PRE: w[h]
   double ld_pre;                 // C2R_PRE pair factor (1/2 or 1)
 };
@@ -89,6 +90,7 @@ struct PassParams {
 struct InterpParams {
   int64_t n, m, w, nbatch;
   int64_t g_bstride, y_bstride;
+  int64_t inner;  // inner stride of the transformed axis (1 = contiguous)
   const void* wt;
   const int32_t* l0;
 };

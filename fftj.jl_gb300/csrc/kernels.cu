@@ -22,26 +22,33 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256, 2)
   pass_body<T, DIR, LOADOP, RuntimeRecipe>(pp, in, out);
 }
 
-// Resampling interpolation (FFTJ _interp!, src/resample.jl:392-424).
+// Resampling interpolation (FFTJ _interp!, src/resample.jl:392-424; along a
+// strided N-d axis, _rows_interp!, src/resample.jl:557-588): output (b, k, i)
+// = sum_t wt[k*w + t] * grid(b, (l0[k] + t) mod m, i), i the inner index
+// (fastest, so neighbouring threads read neighbouring grid elements).
 template <typename T>
-__global__ void k_interp(const __grid_constant__ InterpParams ip, const Cx<T>* __restrict__ g, Cx<T>* __restrict__ y) {
+__global__ void k_interp(const __grid_constant__ InterpParams ip, const Cx<T>* __restrict__ g,
+                         Cx<T>* __restrict__ y) {
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= ip.n * ip.nbatch) return;
-  const int64_t b = idx / ip.n, k = idx - b * ip.n;
+  const int64_t inner = ip.inner > 1 ? ip.inner : 1;
+  if (idx >= ip.n * ip.nbatch * inner) return;
+  int64_t rest = idx, i = 0;
+  if (inner > 1) { rest = idx / inner; i = idx - rest * inner; }
+  const int64_t b = rest / ip.n, k = rest - b * ip.n;
   const T* wt = reinterpret_cast<const T*>(ip.wt) + k * ip.w;
-  const Cx<T>* gb = g + b * ip.g_bstride;
+  const Cx<T>* gb = g + b * ip.g_bstride + i;
   int64_t l = __ldg(ip.l0 + k);
   if (l < 0) l += ip.m;
   T re = 0, im = 0;
-  for (int i = 0; i < ip.w; ++i) {
-    const T wv = __ldg(wt + i);
-    const Cx<T> gv = __ldg(gb + l);
+  for (int t = 0; t < ip.w; ++t) {
+    const T wv = __ldg(wt + t);
+    const Cx<T> gv = __ldg(gb + l * inner);
     re = fma(wv, gv.x, re);
     im = fma(wv, gv.y, im);
     ++l;
     if (l >= ip.m) l -= ip.m;
   }
-  y[b * ip.y_bstride + k] = mk<T>(re, im);
+  y[b * ip.y_bstride + k * inner + i] = mk<T>(re, im);
 }
 
 // rfft even post-pass (FFTJ src/real.jl:85-135): X[k] = xe + w (-i xo).
@@ -156,7 +163,7 @@ cudaError_t launch_pass(const PassParams& pp, int dir, const void* fn, const voi
 
 template <typename T>
 cudaError_t launch_interp(const InterpParams& ip, const void* g, void* y, cudaStream_t st) {
-  const int64_t total = ip.n * ip.nbatch;
+  const int64_t total = ip.n * ip.nbatch * (ip.inner > 1 ? ip.inner : 1);
   const int th = 256;
   k_interp<T><<<(unsigned)((total + th - 1) / th), th, 0, st>>>(ip, reinterpret_cast<const Cx<T>*>(g),
                                                                 reinterpret_cast<Cx<T>*>(y));

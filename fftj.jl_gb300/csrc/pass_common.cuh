@@ -235,13 +235,16 @@ __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in,
     return __ldg(reinterpret_cast<const Cx<T>*>(in) + b * pp.in_bstride + g);
   } else if (LOADOP == LOAD_DECONV) {
     // grid position g of the length-m zero-padded deconvolved input
-    // (FFTJ _deconv! + zero fill, src/resample.jl:258-301)
-    const int64_t n = pp.ld_n, m = pp.ld_m, hp = pp.ld_hp;
+    // (FFTJ _deconv! + zero fill, src/resample.jl:258-301); along a strided
+    // N-d axis g = a * inner + i (RsPass lanes, src/resample.jl:511-536)
+    const int64_t n = pp.ld_n, m = pp.ld_m, hp = pp.ld_hp, inner = pp.ld_inner > 1 ? pp.ld_inner : 1;
+    int64_t a = g, i = 0;
+    if (inner > 1) { a = g / inner; i = g - a * inner; }
     int64_t j;
-    if (g < hp) j = g;
-    else if (g >= m - n + hp) j = g - (m - n);
+    if (a < hp) j = a;
+    else if (a >= m - n + hp) j = a - (m - n);
     else return mk<T>(0, 0);
-    const Cx<T> x = __ldg(reinterpret_cast<const Cx<T>*>(in) + b * pp.ld_stride + j);
+    const Cx<T> x = __ldg(reinterpret_cast<const Cx<T>*>(in) + b * pp.ld_stride + j * inner + i);
     const T c = __ldg(reinterpret_cast<const T*>(pp.ld_tab) + j);
     return mk<T>(x.x * c, x.y * c);
   } else if (LOADOP == LOAD_C2R_PRE) {
@@ -525,12 +528,14 @@ __device__ __forceinline__ Cx<T> load_elem_off(const PassParams& pp, const void*
   if (LOADOP == LOAD_PLAIN) {
     return __ldg(reinterpret_cast<const Cx<T>*>(in) + boff + g);
   } else if (LOADOP == LOAD_DECONV) {
-    const int64_t n = pp.ld_n, m = pp.ld_m, hp = pp.ld_hp;
+    const int64_t n = pp.ld_n, m = pp.ld_m, hp = pp.ld_hp, inner = pp.ld_inner > 1 ? pp.ld_inner : 1;
+    int64_t a = g, i = 0;
+    if (inner > 1) { a = g / inner; i = g - a * inner; }
     int64_t j;
-    if (g < hp) j = g;
-    else if (g >= m - n + hp) j = g - (m - n);
+    if (a < hp) j = a;
+    else if (a >= m - n + hp) j = a - (m - n);
     else return mk<T>(0, 0);
-    const Cx<T> x = __ldg(reinterpret_cast<const Cx<T>*>(in) + boff + j);
+    const Cx<T> x = __ldg(reinterpret_cast<const Cx<T>*>(in) + boff + j * inner + i);
     const T c = __ldg(reinterpret_cast<const T*>(pp.ld_tab) + j);
     return mk<T>(x.x * c, x.y * c);
   } else if (LOADOP == LOAD_C2R_PRE) {

@@ -72,6 +72,14 @@ bool smooth13(i64 n, std::vector<int>* primes) {
 // ---- resampling parameters (FFTJ src/resample.jl) -------------------------
 const int SMOOTH_ODD[7] = {1, 3, 5, 7, 9, 15, 21};
 int top_set_bit(i64 x) { return x <= 0 ? 0 : 64 - __builtin_clzll((unsigned long long)x); }
+i64 nextsmooth7(i64 N) {  // src/resample.jl:25-31
+  for (i64 m = N;; ++m) {
+    i64 r = m;
+    for (int q : {2, 3, 5, 7})
+      while (r % q == 0) r /= q;
+    if (r == 1) return m;
+  }
+}
 i64 nextsmooth(i64 N) {  // src/resample.jl:13-21
   i64 best = INT64_MAX;
   for (int o : SMOOTH_ODD) {
@@ -117,12 +125,12 @@ struct Resample {
   std::vector<int32_t> l0;   // first grid index per output (unwrapped)
 };
 // _resample_parts with table weights (src/resample.jl:202-256)
-Resample resample_parts(i64 n, bool f64, double scale) {
+Resample resample_parts(i64 n, bool f64, double scale, i64 m_override = 0) {
   Resample r;
   r.n = n;
   const double epsT = f64 ? 2.220446049250313e-16 : 1.1920928955078125e-07;
   const double tol = 10 * epsT;
-  r.m = nextsmooth((i64)std::ceil(2.0 * n));
+  r.m = m_override ? m_override : nextsmooth((i64)std::ceil(2.0 * n));
   const double ratio = std::max((double)n / r.m, 0.5);
   i64 wc = (i64)std::ceil(std::log(1 / tol) / (M_PI * std::sqrt(1 - ratio)));
   r.w = 4 * ((wc + 3) / 4);
@@ -570,6 +578,7 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
   f.ld_m = rs.m;
   f.ld_hp = (n + 1) / 2;
   f.ld_stride = idist;
+  f.ld_inner = 1;
   {
     std::vector<T> c(n);
     for (i64 j = 0; j < n; ++j) c[j] = (T)rs.corr[j];
@@ -584,6 +593,7 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
   ip.ip.nbatch = batch;
   ip.ip.g_bstride = rs.m;
   ip.ip.y_bstride = odist;
+  ip.ip.inner = 1;
   {
     std::vector<T> w(rs.wt.size());
     for (size_t i = 0; i < w.size(); ++i) w[i] = (T)rs.wt[i];
@@ -595,6 +605,53 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
   for (auto& o : tmp) ops->push_back(o);
   ops->push_back(ip);
   *route = FFTJ_ROUTE_RESAMPLE;
+  return FFTJ_OK;
+}
+
+// A non-smooth N-d axis (length nd, inner stride Bi, nb outer blocks) by
+// batched resampling (FFTJ RsPass, src/resample.jl:434-588, with
+// m = nextsmooth7(2 nd) and table weights; _rs_pass!, src/ndplan.jl:137-151):
+// the deconvolving first pass writes an m-row grid per block, the smooth
+// passes transform it along the axis, the interpolation writes nd rows back.
+// scale is folded into the deconvolution.
+template <typename T>
+int build_axis_resample(fftj_plan_s* P, i64 nd, i64 Bi, i64 nb, int dir, double scale, std::vector<Op>* ops) {
+  Resample rs = resample_parts(nd, sizeof(T) == 8, scale, nextsmooth7(2 * nd));
+  std::vector<Op> tmp;
+  int rc = build_axis_passes<T>(P, rs.m, Bi, nb, Bi * rs.m, Bi * rs.m, dir, 1.0, &tmp);
+  if (rc) return rc;
+  PassParams& f = tmp.front().pp;
+  f.load_op = LOAD_DECONV;
+  f.ld_n = nd;
+  f.ld_m = rs.m;
+  f.ld_hp = (nd + 1) / 2;
+  f.ld_stride = Bi * nd;
+  f.ld_inner = Bi;
+  {
+    std::vector<T> c(nd);
+    for (i64 j = 0; j < nd; ++j) c[j] = (T)rs.corr[j];
+    f.ld_tab = upload_raw(P, c.data(), c.size() * sizeof(T));
+    if (!f.ld_tab) return fail(FFTJ_ERR_CUDA, "table upload failed");
+  }
+  Op ip;
+  ip.kind = OP_INTERP;
+  ip.ip.n = nd;
+  ip.ip.m = rs.m;
+  ip.ip.w = rs.w;
+  ip.ip.nbatch = nb;
+  ip.ip.g_bstride = Bi * rs.m;
+  ip.ip.y_bstride = Bi * nd;
+  ip.ip.inner = Bi;
+  {
+    std::vector<T> w(rs.wt.size());
+    for (size_t i = 0; i < w.size(); ++i) w[i] = (T)rs.wt[i];
+    ip.ip.wt = upload_raw(P, w.data(), w.size() * sizeof(T));
+    ip.ip.l0 = (const int32_t*)upload_raw(P, rs.l0.data(), rs.l0.size() * sizeof(int32_t));
+    if (!ip.ip.wt || !ip.ip.l0) return fail(FFTJ_ERR_CUDA, "table upload failed");
+  }
+  ip.dst_bytes = (size_t)(nb * Bi * nd) * sizeof(T) * 2;
+  for (auto& o : tmp) ops->push_back(o);
+  ops->push_back(ip);
   return FFTJ_OK;
 }
 
@@ -618,13 +675,13 @@ int plan_c2c_t(fftj_plan_s* P, const std::vector<i64>& dims, i64 batch, i64 idis
     for (size_t ai = 0; ai < active.size(); ++ai) {
       const size_t d = active[ai];
       const i64 nd = dims[d];
-      if (!smooth13(nd, nullptr))
-        return fail(FFTJ_ERR_UNSUPPORTED, "N-d plans with a non-smooth dimension are not supported yet");
       i64 Bi = 1, Bo = 1;
       for (size_t e = 0; e < d; ++e) Bi *= dims[e];
       for (size_t e = d + 1; e < dims.size(); ++e) Bo *= dims[e];
       const bool last = ai + 1 == active.size();
-      int rc = build_axis_passes<T>(P, nd, Bi, Bo * batch, Bi * nd, Bi * nd, dir, last ? scale : 1.0, &P->ops);
+      int rc = smooth13(nd, nullptr)
+                   ? build_axis_passes<T>(P, nd, Bi, Bo * batch, Bi * nd, Bi * nd, dir, last ? scale : 1.0, &P->ops)
+                   : build_axis_resample<T>(P, nd, Bi, Bo * batch, dir, last ? scale : 1.0, &P->ops);
       if (rc) return rc;
     }
     if (P->ops.empty()) {
@@ -779,11 +836,12 @@ int plan_r2c_t(fftj_plan_s* P, const std::vector<i64>& dims, i64 batch, i64 idis
   cd[0] = h1p;
   for (size_t d = 1; d < dims.size(); ++d) {
     if (dims[d] == 1) continue;
-    if (!smooth13(dims[d], nullptr)) return fail(FFTJ_ERR_UNSUPPORTED, "non-smooth N-d real dimension");
     i64 Bi = 1, Bo = 1;
     for (size_t e = 0; e < d; ++e) Bi *= cd[e];
     for (size_t e = d + 1; e < cd.size(); ++e) Bo *= cd[e];
-    rc = build_axis_passes<T>(P, dims[d], Bi, Bo * batch, Bi * dims[d], Bi * dims[d], -1, 1.0, &P->ops);
+    rc = smooth13(dims[d], nullptr)
+             ? build_axis_passes<T>(P, dims[d], Bi, Bo * batch, Bi * dims[d], Bi * dims[d], -1, 1.0, &P->ops)
+             : build_axis_resample<T>(P, dims[d], Bi, Bo * batch, -1, 1.0, &P->ops);
     if (rc) return rc;
   }
   return FFTJ_OK;
@@ -811,11 +869,12 @@ int plan_c2r_t(fftj_plan_s* P, const std::vector<i64>& dims, i64 batch, i64 idis
   cd[0] = h1p;
   for (size_t d = 1; d < dims.size(); ++d) {
     if (dims[d] == 1) continue;
-    if (!smooth13(dims[d], nullptr)) return fail(FFTJ_ERR_UNSUPPORTED, "non-smooth N-d real dimension");
     i64 Bi = 1, Bo = 1;
     for (size_t e = 0; e < d; ++e) Bi *= cd[e];
     for (size_t e = d + 1; e < cd.size(); ++e) Bo *= cd[e];
-    int rc = build_axis_passes<T>(P, dims[d], Bi, Bo * batch, Bi * dims[d], Bi * dims[d], +1, 1.0, &P->ops);
+    int rc = smooth13(dims[d], nullptr)
+                 ? build_axis_passes<T>(P, dims[d], Bi, Bo * batch, Bi * dims[d], Bi * dims[d], +1, 1.0, &P->ops)
+                 : build_axis_resample<T>(P, dims[d], Bi, Bo * batch, +1, 1.0, &P->ops);
     if (rc) return rc;
   }
   const double extra = normalized ? 1.0 / (double)rest : 1.0;

@@ -109,8 +109,6 @@ def test_nd_reference_shapes(fftj, golden, orc, T):
         if not key.startswith("nd_x_"):
             continue
         dims = [int(v) for v in key[5:].split("x")]
-        if any(not _smooth13(d) for d in dims):
-            continue  # non-smooth N-d dims: covered by test_nd_nonsmooth_dim_rejected
         n = int(np.prod(dims))
         tol = 200 * EPS[T]
         x = golden[key]
@@ -127,17 +125,22 @@ def test_nd_reference_shapes(fftj, golden, orc, T):
         assert rel_l2(host(fftj.brfft(dev(rref, T), dims[0])), n * xr) <= tol, dims
 
 
-def _smooth13(n):
-    for p in (2, 3, 5, 7, 11, 13):
-        while n % p == 0:
-            n //= p
-    return n == 1
-
-
-def test_nd_nonsmooth_dim_rejected(fftj):
-    x = torch.zeros((17, 16), dtype=torch.complex64, device="cuda")
-    with pytest.raises(fftj.FFTJError):
-        fftj.fft(x)
+@pytest.mark.parametrize("T", T_LIST)
+@pytest.mark.parametrize("shape", [(17, 16), (16, 17), (19, 23), (3, 17, 8), (101, 64), (7, 97)])
+def test_nd_nonsmooth_dims(fftj, orc, T, shape):
+    """N-d shapes with non-smooth dimensions (batched resampling along the
+    axis, FFTJ RsPass), complex and real, against FP64 and the oracle."""
+    rng = np.random.default_rng(list(shape))
+    x = cn(rng, shape)
+    tol = 200 * EPS[T]
+    y = host(fftj.fft(dev(x, T)))
+    assert rel_l2(y, np.fft.fftn(x)) <= tol, shape
+    assert rel_l2(y, orc.PlanND(T, list(reversed(shape)), "fft")(x)) <= tol, shape
+    assert rel_l2(host(fftj.ifft(dev(y, T))), x) <= tol, shape
+    xr = rng.standard_normal(shape)
+    Y = fftj.rfft(dev(xr, T))
+    assert rel_l2(host(Y), np.fft.rfftn(xr)) <= tol, shape
+    assert rel_l2(host(fftj.irfft(Y, shape[-1])), xr) <= tol, shape
 
 
 # --------------------------------------------------------------------------
