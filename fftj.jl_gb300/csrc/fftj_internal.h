@@ -46,6 +46,7 @@ enum LoadOp : int {
   LOAD_DECONV = 1,    // resampling: deconvolve and zero-pad n -> m
   LOAD_C2R_PRE = 2,   // irfft even pre-pass Z[k] from X[k], conj X[h-k]
   LOAD_REAL = 3,      // real x -> (x, 0)
+  LOAD_SPREAD = 4,    // HvdH: Gaussian spread of the input onto the t-grid
 };
 
 // Parameters of one Stockham super-radix pass over the data: radix-R
@@ -84,6 +85,20 @@ struct PassParams {
   int64_t ld_inner;              // DECONV along a strided axis: inner stride (1 = contiguous)
   const void* ld_tab;            // DECONV: corr[n]; C2R_PRE: w[h]
   double ld_pre;                 // C2R_PRE pair factor (1/2 or 1)
+  int ld_w;                      // SPREAD: taps per grid row
+  const int32_t* ld_l0;          // SPREAD: first input row of each grid row
+};
+
+// HvdH banded solve: thread per (batch, chunk of L rows + 2H halo rows).
+struct SolveParams {
+  int64_t n, t, L, H, R, nchunk, nbatch;
+  int64_t g_bstride, y_bstride;
+  int B;
+  double sc;                 // scale * n / t
+  const void* lf;            // nchunk*R*B multipliers
+  const void* uf;            // nchunk*R*(B+1): 1/U_ii, U_{i,i+1..i+B}
+  const int32_t* oi;         // nchunk*R output index (-1: identity row)
+  void* zw;                  // R * nbatch * nchunk forward-substitution scratch
 };
 
 // Resampling interpolation: y[b*ody + k] = sum_i wt[k*w+i] g[b*m + (l0[k]+i) mod m]
@@ -152,6 +167,8 @@ template <typename T>
 cudaError_t launch_real_post(const RealPostParams& rp, const void* z, void* y, cudaStream_t st);
 template <typename T>
 cudaError_t launch_copy(const CopyParams& cp, const void* in, void* out, cudaStream_t st);
+template <typename T>
+cudaError_t launch_solve(const SolveParams& sp, const void* g, void* y, cudaStream_t st);
 // Opt a pass configuration into the dynamic shared memory it needs.
 template <typename T>
 cudaError_t prepare_pass(const PassParams& pp, int dir, const void* fn);

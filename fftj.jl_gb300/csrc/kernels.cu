@@ -51,6 +51,68 @@ __global__ void k_interp(const __grid_constant__ InterpParams ip, const Cx<T>* _
   y[b * ip.y_bstride + k * inner + i] = mk<T>(re, im);
 }
 
+// HvdH banded solve (FFTJ _hvdh_subst! / _hvdh_back!, src/hvdh.jl:604-686):
+// thread (b, c) runs forward substitution over its chunk's R rows (rows q0
+// .. q0+R-1 of the length-t transform, cyclic), keeping z in a strided
+// scratch, then back substitution, writing the core rows' unknowns to their
+// permuted outputs, scaled by scale * n / t.
+template <typename T, int B>
+__global__ void k_hvdh_solve(const __grid_constant__ SolveParams sp, const Cx<T>* __restrict__ g,
+                             Cx<T>* __restrict__ y) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nt = sp.nbatch * sp.nchunk;
+  if (tid >= nt) return;
+  const int64_t b = tid / sp.nchunk, ch = tid - b * sp.nchunk;
+  const int64_t R = sp.R, t = sp.t;
+  const T* lf = reinterpret_cast<const T*>(sp.lf) + ch * R * B;
+  const T* uf = reinterpret_cast<const T*>(sp.uf) + ch * R * (B + 1);
+  const int32_t* oi = sp.oi + ch * R;
+  Cx<T>* zw = reinterpret_cast<Cx<T>*>(sp.zw) + tid;
+  const Cx<T>* gb = g + b * sp.g_bstride;
+  int64_t q = ch * sp.L - sp.H;
+  q = ((q % t) + t) % t;
+  Cx<T> zp[B];
+#pragma unroll
+  for (int k = 0; k < B; ++k) zp[k] = mk<T>(0, 0);  // zp[k] = z_{i-1-k}
+  for (int64_t i = 0; i < R; ++i) {
+    Cx<T> z = mk<T>(0, 0);
+    if (__ldg(oi + i) >= 0) z = __ldg(gb + q);
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      const T f = __ldg(lf + i * B + k);
+      z.x = fma(-f, zp[k].x, z.x);
+      z.y = fma(-f, zp[k].y, z.y);
+    }
+#pragma unroll
+    for (int k = B - 1; k > 0; --k) zp[k] = zp[k - 1];
+    zp[0] = z;
+    zw[i * nt] = z;
+    if (++q == t) q = 0;
+  }
+  Cx<T> xp[B];
+#pragma unroll
+  for (int k = 0; k < B; ++k) xp[k] = mk<T>(0, 0);  // xp[k] = x_{i+1+k}
+  const T sc = (T)sp.sc;
+  Cx<T>* yb = y + b * sp.y_bstride;
+  for (int64_t i = R - 1; i >= sp.H; --i) {
+    Cx<T> x = zw[i * nt];
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const T u = __ldg(uf + i * (B + 1) + 1 + j);
+      x.x = fma(-u, xp[j].x, x.x);
+      x.y = fma(-u, xp[j].y, x.y);
+    }
+    const T iu = __ldg(uf + i * (B + 1));
+    x.x *= iu;
+    x.y *= iu;
+#pragma unroll
+    for (int k = B - 1; k > 0; --k) xp[k] = xp[k - 1];
+    xp[0] = x;
+    const int32_t o = __ldg(oi + i);
+    if (i < sp.H + sp.L && o >= 0) yb[o] = mk<T>(x.x * sc, x.y * sc);
+  }
+}
+
 // rfft even post-pass (FFTJ src/real.jl:85-135): X[k] = xe + w (-i xo).
 template <typename T>
 __global__ void k_real_post(const RealPostParams rp, const Cx<T>* __restrict__ z, Cx<T>* __restrict__ y) {
@@ -124,6 +186,7 @@ static PassFn<T> pass_fn(int dir, int load_op) {
       case LOAD_DECONV: return k_pass<T, -1, LOAD_DECONV>;
       case LOAD_C2R_PRE: return k_pass<T, -1, LOAD_C2R_PRE>;
       case LOAD_REAL: return k_pass<T, -1, LOAD_REAL>;
+      case LOAD_SPREAD: return k_pass<T, -1, LOAD_SPREAD>;
       default: return k_pass<T, -1, LOAD_PLAIN>;
     }
   }
@@ -131,6 +194,7 @@ static PassFn<T> pass_fn(int dir, int load_op) {
     case LOAD_DECONV: return k_pass<T, 1, LOAD_DECONV>;
     case LOAD_C2R_PRE: return k_pass<T, 1, LOAD_C2R_PRE>;
     case LOAD_REAL: return k_pass<T, 1, LOAD_REAL>;
+    case LOAD_SPREAD: return k_pass<T, 1, LOAD_SPREAD>;
     default: return k_pass<T, 1, LOAD_PLAIN>;
   }
 }
@@ -187,6 +251,24 @@ cudaError_t launch_copy(const CopyParams& cp, const void* in, void* out, cudaStr
   return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_solve(const SolveParams& sp, const void* g, void* y, cudaStream_t st) {
+  const int64_t total = sp.nbatch * sp.nchunk;
+  const int th = 128;
+  const unsigned grid = (unsigned)((total + th - 1) / th);
+  auto gg = reinterpret_cast<const Cx<T>*>(g);
+  auto yy = reinterpret_cast<Cx<T>*>(y);
+  switch (sp.B) {
+    case 1: k_hvdh_solve<T, 1><<<grid, th, 0, st>>>(sp, gg, yy); break;
+    case 2: k_hvdh_solve<T, 2><<<grid, th, 0, st>>>(sp, gg, yy); break;
+    case 3: k_hvdh_solve<T, 3><<<grid, th, 0, st>>>(sp, gg, yy); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_solve<float>(const SolveParams&, const void*, void*, cudaStream_t);
+template cudaError_t launch_solve<double>(const SolveParams&, const void*, void*, cudaStream_t);
 template cudaError_t prepare_pass<float>(const PassParams&, int, const void*);
 template cudaError_t prepare_pass<double>(const PassParams&, int, const void*);
 template cudaError_t launch_pass<float>(const PassParams&, int, const void*, const void*, void*, cudaStream_t);

@@ -247,6 +247,23 @@ __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in,
     const Cx<T> x = __ldg(reinterpret_cast<const Cx<T>*>(in) + b * pp.ld_stride + j * inner + i);
     const T c = __ldg(reinterpret_cast<const T*>(pp.ld_tab) + j);
     return mk<T>(x.x * c, x.y * c);
+  } else if (LOADOP == LOAD_SPREAD) {
+    // HvdH Gaussian spread (src/hvdh.jl:355-470, per output row as the
+    // batched HvPass): grid row g = sum_o wt[g*w + o] * x[(l0[g] + o) mod n]
+    const int64_t n = pp.ld_n;
+    const int w = pp.ld_w;
+    const Cx<T>* x = reinterpret_cast<const Cx<T>*>(in) + b * pp.ld_stride;
+    const T* wt = reinterpret_cast<const T*>(pp.ld_tab) + g * w;
+    int64_t r = __ldg(pp.ld_l0 + g);
+    T re = 0, im = 0;
+    for (int o = 0; o < w; ++o) {
+      const T c = __ldg(wt + o);
+      const Cx<T> v = __ldg(x + r);
+      re = fma(c, v.x, re);
+      im = fma(c, v.y, im);
+      if (++r == n) r = 0;
+    }
+    return mk<T>(re, im);
   } else if (LOADOP == LOAD_C2R_PRE) {
     // irfft pre-pass (FFTJ src/real.jl:149-192): Z[k] = xe + i (w xd)
     const int64_t h = pp.ld_n;
@@ -538,6 +555,21 @@ __device__ __forceinline__ Cx<T> load_elem_off(const PassParams& pp, const void*
     const Cx<T> x = __ldg(reinterpret_cast<const Cx<T>*>(in) + boff + j * inner + i);
     const T c = __ldg(reinterpret_cast<const T*>(pp.ld_tab) + j);
     return mk<T>(x.x * c, x.y * c);
+  } else if (LOADOP == LOAD_SPREAD) {
+    const int64_t n = pp.ld_n;
+    const int w = pp.ld_w;
+    const Cx<T>* x = reinterpret_cast<const Cx<T>*>(in) + boff;
+    const T* wt = reinterpret_cast<const T*>(pp.ld_tab) + g * w;
+    int64_t r = __ldg(pp.ld_l0 + g);
+    T re = 0, im = 0;
+    for (int o = 0; o < w; ++o) {
+      const T c = __ldg(wt + o);
+      const Cx<T> v = __ldg(x + r);
+      re = fma(c, v.x, re);
+      im = fma(c, v.y, im);
+      if (++r == n) r = 0;
+    }
+    return mk<T>(re, im);
   } else if (LOADOP == LOAD_C2R_PRE) {
     const int64_t h = pp.ld_n;
     const Cx<T>* X = reinterpret_cast<const Cx<T>*>(in) + boff;

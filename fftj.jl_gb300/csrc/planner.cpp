@@ -187,6 +187,216 @@ bool split_bins(const int* primes, int np, int k, i64 rmax, i64* bins) {
 
 namespace fftj {
 
+// ---- Gaussian resampling (Harvey-van der Hoeven), FFTJ src/hvdh.jl -------
+// For odd non-smooth n: spread the input with a narrow Gaussian onto a
+// smooth t = n + delta coprime to n (permuted so that the length-t transform
+// lands row q of the banded system on output q), transform at length t, then
+// solve the banded system (band B) for the n unknowns and write them to their
+// permuted outputs (src/hvdh.jl:1-19). The GPU solves chunks of L rows with H
+// halo rows per side independently, one thread per (batch, chunk), with LU
+// factors of every chunk precomputed here in FP64.
+i64 gcd_(i64 a, i64 b) {
+  while (b) { i64 t = a % b; a = b; b = t; }
+  return a < 0 ? -a : a;
+}
+i64 invmod_(i64 a, i64 m) {  // a^{-1} mod m (gcd(a, m) = 1)
+  i64 t = 0, nt = 1, r = m, nr = ((a % m) + m) % m;
+  while (nr) {
+    const i64 q = r / nr;
+    i64 x = t - q * nt; t = nt; nt = x;
+    x = r - q * nr; r = nr; nr = x;
+  }
+  return t < 0 ? t + m : t;
+}
+i64 fld_(i64 a, i64 b) { i64 q = a / b; if ((a % b != 0) && ((a < 0) != (b < 0))) q--; return q; }
+
+// t coprime to odd n, the smallest o*2^k >= n(1 + 1/128) (src/hvdh.jl:79-92)
+i64 hvdh_t(i64 n) {
+  const i64 N = (i64)std::ceil(n * (1.0 + 1.0 / 128));
+  i64 t = INT64_MAX;
+  if (n % 2 == 1) {
+    for (int o : {1, 3, 5, 7, 9, 15, 21}) {
+      if (gcd_(o, n) != 1) continue;
+      int k = 0;
+      while (((i64)o << k) < N) k++;
+      t = std::min<i64>(t, (i64)o << k);
+    }
+  }
+  return (t != INT64_MAX && t - n < n) ? t : 0;
+}
+bool use_hvdh(bool f64, i64 n) { return n % 2 == 1 && n >= (f64 ? 1000 : 16384); }  // src/hvdh.jl:97
+
+// halo rows: the inverse of the band system decays; probe windows of the
+// unknown-indexed system and find where a unit right-hand side's solution
+// falls below tol (src/hvdh.jl:118-146). Dense Gaussian elimination with
+// partial pivoting on (2P+1)^2 systems.
+i64 hvdh_halo(i64 n, i64 t, double a, int B, double tol) {
+  const double rho = (double)t / n;
+  const i64 c = invmod_(t - n, n);
+  std::vector<i64> probes;
+  const i64 np = std::min<i64>(n, 16);
+  for (i64 i = 0; i < np; ++i)
+    probes.push_back(np == 1 ? 0 : (i64)std::llround((double)i * (n - 1) / (np - 1)));
+  for (i64 h : {n / 2, n / 2 + 1}) probes.push_back((h * c) % n);
+  for (i64 P = 64; P <= 512; P *= 2) {
+    i64 H = 0;
+    const i64 m = 2 * P + 1;
+    std::vector<double> M(m * m), rhs(m);
+    for (i64 l0 : probes) {
+      std::fill(M.begin(), M.end(), 0.0);
+      // transpose(M) r = e: build the transpose directly, A[j][i] = M[i][j]
+      for (i64 i = 0; i < m; ++i)
+        for (i64 j = std::max<i64>(0, i - B - 1); j <= std::min<i64>(m - 1, i + B + 1); ++j) {
+          const i64 li = l0 - P + i, lj = l0 - P + j;
+          const double d = (double)(t * lj - n * fld_(2 * t * li + n, 2 * n)) / (double)n;
+          M[j * m + i] = std::exp(-a * d * d);
+        }
+      std::fill(rhs.begin(), rhs.end(), 0.0);
+      rhs[P] = 1;
+      for (i64 k = 0; k < m; ++k) {  // elimination with partial pivoting
+        i64 piv = k;
+        for (i64 r = k + 1; r < m; ++r)
+          if (std::fabs(M[r * m + k]) > std::fabs(M[piv * m + k])) piv = r;
+        if (piv != k) {
+          for (i64 cc = 0; cc < m; ++cc) std::swap(M[k * m + cc], M[piv * m + cc]);
+          std::swap(rhs[k], rhs[piv]);
+        }
+        const double d = M[k * m + k];
+        if (d == 0) continue;
+        for (i64 r = k + 1; r < m; ++r) {
+          const double f = M[r * m + k] / d;
+          if (f == 0) continue;
+          for (i64 cc = k; cc < m; ++cc) M[r * m + cc] -= f * M[k * m + cc];
+          rhs[r] -= f * rhs[k];
+        }
+      }
+      for (i64 k = m - 1; k >= 0; --k) {
+        double v = rhs[k];
+        for (i64 cc = k + 1; cc < m; ++cc) v -= M[k * m + cc] * rhs[cc];
+        rhs[k] = M[k * m + k] != 0 ? v / M[k * m + k] : 0;
+      }
+      double mx = 0;
+      for (i64 j = 0; j < m; ++j) mx = std::max(mx, std::fabs(rhs[j]));
+      for (i64 j = 0; j < m; ++j)
+        if (std::fabs(rhs[j]) > tol * mx) H = std::max<i64>(H, std::abs(j - P));
+    }
+    if (H < P - 2 * B) return (i64)std::ceil(rho * H) + B;
+  }
+  return -1;
+}
+
+struct Hvdh {
+  i64 n, t, delta, c, w, h, H, L, R, nchunk;
+  int B;
+  double alpha, a, b, sc;
+  std::vector<double> wt;    // t*w spread weights
+  std::vector<int32_t> l0;   // t: first input row of each spread output
+  std::vector<double> lf;    // nchunk*R*B forward multipliers (rows i-1 .. i-B)
+  std::vector<double> uf;    // nchunk*R*(B+1): 1/U_ii, U_{i,i+1..i+B}
+  std::vector<int32_t> oi;   // nchunk*R: output index of the row's unknown (-1: identity row)
+  bool ok = false;
+};
+
+Hvdh hvdh_parts(i64 n, bool f64, double scale) {
+  Hvdh P;
+  P.n = n;
+  P.t = hvdh_t(n);
+  if (!P.t) return P;
+  const i64 t = P.t;
+  P.delta = t - n;
+  P.c = invmod_(P.delta, n);
+  P.alpha = f64 ? 1.45 : 1.0;  // src/hvdh.jl:64
+  P.a = M_PI * P.alpha * P.alpha;
+  P.b = M_PI / (P.alpha * P.alpha);
+  const double tol = (f64 ? 2.220446049250313e-16 : 1.1920928955078125e-07) / 4;
+  P.h = (i64)std::ceil(P.alpha * std::sqrt(std::log(1 / tol) / M_PI));
+  P.w = 2 * P.h;
+  P.B = (int)std::floor(std::sqrt(std::log(1 / tol) / P.a) + 0.5);
+  if (P.B < 1 || P.B > 3) return P;
+  P.H = hvdh_halo(n, t, P.a, P.B, tol);
+  if (P.H < 0) return P;
+  // chunks: L rows (a divisor of t near 128), R = L + 2H rows each
+  i64 L = 1;
+  for (i64 d = 1; d <= 256; ++d)
+    if (t % d == 0 && std::abs((double)d - 128) <= std::abs((double)L - 128)) L = d;
+  P.L = L;
+  P.R = L + 2 * P.H;
+  P.nchunk = t / L;
+  P.sc = scale * (double)n / (double)t;
+  // spread table (src/hvdh.jl:726-752 restated per output row)
+  const i64 w = P.w, hw = P.h;
+  P.wt.resize(t * w);
+  P.l0.resize(t);
+  for (i64 q = 0; q < t; ++q) {
+    const double delta = (double)(t - q) / t;
+    for (i64 op = 0; op < w; ++op) {
+      const double o = (double)(op + 1 - hw);
+      P.wt[q * w + op] = std::exp(-P.b * (delta - o) * (delta - o)) / P.alpha;
+    }
+    P.l0[q] = (int32_t)((((q * P.c - hw) % n) + n) % n);
+  }
+  // rows: hit[q] (an unknown sits nearest row q) and that unknown's index
+  std::vector<i64> ell(t, -1);
+  for (i64 l = 0; l < n; ++l) {
+    const i64 q = fld_(2 * t * l + n, 2 * n);  // nearest row of position rho*l
+    ell[((q % t) + t) % t] = l;
+  }
+  // cyclic distance rho*l - q = (t*l - n*q)/n with an exact integer
+  // numerator (rounding rho*l would cost ~1e-13 in the Gaussian entries)
+  const i64 nt_ = n * t;
+  auto dist = [&](i64 l, i64 q) {
+    i64 M = t * l - n * q;
+    M = ((M + nt_ / 2) % nt_ + nt_) % nt_ - nt_ / 2;
+    return (double)M / (double)n;
+  };
+  const int B = P.B;
+  const i64 R = P.R;
+  P.lf.assign(P.nchunk * R * B, 0.0);
+  P.uf.assign(P.nchunk * R * (B + 1), 0.0);
+  P.oi.assign(P.nchunk * R, -1);
+  std::vector<double> A(R * (2 * B + 1));  // band rows: A[i][k], k = col - i + B
+  for (i64 ch = 0; ch < P.nchunk; ++ch) {
+    const i64 q0 = ch * L - P.H;
+    auto qrow = [&](i64 i) { return (((q0 + i) % t) + t) % t; };
+    std::fill(A.begin(), A.end(), 0.0);
+    for (i64 i = 0; i < R; ++i) {
+      const i64 q = qrow(i);
+      if (ell[q] < 0) { A[i * (2 * B + 1) + B] = 1.0; continue; }
+      P.oi[ch * R + i] = (int32_t)((P.delta * ell[q]) % n);
+      for (int k = -B; k <= B; ++k) {
+        const i64 j = i + k;
+        if (j < 0 || j >= R) continue;
+        const i64 lj = ell[qrow(j)];
+        if (lj < 0) continue;
+        const double d = dist(lj, q);
+        A[i * (2 * B + 1) + k + B] = std::exp(-P.a * d * d);
+      }
+    }
+    // banded LU without pivoting (src/hvdh.jl:524-566 does it row by row)
+    for (i64 i = 0; i < R; ++i) {
+      for (int k = B; k >= 1; --k) {
+        const i64 j = i - k;  // eliminate column j < i
+        if (j < 0) continue;
+        const double piv = A[j * (2 * B + 1) + B];
+        const double f = A[i * (2 * B + 1) + (j - i) + B] / piv;
+        P.lf[(ch * R + i) * B + (k - 1)] = f;
+        if (f == 0) continue;
+        for (int cc = 0; cc <= B; ++cc) {  // row j's U part: columns j .. j+B
+          const i64 col = j + cc;
+          const int ki = (int)(col - i) + B;
+          if (ki < 0 || ki > 2 * B) continue;
+          A[i * (2 * B + 1) + ki] -= f * A[j * (2 * B + 1) + B + cc];
+        }
+      }
+      const double d = A[i * (2 * B + 1) + B];
+      P.uf[(ch * R + i) * (B + 1)] = 1.0 / d;
+      for (int j = 1; j <= B; ++j) P.uf[(ch * R + i) * (B + 1) + j] = A[i * (2 * B + 1) + B + j];
+    }
+  }
+  P.ok = true;
+  return P;
+}
+
 // ---- pass decomposition ----
 int env_int(const char* name, int dflt) {
   const char* v = std::getenv(name);
@@ -393,7 +603,7 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
-enum OpKind { OP_PASS = 0, OP_INTERP = 1, OP_RPOST = 2, OP_COPY = 3 };
+enum OpKind { OP_PASS = 0, OP_INTERP = 1, OP_RPOST = 2, OP_COPY = 3, OP_SOLVE = 4 };
 enum BufId { B_IN = 0, B_OUT = 1, B_W0 = 2, B_W1 = 3 };
 
 struct Op {
@@ -405,6 +615,7 @@ struct Op {
   InterpParams ip;
   RealPostParams rp;
   CopyParams cp;
+  SolveParams sv;
   size_t dst_bytes = 0;  // bytes written (for workspace sizing)
 };
 
@@ -547,6 +758,69 @@ int alloc_workspace(fftj_plan_s* P) {
   return FFTJ_OK;
 }
 
+// HvdH route (src/hvdh.jl:222-241): spread fused into the first pass of the
+// length-t transform, the smooth passes, the chunked banded solve.
+template <typename T>
+int build_c2c_hvdh(fftj_plan_s* P, const Hvdh& hv, i64 batch, i64 idist, i64 odist, int dir,
+                   std::vector<Op>* ops, int* route) {
+  std::vector<Op> tmp;
+  int rc = build_axis_passes<T>(P, hv.t, 1, batch, hv.t, hv.t, dir, 1.0, &tmp);
+  if (rc) return rc;
+  PassParams& f = tmp.front().pp;
+  f.load_op = LOAD_SPREAD;
+  f.ld_n = hv.n;
+  f.ld_m = hv.t;
+  f.ld_stride = idist;
+  f.ld_inner = 1;
+  f.ld_w = (int)hv.w;
+  {
+    std::vector<T> w(hv.wt.size());
+    for (size_t i = 0; i < w.size(); ++i) w[i] = (T)hv.wt[i];
+    f.ld_tab = upload_raw(P, w.data(), w.size() * sizeof(T));
+    f.ld_l0 = (const int32_t*)upload_raw(P, hv.l0.data(), hv.l0.size() * sizeof(int32_t));
+    if (!f.ld_tab || !f.ld_l0) return fail(FFTJ_ERR_CUDA, "table upload failed");
+  }
+  Op sv;
+  sv.kind = OP_SOLVE;
+  SolveParams& q = sv.sv;
+  std::memset(&q, 0, sizeof(q));
+  q.n = hv.n;
+  q.t = hv.t;
+  q.L = hv.L;
+  q.H = hv.H;
+  q.R = hv.R;
+  q.nchunk = hv.nchunk;
+  q.nbatch = batch;
+  q.g_bstride = hv.t;
+  q.y_bstride = odist;
+  q.B = hv.B;
+  q.sc = hv.sc;
+  {
+    std::vector<T> lf(hv.lf.size()), uf(hv.uf.size());
+    for (size_t i = 0; i < lf.size(); ++i) lf[i] = (T)hv.lf[i];
+    for (size_t i = 0; i < uf.size(); ++i) uf[i] = (T)hv.uf[i];
+    q.lf = upload_raw(P, lf.data(), lf.size() * sizeof(T));
+    q.uf = upload_raw(P, uf.data(), uf.size() * sizeof(T));
+    q.oi = (const int32_t*)upload_raw(P, hv.oi.data(), hv.oi.size() * sizeof(int32_t));
+    if (!q.lf || !q.uf || !q.oi) return fail(FFTJ_ERR_CUDA, "table upload failed");
+  }
+  {
+    // forward-substitution scratch owned by the plan
+    DevBuf zb;
+    zb.bytes = (size_t)hv.R * batch * hv.nchunk * sizeof(T) * 2;
+    if (cudaMalloc(&zb.p, zb.bytes) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "workspace allocation failed");
+    P->tables.push_back(zb);
+    q.zw = zb.p;
+  }
+  sv.dst_bytes = (size_t)(batch * odist) * sizeof(T) * 2;
+  for (auto& o : tmp) ops->push_back(o);
+  ops->push_back(sv);
+  P->resample_m = hv.t;
+  P->resample_w = hv.w;
+  *route = FFTJ_ROUTE_HVDH;
+  return FFTJ_OK;
+}
+
 // complex 1-D transform of length n (batch at idist/odist) appended to ops;
 // if load_op != PLAIN, the first pass uses it with the given parameters.
 template <typename T>
@@ -564,6 +838,11 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
     *route = tmp.size() > 1 ? FFTJ_ROUTE_FOURSTEP : FFTJ_ROUTE_DIRECT;
     for (auto& o : tmp) ops->push_back(o);
     return FFTJ_OK;
+  }
+  // odd non-smooth lengths FFTJ sends to Gaussian resampling (HvdH)
+  if (use_hvdh(sizeof(T) == 8, n)) {
+    Hvdh hv = hvdh_parts(n, sizeof(T) == 8, scale);
+    if (hv.ok) return build_c2c_hvdh<T>(P, hv, batch, idist, odist, dir, ops, route);
   }
   // non-smooth: resample onto m (src/resample.jl:258-276)
   Resample rs = resample_parts(n, sizeof(T) == 8, scale);
@@ -1026,6 +1305,7 @@ int fftj_execute(fftj_plan plan, const void* d_in, void* d_out, void* stream) {
         case OP_INTERP: e = launch_interp<float>(op.ip, src, dst, st); break;
         case OP_RPOST: e = launch_real_post<float>(op.rp, src, dst, st); break;
         case OP_COPY: e = launch_copy<float>(op.cp, src, dst, st); break;
+        case OP_SOLVE: e = launch_solve<float>(op.sv, src, dst, st); break;
       }
     } else {
       switch (op.kind) {
@@ -1033,6 +1313,7 @@ int fftj_execute(fftj_plan plan, const void* d_in, void* d_out, void* stream) {
         case OP_INTERP: e = launch_interp<double>(op.ip, src, dst, st); break;
         case OP_RPOST: e = launch_real_post<double>(op.rp, src, dst, st); break;
         case OP_COPY: e = launch_copy<double>(op.cp, src, dst, st); break;
+        case OP_SOLVE: e = launch_solve<double>(op.sv, src, dst, st); break;
       }
     }
     if (e != cudaSuccess) return fail(FFTJ_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));

@@ -379,3 +379,35 @@ def test_library_loaded_from_tree(fftj):
     import os
     assert os.path.dirname(fftj._build.LIB).endswith("fftj.jl_gb300")
     assert fftj.lib()._name == fftj._build.LIB
+
+
+# --------------------------------------------------------------------------
+# Gaussian resampling (HvdH, src/hvdh.jl): FFTJ's route for odd non-smooth
+# n >= 1000 (F64) / >= 16384 (F32) (test/runtests.jl:110-144, 411-414)
+
+
+@pytest.mark.parametrize("T,n", [(np.float64, 3107), (np.float64, 10007), (np.float64, 20011),
+                                 (np.float64, 65537), (np.float32, 20011), (np.float32, 65537)])
+def test_hvdh_route_and_parity(fftj, orc, T, n):
+    rng = np.random.default_rng([0x4D4, n])
+    B = 3
+    x = cn(rng, (B, n))
+    p = fftj.plan_fft(T, n, batch=B)
+    assert p.route == "HvdhPlan"
+    y = p(dev(x, T))
+    tol = parity_tol(T, n)
+    ref = np.fft.fft(x, axis=-1)
+    assert rel_l2(host(y), ref) <= tol, (n, rel_l2(host(y), ref) / EPS[T])
+    assert rel_l2(host(y)[:1], orc.Plan1D(T, n, "fft")(x[:1])) <= tol
+    xi = host(fftj.plan_ifft(T, n, batch=B)(y))
+    assert rel_l2(xi, x) <= 2 * tol
+    xb = host(fftj.plan_bfft(T, n, batch=B)(dev(ref, T)))
+    assert rel_l2(xb, n * x) <= 2 * tol
+
+
+def test_resample_routes(fftj):
+    """Non-smooth lengths below the HvdH thresholds, and even ones, resample
+    (test/runtests.jl:412-416)."""
+    assert fftj.plan_fft(np.float64, 10006).route == "ResamplePlan"
+    assert fftj.plan_fft(np.float32, 10007).route == "ResamplePlan"
+    assert fftj.plan_fft(np.float64, 997).route == "ResamplePlan"
