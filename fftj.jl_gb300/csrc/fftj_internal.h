@@ -149,6 +149,20 @@ struct DtypeCfg {
   int rmax_multi;   // largest per-pass radix when more than one pass
   int min_run;      // minimum contiguous elements per tile row (coalescing)
 };
+// Schedule options of the plan being built on this host thread (set by the
+// fftj_plan_*_ex entry points for the duration of one planning call; all
+// zero otherwise, which is the default schedule).
+struct SchedOpts {
+  int tile = 0;
+  int extra_passes = 0;
+  int order = 0;
+  int tf_mult = 0;
+  int route = 0;
+  int threads_max = 0;
+  bool dry = false;
+};
+extern thread_local SchedOpts g_sched;
+
 DtypeCfg dtype_cfg(bool f64);
 int pass_radices(int64_t n, bool f64, bool strided, int64_t* Rs, int cap);
 int sub_radices(int64_t R, int* out, int cap);

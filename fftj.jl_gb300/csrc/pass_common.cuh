@@ -40,6 +40,15 @@ __device__ __forceinline__ C mul_di(C z) {
   return c;
 }
 
+// Load of transform data. Kernels read their inputs through the read-only
+// path (__ldg); the persistent group kernel reads data that other CTAs of
+// the same launch wrote, so it uses L2-coherent loads (__ldcg) instead.
+template <bool CG, typename V>
+__device__ __forceinline__ V ldd(const V* p) {
+  if constexpr (CG) return __ldcg(p);
+  else return __ldg(p);
+}
+
 // Shared-memory padding: one element per 16 (8-byte) or 8 (16-byte) elements,
 // so power-of-two strides spread over the banks.
 template <typename T>
@@ -229,10 +238,29 @@ __device__ __noinline__ void substage(Cx<T>* __restrict__ buf, const int b, cons
   __syncthreads();
 }
 
-template <typename T, int LOADOP>
+// LOADOP = LOAD_RUNTIME reads the load op from pp (one code path for all;
+// the group kernel uses it to keep its instantiation count small).
+constexpr int LOAD_RUNTIME = -1;
+
+template <typename T, int LOADOP, bool CG = false>
+__device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in, int64_t b, int64_t g);
+
+template <typename T, bool CG>
+__device__ __forceinline__ Cx<T> load_elem_rt(const PassParams& pp, const void* in, int64_t b, int64_t g) {
+  switch (pp.load_op) {
+    case LOAD_DECONV: return load_elem<T, LOAD_DECONV, CG>(pp, in, b, g);
+    case LOAD_SPREAD: return load_elem<T, LOAD_SPREAD, CG>(pp, in, b, g);
+    case LOAD_C2R_PRE: return load_elem<T, LOAD_C2R_PRE, CG>(pp, in, b, g);
+    case LOAD_REAL: return load_elem<T, LOAD_REAL, CG>(pp, in, b, g);
+    default: return load_elem<T, LOAD_PLAIN, CG>(pp, in, b, g);
+  }
+}
+
+template <typename T, int LOADOP, bool CG>
 __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in, int64_t b, int64_t g) {
+  if constexpr (LOADOP == LOAD_RUNTIME) return load_elem_rt<T, CG>(pp, in, b, g);
   if (LOADOP == LOAD_PLAIN) {
-    return __ldg(reinterpret_cast<const Cx<T>*>(in) + b * pp.in_bstride + g);
+    return ldd<CG>(reinterpret_cast<const Cx<T>*>(in) + b * pp.in_bstride + g);
   } else if (LOADOP == LOAD_DECONV) {
     // grid position g of the length-m zero-padded deconvolved input
     // (FFTJ _deconv! + zero fill, src/resample.jl:258-301); along a strided
@@ -244,7 +272,7 @@ __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in,
     if (a < hp) j = a;
     else if (a >= m - n + hp) j = a - (m - n);
     else return mk<T>(0, 0);
-    const Cx<T> x = __ldg(reinterpret_cast<const Cx<T>*>(in) + b * pp.ld_stride + j * inner + i);
+    const Cx<T> x = ldd<CG>(reinterpret_cast<const Cx<T>*>(in) + b * pp.ld_stride + j * inner + i);
     const T c = __ldg(reinterpret_cast<const T*>(pp.ld_tab) + j);
     return mk<T>(x.x * c, x.y * c);
   } else if (LOADOP == LOAD_SPREAD) {
@@ -258,7 +286,7 @@ __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in,
     T re = 0, im = 0;
     for (int o = 0; o < w; ++o) {
       const T c = __ldg(wt + o);
-      const Cx<T> v = __ldg(x + r);
+      const Cx<T> v = ldd<CG>(x + r);
       re = fma(c, v.x, re);
       im = fma(c, v.y, im);
       if (++r == n) r = 0;
@@ -268,8 +296,8 @@ __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in,
     // irfft pre-pass (FFTJ src/real.jl:149-192): Z[k] = xe + i (w xd)
     const int64_t h = pp.ld_n;
     const Cx<T>* X = reinterpret_cast<const Cx<T>*>(in) + b * pp.ld_stride;
-    const Cx<T> a = __ldg(X + g);
-    Cx<T> bb = __ldg(X + (h - g));
+    const Cx<T> a = ldd<CG>(X + g);
+    Cx<T> bb = ldd<CG>(X + (h - g));
     bb.y = -bb.y;
     const T pre = (T)pp.ld_pre;
     const Cx<T> xe = mk<T>((a.x + bb.x) * pre, (a.y + bb.y) * pre);
@@ -279,7 +307,7 @@ __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in,
     const T ti = fma(w.x, xd.y, w.y * xd.x);
     return mk<T>(xe.x - ti, xe.y + tr);
   } else {  // LOAD_REAL
-    const T x = __ldg(reinterpret_cast<const T*>(in) + b * pp.ld_stride + g);
+    const T x = ldd<CG>(reinterpret_cast<const T*>(in) + b * pp.ld_stride + g);
     return mk<T>(x, 0);
   }
 }
@@ -386,13 +414,19 @@ __device__ __forceinline__ void run_recipe(Recipe<Rs...>*, Cx<T>* buf, const int
 // One Stockham pass over one tile (the kernel comment in kernels.cu gives
 // the maps). Rec is RuntimeRecipe (radix sequence read from pp.sub) or a
 // Recipe<r...> fixed at compile time.
-template <typename T, int DIR, int LOADOP, class Rec>
-__device__ __forceinline__ void pass_body(const PassParams& pp, const void* __restrict__ in,
-                                          Cx<T>* __restrict__ out) {
+//
+// pass_tile runs tile `tile` with threads [0, nthr) of the CTA doing the
+// work. GROUP (the persistent group kernel): the CTA may have more threads
+// than the pass (the extra ones only join the barriers), and data loads are
+// L2-coherent.
+template <typename T, int DIR, int LOADOP, class Rec, bool GROUP>
+__device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __restrict__ in,
+                                          Cx<T>* __restrict__ out, const uint32_t tile, const int tid,
+                                          const int nthr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* buf = reinterpret_cast<Cx<T>*>(smem_raw);
   constexpr int EPT = Rec::kConst ? (Rec::R + Rec::Tf - 1) / Rec::Tf : 16;
-  const uint32_t tile = blockIdx.x;
+  const bool active = !GROUP || tid < nthr;
   const uint32_t t1 = pp.ftq.div(tile);
   const uint32_t tq = tile - t1 * pp.tiles_q;
   const uint32_t tb = pp.ftp.div(t1);
@@ -401,13 +435,13 @@ __device__ __forceinline__ void pass_body(const PassParams& pp, const void* __re
   const int R = Rec::kConst ? Rec::R : pp.R;
   const int Tf = Rec::kConst ? Rec::Tf : pp.Tf;
   const int P = pp.P, Q = pp.Q, NB = pp.NB;
-  const int E = NB * R;
+  const int E = active ? NB * R : 0;  // idle threads own no elements
   const int64_t ms = pp.m * pp.s;
-  const int tid = threadIdx.x, nthr = blockDim.x;
 
-  // this thread's column b = (bt, pl, ql) and first butterfly row kg
-  const int kg = (int)pp.fNB.div((uint32_t)tid);
-  const int b = tid - kg * NB;
+  // this thread's column b = (bt, pl, ql) and first butterfly row kg (idle
+  // threads get a row beyond every sub-stage, so they own no butterflies)
+  const int kg = active ? (int)pp.fNB.div((uint32_t)tid) : (1 << 29);
+  const int b = active ? tid - kg * NB : 0;
   const int cq = (int)pp.fQ.div((uint32_t)b);
   const int ql = b - cq * Q;
   const int cbt = (int)pp.fP.div((uint32_t)cq);
@@ -427,7 +461,7 @@ __device__ __forceinline__ void pass_body(const PassParams& pp, const void* __re
         if (e < E) {
           const int c = Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e);
           const int64_t bb = b0 + c;
-          v[i] = bb < pp.nbatch ? load_elem<T, LOADOP>(pp, in, bb, e - c * R) : mk<T>(0, 0);
+          v[i] = bb < pp.nbatch ? load_elem<T, LOADOP, GROUP>(pp, in, bb, e - c * R) : mk<T>(0, 0);
         }
       }
 #pragma unroll
@@ -445,7 +479,7 @@ __device__ __forceinline__ void pass_body(const PassParams& pp, const void* __re
 #pragma unroll
       for (int i = 0; i < EPT; ++i) {
         const int j = kg + i * Tf;
-        if (j < R) v[i] = ok ? load_elem<T, LOADOP>(pp, in, batch, gcol + (int64_t)j * ms) : mk<T>(0, 0);
+        if (j < R) v[i] = ok ? load_elem<T, LOADOP, GROUP>(pp, in, batch, gcol + (int64_t)j * ms) : mk<T>(0, 0);
       }
 #pragma unroll
       for (int i = 0; i < EPT; ++i) {
@@ -537,6 +571,12 @@ __device__ __forceinline__ void pass_body(const PassParams& pp, const void* __re
       }
     }
   }
+}
+
+template <typename T, int DIR, int LOADOP, class Rec>
+__device__ __forceinline__ void pass_body(const PassParams& pp, const void* __restrict__ in,
+                                          Cx<T>* __restrict__ out) {
+  pass_tile<T, DIR, LOADOP, Rec, false>(pp, in, out, blockIdx.x, threadIdx.x, blockDim.x);
 }
 
 // load_elem with the batch offset already applied (boff = batch * stride)

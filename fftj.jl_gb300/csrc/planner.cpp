@@ -11,15 +11,20 @@
 // in shared memory by radix-2..16 sub-stages).
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
 #include "../../include/fftj.h"
 #include "fftj_internal.h"
+#include "plan_internal.h"
 
 using namespace fftj;
 typedef int64_t i64;
@@ -136,6 +141,7 @@ Resample resample_parts(i64 n, bool f64, double scale, i64 m_override = 0) {
   r.w = 4 * ((wc + 3) / 4);
   r.beta = 0.97 * M_PI * r.w * (1 - (double)n / (2.0 * r.m));
   r.h = r.w / 2;
+  if (g_sched.dry) return r;  // a dry plan needs the sizes, not the tables
   std::vector<double> zq, wq;
   gausslegendre((int)(2 * r.w + 20), zq, wq);
   r.corr.resize(n);
@@ -313,7 +319,16 @@ Hvdh hvdh_parts(i64 n, bool f64, double scale) {
   P.w = 2 * P.h;
   P.B = (int)std::floor(std::sqrt(std::log(1 / tol) / P.a) + 0.5);
   if (P.B < 1 || P.B > 3) return P;
-  P.H = hvdh_halo(n, t, P.a, P.B, tol);
+  {
+    // the probe costs milliseconds; plans of one length (and the tuner's
+    // candidates) share its result
+    static std::mutex mu;
+    static std::map<std::tuple<i64, i64, int, bool>, i64> cache;
+    const auto key = std::make_tuple(n, t, P.B, f64);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    P.H = it != cache.end() ? it->second : (cache[key] = hvdh_halo(n, t, P.a, P.B, tol));
+  }
   if (P.H < 0) return P;
   // chunks: L rows (a divisor of t near 128), R = L + 2H rows each
   i64 L = 1;
@@ -323,6 +338,10 @@ Hvdh hvdh_parts(i64 n, bool f64, double scale) {
   P.R = L + 2 * P.H;
   P.nchunk = t / L;
   P.sc = scale * (double)n / (double)t;
+  if (g_sched.dry) {  // a dry plan needs the sizes, not the tables
+    P.ok = true;
+    return P;
+  }
   // spread table (src/hvdh.jl:726-752 restated per output row)
   const i64 w = P.w, hw = P.h;
   P.wt.resize(t * w);
@@ -402,11 +421,16 @@ int env_int(const char* name, int dflt) {
   const char* v = std::getenv(name);
   return v && *v ? std::atoi(v) : dflt;
 }
+thread_local SchedOpts g_sched;
+
 DtypeCfg dtype_cfg(bool f64) {
   // F32: 4096-element tiles (35 KB) give 4 CTAs of 256 threads per SM,
   // measured faster than 8192-element tiles at 2 CTAs per SM
-  if (f64) return DtypeCfg{16, env_int("FFTJ_TILE_F64", 4096), 4096, 256, 1024, 4};
-  return DtypeCfg{8, env_int("FFTJ_TILE_F32", 4096), 8192, 512, 1024, 8};
+  DtypeCfg c = f64 ? DtypeCfg{16, env_int("FFTJ_TILE_F64", 4096), 4096, 256, 1024, 4}
+                   : DtypeCfg{8, env_int("FFTJ_TILE_F32", 4096), 8192, 512, 1024, 8};
+  if (g_sched.tile > 0) c.tile_max = std::min(std::max(g_sched.tile, 256), c.tile_cap);
+  if (g_sched.threads_max > 0) c.threads_max = std::min(c.threads_max, std::max(g_sched.threads_max, 64));
+  return c;
 }
 
 
@@ -429,10 +453,32 @@ int pass_radices(i64 n, bool f64, bool strided, i64* Rs, int cap) {
   for (int p : {2, 3, 5, 7, 11, 13})
     while (r % p == 0 && np < 64) { r /= p; primes[np++] = p; }
   if (r != 1 || n < 1) return 0;
-  if ((!strided && n <= cfg.tile_cap) || n <= cfg.rmax_multi) { Rs[0] = n; return 1; }
-  for (int k = 1; k <= cap && k < 16; ++k)
-    if (split_bins(primes, np, k, cfg.rmax_multi, Rs)) return k;
-  return 0;
+  // one pass holds the whole transform in a tile of <= 16 elements per thread
+  const i64 one_cap = std::min<i64>(cfg.tile_cap, 16 * (i64)cfg.threads_max);
+  int k = 0;
+  if ((!strided && n <= one_cap) || n <= cfg.rmax_multi) {
+    Rs[0] = n;
+    k = 1;
+  } else {
+    for (int kk = 1; kk <= cap && kk < 16 && !k; ++kk)
+      if (split_bins(primes, np, kk, cfg.rmax_multi, Rs)) k = kk;
+    if (!k) return 0;
+  }
+  // schedule options: more passes than the fewest, then a permutation
+  const int want = std::min(std::min(k + std::max(g_sched.extra_passes, 0), cap), std::min(np, 15));
+  if (want > k && split_bins(primes, np, want, cfg.rmax_multi, Rs)) k = want;
+  if (g_sched.order > 0 && k > 1) {
+    // the order-th lexicographic permutation of the (descending) bins
+    int idx[16];
+    for (int i = 0; i < k; ++i) idx[i] = i;
+    int64_t f = 1;
+    for (int i = 2; i <= k; ++i) f *= i;
+    for (int it = 0; it < (int)(g_sched.order % f); ++it) std::next_permutation(idx, idx + k);
+    i64 tmp[16];
+    for (int i = 0; i < k; ++i) tmp[i] = Rs[idx[i]];
+    for (int i = 0; i < k; ++i) Rs[i] = tmp[i];
+  }
+  return k;
 }
 
 // sub-radix sequence of one pass: odd primes first, then the power-of-two
@@ -494,6 +540,7 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
     };
     i64 Tf = 1;
     while (!tf_ok(Tf)) Tf++;
+    if (g_sched.tf_mult > 1 && Tf * g_sched.tf_mult <= std::min<i64>(R, cfg.threads_max)) Tf *= g_sched.tf_mult;
     // tile: columns (batch, p, q); NB * Tf threads. Passes over strided
     // data keep >= min_run columns (contiguous elements per HBM run).
     const bool one_pass = (m == 1 && s == 1);
@@ -598,54 +645,15 @@ namespace {
 }  // namespace
 
 // ---------------------------------------------------------------------------
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-};
-
-enum OpKind { OP_PASS = 0, OP_INTERP = 1, OP_RPOST = 2, OP_COPY = 3, OP_SOLVE = 4 };
-enum BufId { B_IN = 0, B_OUT = 1, B_W0 = 2, B_W1 = 3 };
-
-struct Op {
-  OpKind kind;
-  int src, dst;
-  int dir = -1;
-  const void* kfn = nullptr;  // recipe kernel for OP_PASS (nullptr: generic)
-  PassParams pp;
-  InterpParams ip;
-  RealPostParams rp;
-  CopyParams cp;
-  SolveParams sv;
-  size_t dst_bytes = 0;  // bytes written (for workspace sizing)
-};
-
-struct fftj_plan_s {
-  int dtype = 0;
-  int kind = 0;  // 0 c2c, 1 r2c, 2 c2r
-  int route = FFTJ_ROUTE_DIRECT;
-  std::vector<i64> dims;
-  i64 n = 1, batch = 1;
-  i64 resample_m = 0, resample_w = 0;
-  std::vector<Op> ops;
-  std::vector<DevBuf> tables;
-  DevBuf ws[2];
-  size_t table_bytes = 0;
-  bool inplace_safe = false;
-  int npasses = 0;
-  std::vector<int> pass_R;
-  ~fftj_plan_s() {
-    for (auto& t : tables)
-      if (t.p) cudaFree(t.p);
-    for (auto& w : ws)
-      if (w.p) cudaFree(w.p);
-  }
-};
-
 namespace {
 
 // upload a table of complex values (re, im pairs in double) as T
+// stand-in address of a table that a dry plan does not build
+const void* const kDryTable = reinterpret_cast<const void*>(uintptr_t(256));
+
 template <typename T>
 const void* upload_cplx(fftj_plan_s* P, const std::vector<double>& ri) {
+  if (g_sched.dry) return kDryTable;
   std::vector<T> h(ri.size());
   for (size_t i = 0; i < ri.size(); ++i) h[i] = (T)ri[i];
   DevBuf b;
@@ -660,6 +668,7 @@ const void* upload_cplx(fftj_plan_s* P, const std::vector<double>& ri) {
   return b.p;
 }
 const void* upload_raw(fftj_plan_s* P, const void* data, size_t bytes) {
+  if (g_sched.dry) return kDryTable;
   DevBuf b;
   b.bytes = bytes;
   if (cudaMalloc(&b.p, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
@@ -675,6 +684,7 @@ const void* upload_raw(fftj_plan_s* P, const void* data, size_t bytes) {
 // the complex table w_n^e for e in [0, count), sign dir
 template <typename T>
 const void* omega_table(fftj_plan_s* P, i64 n, i64 count, i64 stride, int dir) {
+  if (g_sched.dry) return kDryTable;
   std::vector<double> ri(2 * count);
   for (i64 e = 0; e < count; ++e) omega(e * stride, n, dir, &ri[2 * e], &ri[2 * e + 1]);
   return upload_cplx<T>(P, ri);
@@ -753,6 +763,7 @@ int alloc_workspace(fftj_plan_s* P) {
   for (int i = 0; i < 2; ++i) {
     if (need[i] == 0) continue;
     P->ws[i].bytes = need[i];
+    if (P->dry) continue;
     if (cudaMalloc(&P->ws[i].p, need[i]) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "workspace allocation failed");
   }
   return FFTJ_OK;
@@ -808,7 +819,8 @@ int build_c2c_hvdh(fftj_plan_s* P, const Hvdh& hv, i64 batch, i64 idist, i64 odi
     // forward-substitution scratch owned by the plan
     DevBuf zb;
     zb.bytes = (size_t)hv.R * batch * hv.nchunk * sizeof(T) * 2;
-    if (cudaMalloc(&zb.p, zb.bytes) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "workspace allocation failed");
+    if (g_sched.dry) zb.bytes = 0, zb.p = const_cast<void*>(kDryTable);
+    else if (cudaMalloc(&zb.p, zb.bytes) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "workspace allocation failed");
     P->tables.push_back(zb);
     q.zw = zb.p;
   }
@@ -840,7 +852,8 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
     return FFTJ_OK;
   }
   // odd non-smooth lengths FFTJ sends to Gaussian resampling (HvdH)
-  if (use_hvdh(sizeof(T) == 8, n)) {
+  const bool hv_ok = g_sched.route == 2 ? (n % 2 == 1 && n >= 64) : (g_sched.route == 0 && use_hvdh(sizeof(T) == 8, n));
+  if (hv_ok) {
     Hvdh hv = hvdh_parts(n, sizeof(T) == 8, scale);
     if (hv.ok) return build_c2c_hvdh<T>(P, hv, batch, idist, odist, dir, ops, route);
   }
@@ -859,8 +872,8 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
   f.ld_stride = idist;
   f.ld_inner = 1;
   {
-    std::vector<T> c(n);
-    for (i64 j = 0; j < n; ++j) c[j] = (T)rs.corr[j];
+    std::vector<T> c(rs.corr.size());  // empty in a dry plan
+    for (size_t j = 0; j < c.size(); ++j) c[j] = (T)rs.corr[j];
     f.ld_tab = upload_raw(P, c.data(), c.size() * sizeof(T));
     if (!f.ld_tab) return fail(FFTJ_ERR_CUDA, "table upload failed");
   }
@@ -907,8 +920,8 @@ int build_axis_resample(fftj_plan_s* P, i64 nd, i64 Bi, i64 nb, int dir, double 
   f.ld_stride = Bi * nd;
   f.ld_inner = Bi;
   {
-    std::vector<T> c(nd);
-    for (i64 j = 0; j < nd; ++j) c[j] = (T)rs.corr[j];
+    std::vector<T> c(rs.corr.size());  // empty in a dry plan
+    for (size_t j = 0; j < c.size(); ++j) c[j] = (T)rs.corr[j];
     f.ld_tab = upload_raw(P, c.data(), c.size() * sizeof(T));
     if (!f.ld_tab) return fail(FFTJ_ERR_CUDA, "table upload failed");
   }
@@ -1179,6 +1192,7 @@ int finalize_passes(fftj_plan_s* P) {
     if (op.kind != OP_PASS) continue;
     op.kfn = pick_pass_kernel(sizeof(T) == 8, op.dir, op.pp);
     op.pp.smem_tw_elems = op.kfn ? op.pp.R : 0;
+    if (P->dry) continue;
     if (prepare_pass<T>(op.pp, op.dir, op.kfn) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
   }
   return FFTJ_OK;
@@ -1198,18 +1212,42 @@ int finish(fftj_plan_s* P, fftj_plan* out) {
 
 }  // namespace
 
+// Installs a planning call's schedule options on this host thread and
+// restores the defaults when the call returns.
+struct SchedScope {
+  explicit SchedScope(const fftj_plan_opts_t* o) {
+    g_sched = SchedOpts();
+    if (!o) return;
+    g_sched.tile = o->tile;
+    g_sched.extra_passes = std::min(std::max(o->extra_passes, 0), 2);
+    g_sched.order = std::max(o->order, 0);
+    g_sched.tf_mult = std::min(std::max(o->tf_mult, 0), 4);
+    g_sched.route = o->route;
+    g_sched.threads_max = o->threads_max;
+    g_sched.dry = o->dry != 0;
+  }
+  ~SchedScope() { g_sched = SchedOpts(); }
+};
+
 extern "C" {
 
 int fftj_plan_c2c(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch, int64_t idist,
                   int64_t odist, int dir, double scale) {
+  return fftj_plan_c2c_ex(out, dtype, rank, dims, batch, idist, odist, dir, scale, nullptr);
+}
+
+int fftj_plan_c2c_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch, int64_t idist,
+                     int64_t odist, int dir, double scale, const fftj_plan_opts_t* opts) {
   if (!out) return fail(FFTJ_ERR_ARG, "null plan pointer");
   *out = nullptr;
+  SchedScope scope(opts);
   std::vector<i64> d;
   if (int rc = check_dims(rank, dims, &d)) return rc;
   if (dtype != FFTJ_F32 && dtype != FFTJ_F64) return fail(FFTJ_ERR_ARG, "dtype must be F32 or F64");
   if (dir != -1 && dir != 1) return fail(FFTJ_ERR_ARG, "dir must be -1 or +1");
   if (batch < 1) return fail(FFTJ_ERR_ARG, "batch must be >= 1");
   std::unique_ptr<fftj_plan_s> P(new fftj_plan_s());
+  P->dry = g_sched.dry;
   P->dtype = dtype;
   P->kind = 0;
   P->dims = d;
@@ -1233,13 +1271,20 @@ int fftj_plan_c2c(fftj_plan* out, int dtype, int rank, const int64_t* dims, int6
 
 int fftj_plan_r2c(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch, int64_t idist,
                   int64_t odist) {
+  return fftj_plan_r2c_ex(out, dtype, rank, dims, batch, idist, odist, nullptr);
+}
+
+int fftj_plan_r2c_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch, int64_t idist,
+                     int64_t odist, const fftj_plan_opts_t* opts) {
   if (!out) return fail(FFTJ_ERR_ARG, "null plan pointer");
   *out = nullptr;
+  SchedScope scope(opts);
   std::vector<i64> d;
   if (int rc = check_dims(rank, dims, &d)) return rc;
   if (dtype != FFTJ_F32 && dtype != FFTJ_F64) return fail(FFTJ_ERR_ARG, "dtype must be F32 or F64");
   if (batch < 1) return fail(FFTJ_ERR_ARG, "batch must be >= 1");
   std::unique_ptr<fftj_plan_s> P(new fftj_plan_s());
+  P->dry = g_sched.dry;
   P->dtype = dtype;
   P->kind = 1;
   P->dims = d;
@@ -1261,13 +1306,20 @@ int fftj_plan_r2c(fftj_plan* out, int dtype, int rank, const int64_t* dims, int6
 
 int fftj_plan_c2r(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch, int64_t idist,
                   int64_t odist, int normalized) {
+  return fftj_plan_c2r_ex(out, dtype, rank, dims, batch, idist, odist, normalized, nullptr);
+}
+
+int fftj_plan_c2r_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch, int64_t idist,
+                     int64_t odist, int normalized, const fftj_plan_opts_t* opts) {
   if (!out) return fail(FFTJ_ERR_ARG, "null plan pointer");
   *out = nullptr;
+  SchedScope scope(opts);
   std::vector<i64> d;
   if (int rc = check_dims(rank, dims, &d)) return rc;
   if (dtype != FFTJ_F32 && dtype != FFTJ_F64) return fail(FFTJ_ERR_ARG, "dtype must be F32 or F64");
   if (batch < 1) return fail(FFTJ_ERR_ARG, "batch must be >= 1");
   std::unique_ptr<fftj_plan_s> P(new fftj_plan_s());
+  P->dry = g_sched.dry;
   P->dtype = dtype;
   P->kind = 2;
   P->dims = d;
@@ -1290,6 +1342,7 @@ int fftj_plan_c2r(fftj_plan* out, int dtype, int rank, const int64_t* dims, int6
 int fftj_execute(fftj_plan plan, const void* d_in, void* d_out, void* stream) {
   if (!plan) return fail(FFTJ_ERR_ARG, "null plan");
   if (!d_in || !d_out) return fail(FFTJ_ERR_ARG, "null data pointer");
+  if (plan->dry) return fail(FFTJ_ERR_ARG, "a dry plan (opts.dry = 1) holds no tables and cannot execute");
   cudaStream_t st = (cudaStream_t)stream;
   fftj_plan_s* P = plan;
   void* bufs[4] = {const_cast<void*>(d_in), d_out, P->ws[0].p, P->ws[1].p};
@@ -1338,8 +1391,101 @@ int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info) {
   for (size_t i = 0; i < plan->pass_R.size() && i < 8; ++i) info->pass_radix[i] = plan->pass_R[i];
   info->workspace_bytes = plan->ws[0].bytes + plan->ws[1].bytes;
   info->table_bytes = plan->table_bytes;
-  for (auto& op : plan->ops)
-    if (op.kind == OP_PASS && op.kfn) info->specialized_passes++;
+  info->nops = (int)plan->ops.size();
+  info->dry = plan->dry ? 1 : 0;
+  // FNV-1a over everything that shapes the launches
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](int64_t v) {
+    for (int i = 0; i < 8; ++i) {
+      h ^= (uint64_t)((v >> (8 * i)) & 0xff);
+      h *= 1099511628211ull;
+    }
+  };
+  mix(plan->route);
+  mix(plan->kind);
+  mix(plan->dtype);
+  int pi = 0;
+  for (auto& op : plan->ops) {
+    mix(op.kind);
+    if (op.kind == OP_PASS) {
+      const PassParams& pp = op.pp;
+      if (op.kfn) info->specialized_passes++;
+      if (pi < 8) {
+        info->pass_tile[pi] = pp.NB * pp.R;
+        info->pass_threads[pi] = pp.threads;
+        info->pass_ctas[pi] = (int64_t)pp.tiles_q * pp.tiles_p * pp.tiles_b;
+      }
+      pi++;
+      for (int64_t v : {(int64_t)pp.R, (int64_t)pp.P, (int64_t)pp.Q, (int64_t)pp.NBt, (int64_t)pp.Tf,
+                        (int64_t)pp.threads, (int64_t)pp.nsub, (int64_t)pp.tw_mode, (int64_t)pp.load_op,
+                        (int64_t)(uintptr_t)op.kfn})
+        mix(v);
+      for (int i = 0; i < pp.nsub; ++i) mix(pp.sub[i].r);
+    } else if (op.kind == OP_INTERP) {
+      mix(op.ip.w);
+      mix(op.ip.m);
+    } else if (op.kind == OP_SOLVE) {
+      mix(op.sv.L);
+      mix(op.sv.H);
+      mix(op.sv.B);
+    } else if (op.kind == OP_COPY) {
+      mix(op.cp.mode);
+    }
+  }
+  info->schedule_hash = h;
+  return FFTJ_OK;
+}
+
+int fftj_plan_features(fftj_plan plan, float* out, int cap) {
+  if (!plan || !out || cap < FFTJ_NFEATURES) return fail(FFTJ_ERR_ARG, "null plan/output or cap < FFTJ_NFEATURES");
+  auto lg = [](double x) { return x > 0 ? std::log2(x) : 0.0; };
+  double f[FFTJ_NFEATURES] = {0};
+  const bool f64 = plan->dtype == FFTJ_F64;
+  f[0] = lg((double)plan->n);
+  f[1] = lg((double)plan->batch);
+  f[2] = f64 ? 1 : 0;
+  f[3] = plan->kind == 1;
+  f[4] = plan->kind == 2;
+  f[5] = plan->route == FFTJ_ROUTE_RESAMPLE;
+  f[6] = plan->route == FFTJ_ROUTE_HVDH;
+  f[7] = plan->route == FFTJ_ROUTE_ND;
+  f[8] = (double)plan->ops.size();
+  int np = 0, spec = 0;
+  double bytes = 0, ctas = 0;
+  for (auto& op : plan->ops) {
+    bytes += 2.0 * (double)op.dst_bytes;
+    if (op.kind == OP_PASS) {
+      const PassParams& pp = op.pp;
+      const double c = (double)pp.tiles_q * pp.tiles_p * pp.tiles_b;
+      ctas += c;
+      if (np < 3) {
+        f[10 + np] = lg(pp.R);
+        f[13 + np] = lg((double)pp.NB * pp.R);
+        f[16 + np] = lg(pp.threads);
+        f[19 + np] = lg(c);
+      }
+      np++;
+      if (op.kfn) spec++;
+    } else {
+      double total = 0;
+      if (op.kind == OP_INTERP) total = (double)op.ip.n * op.ip.nbatch * std::max<int64_t>(op.ip.inner, 1);
+      else if (op.kind == OP_RPOST) total = (double)(op.rp.h + 1) * op.rp.nbatch;
+      else if (op.kind == OP_COPY) total = (double)op.cp.n * op.cp.nbatch;
+      else if (op.kind == OP_SOLVE) total = (double)op.sv.nbatch * op.sv.nchunk;
+      ctas += std::ceil(total / 256.0);
+    }
+  }
+  f[9] = np;
+  f[22] = np ? (double)spec / np : 0;
+  f[23] = lg(bytes);
+  const double grid = (double)(plan->resample_m ? plan->resample_m : plan->n);
+  f[24] = lg(grid);
+  i64 g = plan->resample_m ? plan->resample_m : plan->n;
+  while (g > 1 && g % 2 == 0) g /= 2;
+  f[25] = lg((double)g);
+  f[26] = np - spec;
+  f[27] = lg(ctas);
+  for (int i = 0; i < FFTJ_NFEATURES; ++i) out[i] = (float)f[i];
   return FFTJ_OK;
 }
 

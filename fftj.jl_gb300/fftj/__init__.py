@@ -50,14 +50,47 @@ class PlanInfo(ctypes.Structure):
         ("batch", ctypes.c_int64), ("resample_m", ctypes.c_int64), ("resample_w", ctypes.c_int64),
         ("pass_radix", ctypes.c_int * 8), ("workspace_bytes", ctypes.c_size_t),
         ("table_bytes", ctypes.c_size_t), ("specialized_passes", ctypes.c_int),
+        ("schedule_hash", ctypes.c_uint64), ("pass_tile", ctypes.c_int * 8),
+        ("pass_threads", ctypes.c_int * 8), ("pass_ctas", ctypes.c_int64 * 8), ("nops", ctypes.c_int),
+        ("dry", ctypes.c_int),
     ]
+
+
+class PlanOpts(ctypes.Structure):
+    """fftj_plan_opts_t: schedule options (all zero = the planner's default)."""
+    _fields_ = [(k, ctypes.c_int32) for k in
+                ("tile", "extra_passes", "order", "tf_mult", "route", "threads_max", "dry", "reserved")]
+
+
+class TuneQuery(ctypes.Structure):
+    """fftj_tune_query_t: one transform problem for the autotuner."""
+    _fields_ = [("kind", ctypes.c_int32), ("dtype", ctypes.c_int32), ("rank", ctypes.c_int32),
+                ("dir", ctypes.c_int32), ("dims", ctypes.c_int64 * 3), ("batch", ctypes.c_int64),
+                ("min_ms", ctypes.c_double), ("trials", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+NFEATURES = 28
+
+
+class GroupInfo(ctypes.Structure):
+    """fftj_group_info_t."""
+    _fields_ = [(k, ctypes.c_int) for k in
+                ("mode", "nplans", "nops", "nitems", "ctas", "smem_bytes", "branches", "kernels")]
+
+
+GROUP_MODES = {"stream": 0, "graph": 1, "persistent": 2}
 
 
 _lib = None
 EXPORTS = [
     "fftj_plan_c2c", "fftj_plan_r2c", "fftj_plan_c2r", "fftj_execute", "fftj_plan_get_info",
     "fftj_plan_workspace_bytes", "fftj_plan_destroy", "fftj_last_error_string", "fftj_version",
-    "fftj_execute_noalloc_c2c",
+    "fftj_execute_noalloc_c2c", "fftj_plan_c2c_ex", "fftj_plan_r2c_ex", "fftj_plan_c2r_ex",
+    "fftj_plan_features", "fftj_tune_plan", "fftj_tune_candidates", "fftj_tune_measure", "fftj_autotune",
+    "fftj_mlp_create", "fftj_mlp_destroy", "fftj_mlp_num_params", "fftj_mlp_get_params",
+    "fftj_mlp_set_params", "fftj_mlp_grad", "fftj_mlp_train", "fftj_mlp_predict",
+    "fftj_group_create", "fftj_group_execute", "fftj_group_status", "fftj_group_get_info",
+    "fftj_group_set_wait_limit", "fftj_group_debug_stall", "fftj_group_destroy",
 ]
 
 
@@ -84,6 +117,32 @@ def lib():
         L.fftj_plan_workspace_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
         L.fftj_plan_destroy.argtypes = [vp]
         L.fftj_execute_noalloc_c2c.argtypes = [i32, i64, i64, i32, ctypes.c_double, vp, vp, vp]
+        PO, PQ = ctypes.POINTER(PlanOpts), ctypes.POINTER(TuneQuery)
+        PF, PD = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_double)
+        L.fftj_plan_c2c_ex.argtypes = L.fftj_plan_c2c.argtypes + [PO]
+        L.fftj_plan_r2c_ex.argtypes = L.fftj_plan_r2c.argtypes + [PO]
+        L.fftj_plan_c2r_ex.argtypes = L.fftj_plan_c2r.argtypes + [PO]
+        L.fftj_plan_features.argtypes = [vp, PF, i32]
+        L.fftj_tune_plan.argtypes = [PQ, PO, ctypes.POINTER(vp)]
+        L.fftj_tune_candidates.argtypes = [PQ, PO, i32, ctypes.POINTER(i32)]
+        L.fftj_tune_measure.argtypes = [PQ, PO, i32, PD, vp]
+        L.fftj_autotune.argtypes = [PQ, PO, PD]
+        L.fftj_mlp_create.argtypes = [ctypes.POINTER(vp), i32, ctypes.c_uint64]
+        L.fftj_mlp_destroy.argtypes = [vp]
+        L.fftj_mlp_num_params.argtypes = [vp, ctypes.POINTER(i64)]
+        L.fftj_mlp_get_params.argtypes = [vp, PF, i64]
+        L.fftj_mlp_set_params.argtypes = [vp, PF, i64]
+        L.fftj_mlp_grad.argtypes = [vp, PF, PF, i64, PF, PD]
+        L.fftj_mlp_train.argtypes = [vp, PF, PF, i64, i32, i32, ctypes.c_float, ctypes.c_uint64, PD]
+        L.fftj_mlp_predict.argtypes = [vp, PF, i64, PF]
+        L.fftj_group_create.argtypes = [ctypes.POINTER(vp), i32, ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                        ctypes.POINTER(vp), i32]
+        L.fftj_group_execute.argtypes = [vp, vp]
+        L.fftj_group_status.argtypes = [vp]
+        L.fftj_group_get_info.argtypes = [vp, ctypes.POINTER(GroupInfo)]
+        L.fftj_group_set_wait_limit.argtypes = [vp, ctypes.c_uint32]
+        L.fftj_group_debug_stall.argtypes = [vp, i32]
+        L.fftj_group_destroy.argtypes = [vp]
         L.fftj_last_error_string.restype = ctypes.c_char_p
         L.fftj_version.restype = ctypes.c_char_p
         for name in EXPORTS:
@@ -120,7 +179,7 @@ class Plan:
 
     kind: 'c2c' | 'r2c' | 'c2r'. dims are FFTJ's column-major lengths."""
 
-    def __init__(self, T, dims, kind="c2c", direction=-1, scale=1.0, batch=1, normalized=True):
+    def __init__(self, T, dims, kind="c2c", direction=-1, scale=1.0, batch=1, normalized=True, opts=None):
         self.dt = _dtcode(T)
         self.dims = tuple(int(d) for d in dims)
         if any(d < 1 for d in self.dims):
@@ -133,14 +192,22 @@ class Plan:
         self.n = int(np.prod(self.dims))
         h = ctypes.c_void_p()
         arr = (ctypes.c_int64 * len(self.dims))(*self.dims)
-        if kind == "c2c":
-            rc = lib().fftj_plan_c2c(ctypes.byref(h), self.dt, len(self.dims), arr, self.batch, 0, 0,
-                                     int(direction), self.scale)
-        elif kind == "r2c":
-            rc = lib().fftj_plan_r2c(ctypes.byref(h), self.dt, len(self.dims), arr, self.batch, 0, 0)
+        # schedule options (fftj_plan_opts_t): a PlanOpts, a dict of its
+        # fields, or None for the planner's default schedule
+        if isinstance(opts, dict):
+            o = PlanOpts(**opts)
         else:
-            rc = lib().fftj_plan_c2r(ctypes.byref(h), self.dt, len(self.dims), arr, self.batch, 0, 0,
-                                     1 if normalized else 0)
+            o = opts if opts is not None else PlanOpts()
+        self.opts = o
+        po = ctypes.byref(o)
+        if kind == "c2c":
+            rc = lib().fftj_plan_c2c_ex(ctypes.byref(h), self.dt, len(self.dims), arr, self.batch, 0, 0,
+                                        int(direction), self.scale, po)
+        elif kind == "r2c":
+            rc = lib().fftj_plan_r2c_ex(ctypes.byref(h), self.dt, len(self.dims), arr, self.batch, 0, 0, po)
+        else:
+            rc = lib().fftj_plan_c2r_ex(ctypes.byref(h), self.dt, len(self.dims), arr, self.batch, 0, 0,
+                                        1 if normalized else 0, po)
         _check(rc)
         self._h = h
 
@@ -216,6 +283,56 @@ class Plan:
     def __repr__(self):
         return "fftj.Plan(%s, dims=%s, dir=%d, batch=%d, route=%s)" % (
             self.kind, self.dims, self.direction, self.batch, self.route)
+
+
+class Group:
+    """Many plans executed as one unit (no counterpart in FFTJ, which runs one
+    plan per call). mode: "stream" (launches back to back), "graph" (one
+    CUDA graph, plans on parallel branches) or "persistent" (one persistent
+    work-queue kernel in a CUDA graph; plans need opts.threads_max = 256).
+    Buffers are bound here; each call runs every plan on the current stream."""
+
+    def __init__(self, plans, inputs, outputs, mode="graph"):
+        if not (len(plans) == len(inputs) == len(outputs)) or not plans:
+            raise DimensionMismatch("a group needs one input and one output per plan")
+        for p, x, y in zip(plans, inputs, outputs):
+            p._validate(x, p.in_spec(), "input")
+            p._validate(y, p.out_spec(), "output")
+        n = len(plans)
+        self.plans, self.inputs, self.outputs = list(plans), list(inputs), list(outputs)
+        hs = (ctypes.c_void_p * n)(*[p._h.value for p in plans])
+        xi = (ctypes.c_void_p * n)(*[x.data_ptr() for x in inputs])
+        yo = (ctypes.c_void_p * n)(*[y.data_ptr() for y in outputs])
+        h = ctypes.c_void_p()
+        _check(lib().fftj_group_create(ctypes.byref(h), n, hs, xi, yo, GROUP_MODES[mode]))
+        self._h = h
+        self.mode = mode
+
+    def __call__(self):
+        stream = torch.cuda.current_stream(self.inputs[0].device).cuda_stream
+        _check(lib().fftj_group_execute(self._h, ctypes.c_void_p(stream)))
+
+    def status(self):
+        """Waits for the last execution; raises FFTJError on a timed-out wait."""
+        _check(lib().fftj_group_status(self._h))
+
+    @property
+    def info(self):
+        inf = GroupInfo()
+        _check(lib().fftj_group_get_info(self._h, ctypes.byref(inf)))
+        return inf
+
+    def set_wait_limit(self, spins):
+        _check(lib().fftj_group_set_wait_limit(self._h, int(spins)))
+
+    def debug_stall(self, op):
+        _check(lib().fftj_group_debug_stall(self._h, int(op)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.fftj_group_destroy(h)
+            self._h = None
 
 
 class InplacePlan:

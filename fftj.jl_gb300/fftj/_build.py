@@ -1,6 +1,6 @@
 """Builds libfftj_gb300.so (sm_103a) in-tree with nvcc.
 
-One -gencode (sm_103a), two translation units compiled in parallel, linked as
+One -gencode (sm_103a), the translation units compiled in parallel, linked as
 a shared library with the CUDA runtime statically linked. Used by
 __graft_entry__.build() on x86 and Arm (x86 here, aarch64 on the GPU machine).
 """
@@ -14,7 +14,7 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD = os.path.join(PKG_DIR, "_build")
 LIB = os.path.join(PKG_DIR, "libfftj_gb300.so")
 SOURCES = ["kernels.cu", "recipes_f32_fwd.cu", "recipes_f32_bwd.cu", "recipes_f64_fwd.cu",
-           "recipes_f64_bwd.cu", "noalloc.cu", "planner.cpp"]
+           "recipes_f64_bwd.cu", "noalloc.cu", "mlp.cu", "group.cu", "planner.cpp", "tune.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -55,7 +55,7 @@ def build(force=False, verbose=False):
     with ThreadPoolExecutor(len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)

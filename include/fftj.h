@@ -65,7 +65,102 @@ typedef struct {
   size_t workspace_bytes;
   size_t table_bytes;
   int specialized_passes; /* passes run by compile-time specialised kernels */
+  uint64_t schedule_hash; /* identifies the launch schedule (equal hash: same kernels, tiles, threads) */
+  int pass_tile[8];       /* elements per CTA tile of each pass */
+  int pass_threads[8];    /* threads per CTA of each pass */
+  int64_t pass_ctas[8];   /* CTAs (tiles) of each pass */
+  int nops;               /* kernel launches per execution (passes + elementwise ops) */
+  int dry;                /* 1: planned without tables or workspace (cannot execute) */
 } fftj_plan_info_t;
+
+/*
+ * Schedule options. No counterpart in the reference's API: FFTJ fixes its
+ * schedule from the vector width and cache thresholds (src/plan.jl:105-151,
+ * src/fourstep.jl:166-230); here the same choices -- radix split and order,
+ * tile shape, threads per transform, route for non-smooth lengths -- are
+ * exposed so that an autotuner can search them. All-zero = the planner's
+ * default schedule. Options that cannot apply to a length are ignored.
+ */
+typedef struct {
+  int32_t tile;          /* max elements per CTA tile (256 .. 8192 F32 / 4096 F64); 0 = default */
+  int32_t extra_passes;  /* HBM passes beyond the fewest that fit (0, 1, 2) */
+  int32_t order;         /* k-th lexicographic permutation of the pass radices (0 = largest first) */
+  int32_t tf_mult;       /* threads per transform column = the minimum x tf_mult (0/1 = minimum) */
+  int32_t route;         /* non-smooth lengths: 0 planner, 1 resampling, 2 Gaussian (HvdH) */
+  int32_t threads_max;   /* cap on threads per CTA (0 = 512 F32 / 256 F64) */
+  int32_t dry;           /* 1: plan the schedule only (no tables, no workspace, cannot execute) */
+  int32_t reserved;
+} fftj_plan_opts_t;
+
+int fftj_plan_c2c_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch,
+                     int64_t idist, int64_t odist, int dir, double scale, const fftj_plan_opts_t* opts);
+int fftj_plan_r2c_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch,
+                     int64_t idist, int64_t odist, const fftj_plan_opts_t* opts);
+int fftj_plan_c2r_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch,
+                     int64_t idist, int64_t odist, int normalized, const fftj_plan_opts_t* opts);
+
+/* Length of the feature vector fftj_plan_features writes. */
+#define FFTJ_NFEATURES 28
+
+/*
+ * Cost-model features of a plan's schedule (FFTJ_NFEATURES floats): sizes,
+ * dtype, kind, route, per-pass radix / tile / threads / CTAs, bytes moved.
+ * Works on dry plans. Used by the learned planner to score candidates.
+ */
+int fftj_plan_features(fftj_plan plan, float* out, int cap);
+
+/*
+ * Autotuner (no counterpart in the reference). A query names one transform
+ * problem; its candidates are the distinct schedules of a grid of
+ * fftj_plan_opts_t values (dry-planned, deduplicated by schedule hash; the
+ * default schedule is candidate 0).
+ */
+typedef struct {
+  int32_t kind;     /* 0 c2c, 1 r2c, 2 c2r (irfft) */
+  int32_t dtype;    /* fftj_dtype */
+  int32_t rank;     /* 1..3 */
+  int32_t dir;      /* c2c: -1 forward, +1 backward */
+  int64_t dims[3];  /* real dims for r2c/c2r */
+  int64_t batch;
+  double min_ms;    /* minimum timed region per trial (0 = 0.3 ms) */
+  int32_t trials;   /* timed trials per candidate, best kept (0 = 3) */
+  int32_t reserved;
+} fftj_tune_query_t;
+
+/* Plan a query with the given options (NULL = default). */
+int fftj_tune_plan(const fftj_tune_query_t* q, const fftj_plan_opts_t* opts, fftj_plan* out);
+/* Distinct candidate schedules of a query (up to cap); *count = how many. */
+int fftj_tune_candidates(const fftj_tune_query_t* q, fftj_plan_opts_t* out, int cap, int* count);
+/*
+ * Time candidates on the GPU: plans built in parallel on host threads, each
+ * timed with CUDA events on `stream` (best of q->trials trials of
+ * back-to-back executions); ms_out[i] = milliseconds per execution
+ * (HUGE_VAL if candidate i cannot be planned). Allocates its own buffers.
+ */
+int fftj_tune_measure(const fftj_tune_query_t* q, const fftj_plan_opts_t* cands, int ncand, double* ms_out,
+                      void* stream);
+/* Exhaustive autotune: candidates + measurement; the fastest schedule. */
+int fftj_autotune(const fftj_tune_query_t* q, fftj_plan_opts_t* best, double* best_ms);
+
+/*
+ * Learned cost model (no counterpart in the reference): an MLP in_dim -> 64
+ * -> 64 -> 1 (ReLU, FP32) whose training (forward, backward, Adam) and
+ * inference run as this library's own CUDA kernels. Host arrays in/out;
+ * X is row-major n x in_dim. Parameters flattened as W1[64][in_dim], b1[64],
+ * W2[64][64], b2[64], w3[64], b3.
+ */
+typedef struct fftj_mlp_s* fftj_mlp;
+int fftj_mlp_create(fftj_mlp* out, int in_dim, uint64_t seed); /* He-uniform init, in_dim <= 32 */
+int fftj_mlp_destroy(fftj_mlp m);
+int fftj_mlp_num_params(fftj_mlp m, int64_t* count);
+int fftj_mlp_get_params(fftj_mlp m, float* host, int64_t count);
+int fftj_mlp_set_params(fftj_mlp m, const float* host, int64_t count);
+/* Gradient of mean((f(X) - y)^2) over all n rows; *loss = that mean. */
+int fftj_mlp_grad(fftj_mlp m, const float* X, const float* y, int64_t n, float* grad, double* loss);
+/* Minibatch Adam for `epochs` passes (each epoch one replayed CUDA graph). */
+int fftj_mlp_train(fftj_mlp m, const float* X, const float* y, int64_t n, int epochs, int minibatch, float lr,
+                   uint64_t seed, double* final_loss);
+int fftj_mlp_predict(fftj_mlp m, const float* X, int64_t n, float* out);
 
 /*
  * 1-D / N-d complex plan.
@@ -141,6 +236,46 @@ const char* fftj_version(void);
  */
 int fftj_execute_noalloc_c2c(int dtype, int64_t n, int64_t batch, int dir, double scale, const void* d_in,
                              void* d_out, void* stream);
+
+/*
+ * Groups: many plans executed as one unit (no counterpart in the reference,
+ * which runs one plan per call). A group binds distinct plans to their
+ * buffers at creation; each execution runs all of them on `stream`.
+ *   FFTJ_GROUP_STREAM      the plans' kernels launched back to back;
+ *   FFTJ_GROUP_GRAPH       the same launches captured once as a CUDA graph
+ *                          with the plans on parallel branches;
+ *   FFTJ_GROUP_PERSISTENT  one persistent kernel draining a device queue of
+ *                          (op, tile range) items with bounded dependency
+ *                          waits, captured with its queue reset as a CUDA
+ *                          graph. Every pass must use <= 256 threads per CTA
+ *                          (plan with opts.threads_max = 256).
+ * Plans must outlive the group and must not run elsewhere while it runs.
+ */
+typedef struct fftj_group_s* fftj_group;
+typedef enum { FFTJ_GROUP_STREAM = 0, FFTJ_GROUP_GRAPH = 1, FFTJ_GROUP_PERSISTENT = 2 } fftj_group_mode;
+typedef struct {
+  int mode;
+  int nplans;
+  int nops;        /* ops over all plans */
+  int nitems;      /* queue items (persistent) */
+  int ctas;        /* persistent CTAs (one per resident slot) */
+  int smem_bytes;  /* dynamic shared memory of the persistent kernel */
+  int branches;    /* parallel graph branches (graph mode) */
+  int kernels;     /* kernel launches per execution */
+} fftj_group_info_t;
+
+int fftj_group_create(fftj_group* out, int count, const fftj_plan* plans, const void* const* d_in,
+                      void* const* d_out, int mode);
+int fftj_group_execute(fftj_group g, void* stream);
+/* Waits for the last execution; FFTJ_ERR_TIMEOUT if a persistent wait gave up. */
+int fftj_group_status(fftj_group g);
+int fftj_group_get_info(fftj_group g, fftj_group_info_t* info);
+/* Spin limit of each persistent dependency wait (default 2e6 polls, ~1 s). */
+int fftj_group_set_wait_limit(fftj_group g, uint32_t spins);
+/* Test hook: op `op` of a persistent group waits for a count that is never
+ * reached, so its waits run out (to exercise the timeout path). */
+int fftj_group_debug_stall(fftj_group g, int op);
+int fftj_group_destroy(fftj_group g);
 
 #ifdef __cplusplus
 }

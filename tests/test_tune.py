@@ -1,0 +1,101 @@
+"""Schedule options, dry planning, the autotuner's candidate sets, the uneven
+workload generator and the cost model's numpy restatement -- everything of
+the tuning path that needs no GPU. (Timing, training and the group executor
+are in test_learned_gpu.py / test_group_gpu.py.)"""
+import numpy as np
+import pytest
+
+from conftest import ROOT  # noqa: F401  (puts the package on sys.path)
+
+
+@pytest.fixture(scope="module")
+def T():
+    import fftj
+    fftj.build()
+    from fftj import tune
+    return tune
+
+
+def info(T, kind, dtype, n, **opts):
+    q = T.query(kind, dtype, n)
+    t = tuple(opts.get(f, 0) for f in T.OPT_FIELDS)
+    return T.plan_info(q, t, dry=True)
+
+
+def test_dry_plans_need_no_gpu_and_hold_nothing(T):
+    inf = info(T, "c2c", np.float64, 1 << 18)
+    assert inf.dry == 1 and inf.table_bytes == 0
+    assert inf.workspace_bytes > 0  # sized, not allocated
+    assert list(inf.pass_radix[:inf.npasses]) == [512, 512]
+
+
+def test_options_shape_the_schedule(T):
+    base = info(T, "c2c", np.float32, 42525)
+    assert list(base.pass_radix[:2]) == [225, 189]
+    rev = info(T, "c2c", np.float32, 42525, order=1)
+    assert list(rev.pass_radix[:2]) == [189, 225]
+    more = info(T, "c2c", np.float32, 1 << 18, extra_passes=1)
+    assert more.npasses == 3 and np.prod(more.pass_radix[:3]) == 1 << 18
+    tf = info(T, "c2c", np.float32, 1 << 18, tf_mult=2)
+    assert tf.pass_threads[0] == 2 * base.pass_threads[0] or tf.pass_threads[0] > info(
+        T, "c2c", np.float32, 1 << 18).pass_threads[0]
+    cap = info(T, "c2c", np.float32, 8192, threads_max=256)
+    assert cap.npasses == 2 and max(cap.pass_threads[:2]) <= 256
+    small = info(T, "c2c", np.float32, 1 << 18, tile=2048)
+    assert small.pass_tile[0] <= 8192
+    # route knob for non-smooth lengths
+    assert info(T, "c2c", np.float64, 10007).route == 3            # HvdH by default (F64)
+    assert info(T, "c2c", np.float64, 10007, route=1).route == 2   # forced resampling
+    assert info(T, "c2c", np.float32, 10007).route == 2            # resampling by default (F32)
+    assert info(T, "c2c", np.float32, 10007, route=2).route == 3   # forced HvdH
+    assert info(T, "c2c", np.float32, 10240, route=2).route in (0, 1)  # smooth: knob ignored
+
+
+def test_candidates_are_distinct_and_start_with_default(T):
+    for kind, dt, n in [("c2c", np.float32, 1 << 18), ("c2c", np.float64, 10007), ("r2c", np.float32, 4096),
+                        ("c2c", np.float32, 64), ("r2c", np.float64, 1009), ("c2c", np.float64, 42525)]:
+        q = T.query(kind, dt, n)
+        c = T.candidates(q)
+        assert c[0] == (0,) * len(T.OPT_FIELDS)
+        hashes = [T.plan_info(q, t).schedule_hash for t in c]
+        assert len(set(hashes)) == len(c) >= 2, (kind, n)
+        f = T.features(q, c)
+        assert f.shape == (len(c), T.NFEATURES) and np.isfinite(f).all()
+
+
+def test_features_follow_the_schedule(T):
+    q = T.query("c2c", np.float32, 1 << 18)
+    f = T.features(q, [(0, 0, 0, 0, 0, 0), (0, 1, 0, 0, 0, 0)])
+    assert f[0, 0] == pytest.approx(18.0) and f[0, 9] == 2 and f[1, 9] == 3
+    q = T.query("r2c", np.float64, 1009)
+    f = T.features(q, [(0,) * 6])[0]
+    assert f[2] == 1 and f[3] == 1
+
+
+def test_uneven_workload_distribution(T):
+    w = T.uneven_workload(10000, seed=5)
+    ns = np.array([x[2] for x in w])
+    primes = np.array([T.is_prime(int(n)) for n in ns])
+    assert abs(primes.mean() - 0.15) < 0.02
+    assert all(T.is_smooth13(int(n)) for n, p in zip(ns, primes) if not p)
+    assert ns.min() >= 64 and ns.max() <= (1 << 20) + 100
+    assert abs(np.mean([x[1] is np.float64 for x in w]) - 0.5) < 0.02
+    assert abs(np.mean([x[0] == "r2c" for x in w]) - 0.2) < 0.02
+    # log-uniform: about half the lengths below the geometric midpoint 2^13
+    assert abs(np.mean(ns < 8192) - 0.5) < 0.03
+
+
+def test_mlp_restatement_gradient_by_finite_differences():
+    from oracle import mlp_oracle as M
+    rng = np.random.default_rng(3)
+    D = 5
+    _, total = M.layout(D)
+    p = rng.standard_normal(total) * 0.3
+    X = rng.standard_normal((7, D))
+    y = rng.standard_normal(7)
+    _, g = M.loss_and_grad(p, X, y)
+    for i in rng.choice(total, 40, replace=False):
+        e = np.zeros(total)
+        e[i] = 1e-6
+        num = (M.loss_and_grad(p + e, X, y)[0] - M.loss_and_grad(p - e, X, y)[0]) / 2e-6
+        assert abs(num - g[i]) <= 1e-6 + 1e-5 * abs(num), i
