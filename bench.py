@@ -374,6 +374,239 @@ def run_ours(args):
         pg.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# the uneven batched workload (`--workload uneven`)
+
+UNEVEN_COUNT = 10000
+UNEVEN_METRIC = "uneven batch GFLOP/s (5N·log2N complex, 2.5N·log2N real)"
+
+
+def uneven_items(count):
+    from fftj import tune
+    items = tune.uneven_workload(count, seed=5)
+    items.append(("r2c3d", np.float32, (256, 256, 256)))
+    return items
+
+
+def uneven_flops(kind, n):
+    nn = int(np.prod(n)) if isinstance(n, tuple) else n
+    return (2.5 if kind.startswith("r2c") else 5.0) * nn * math.log2(nn)
+
+
+def learned_planner_report():
+    """Train the cost model with the library's CUDA kernels on the committed
+    GB300 timing set and score its choices on the held-out lengths."""
+    from fftj import tune
+    path = os.path.join(ROOT, "tests", "golden", "tune_gb300.npz")
+    if not os.path.exists(path):
+        return None
+    z = np.load(path)
+    ds = {k: z[k] for k in z.files}
+    t0 = time.perf_counter()
+    feats = np.zeros((len(ds["ms"]), tune.NFEATURES), dtype=np.float32)
+    for q in np.unique(ds["qid"]):
+        sel = np.nonzero(ds["qid"] == q)[0]
+        kind = {0: "c2c", 1: "r2c", 2: "c2r"}[int(ds["kind"][sel[0]])]
+        dt = np.float64 if ds["f64"][sel[0]] else np.float32
+        tq = tune.query(kind, dt, int(ds["n"][sel[0]]), batch=int(ds["batch"][sel[0]]))
+        feats[sel] = tune.features(tq, [tuple(int(v) for v in o) for o in ds["opts"][sel]])
+    ds["feat"] = feats
+    t_feat = time.perf_counter() - t0
+    held_in = np.unique(ds["qid"][ds["split"] == 0])
+    held_out = np.unique(ds["qid"][ds["split"] == 1])
+    tr = np.isin(ds["qid"], held_in) & np.isfinite(ds["ms"])
+    model = tune.CostModel(seed=3)
+    t0 = time.perf_counter()
+    loss = model.fit(ds["feat"][tr], ds["ms"][tr])
+    t_train = time.perf_counter() - t0
+    learned = tune.regrets(ds, held_out, lambda f, o: int(np.argmin(model.predict_log_ms(f))))
+    default = tune.regrets(ds, held_out, lambda f, o: int(np.nonzero((o == 0).all(1))[0][0]))
+    held_in_r = tune.regrets(ds, held_in, lambda f, o: int(np.argmin(model.predict_log_ms(f))))
+    # planning cost: exhaustive timing of every candidate vs scoring them
+    qs = held_out[:20]
+    t_model = t_exh = 0.0
+    for q in qs:
+        sel = np.nonzero(ds["qid"] == q)[0]
+        kind = {0: "c2c", 1: "r2c", 2: "c2r"}[int(ds["kind"][sel[0]])]
+        dt = np.float64 if ds["f64"][sel[0]] else np.float32
+        tq = tune.query(kind, dt, int(ds["n"][sel[0]]), batch=int(ds["batch"][sel[0]]))
+        t0 = time.perf_counter()
+        model.choose(tq, fallback=False)
+        t_model += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        tune.autotune(tq)
+        t_exh += time.perf_counter() - t0
+    return {
+        "held_in_problems": int(held_in.size), "held_out_problems": int(held_out.size),
+        "timed_schedules": int(len(ds["ms"])),
+        "mlp": "28 -> 64 -> 64 -> 1 ReLU FP32, Adam, trained by the library's CUDA kernels",
+        "train_seconds": round(t_train, 2), "final_loss": round(float(loss), 4),
+        "regret_learned_mean": round(float(learned.mean()), 4),
+        "regret_learned_p90": round(float(np.quantile(learned, 0.9)), 4),
+        "regret_learned_max": round(float(learned.max()), 4),
+        "regret_default_mean": round(float(default.mean()), 4),
+        "regret_default_p90": round(float(np.quantile(default, 0.9)), 4),
+        "regret_learned_held_in_mean": round(float(held_in_r.mean()), 4),
+        "within_10pct_of_best": round(float(np.mean(learned <= 1.10)), 4),
+        "planning_ms_model": round(1e3 * t_model / len(qs), 2),
+        "planning_ms_exhaustive": round(1e3 * t_exh / len(qs), 2),
+        "feature_seconds": round(t_feat, 2),
+    }
+
+
+def run_uneven(args):
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+
+    import fftj
+
+    world, rank, local = dist_setup()
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU (there is no CPU path)")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    fftj.build()
+    items = uneven_items(args.count)
+    t0 = time.perf_counter()
+
+    def mk(it):
+        kind, dt, n = it
+        if kind == "r2c3d":
+            # column-major dims, as FFTJ's plan_rfft(x) of a 256^3 array
+            return fftj.Plan(dt, n, kind="r2c", opts={"threads_max": 256})
+        return fftj.Plan(dt, (n,), kind=kind, opts={"threads_max": 256})
+
+    with ThreadPoolExecutor(16) as ex:
+        plans = list(ex.map(mk, items))
+    t_plan = time.perf_counter() - t0
+    # inputs and outputs live in two contiguous arenas (one copy each way e2e)
+    def nbytes(spec):
+        shape, dt = spec
+        return int(np.prod(shape)) * torch.empty((), dtype=dt).element_size()
+
+    def arena(specs):
+        offs, off = [], 0
+        for sp in specs:
+            offs.append(off)
+            off += (nbytes(sp) + 255) // 256 * 256
+        buf = torch.empty(off, dtype=torch.uint8, device=dev)
+        views = [buf[o:o + nbytes(sp)].view(sp[1]).view(sp[0]) for o, sp in zip(offs, specs)]
+        return buf, views
+
+    in_buf, xs = arena([p.in_spec() for p in plans])
+    out_buf, ys = arena([p.out_spec() for p in plans])
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0xF17)
+    for x in xs:
+        x.copy_(torch.randn(x.shape, dtype=x.dtype, device=dev, generator=gen))
+    step_flops = sum(uneven_flops(k, n) for k, _, n in items)
+    groups = {}
+    for mode in ("persistent", "graph", "stream"):
+        groups[mode] = fftj.Group(plans, xs, ys, mode=mode)
+    stream = torch.cuda.current_stream(dev)
+
+    def time_mode(g, steps):
+        for _ in range(max(args.warmup, 3)):
+            g()
+        g.status()
+        torch.cuda.synchronize(dev)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            g()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        g.status()
+        return a.elapsed_time(b) / steps
+
+    modes = {}
+    with ClockSampler(local) as clk:
+        for mode in ("persistent", "graph", "stream"):
+            ms = time_mode(groups[mode], args.steps)
+            inf = groups[mode].info
+            modes[mode] = {"ms": round(ms, 3), "gflops": round(step_flops / (ms * 1e-3) / 1e9, 1),
+                           "kernels_per_step": int(inf.kernels)}
+            if mode == "persistent":
+                modes[mode].update({"ctas": int(inf.ctas), "queue_items": int(inf.nitems),
+                                    "smem_bytes": int(inf.smem_bytes)})
+            if mode == "graph":
+                modes[mode]["branches"] = int(inf.branches)
+    ms = modes["persistent"]["ms"]
+    value = step_flops * world / (ms * 1e-3) / 1e9
+
+    # outputs of the persistent form against numpy (a sample of transforms)
+    groups["persistent"]()
+    groups["persistent"].status()
+    rng = np.random.default_rng(3)
+    check = sorted(set(rng.choice(len(items) - 1, 40, replace=False).tolist()) | {len(items) - 1})
+    worst = {}
+    for i in check:
+        kind, dt, n = items[i]
+        x = xs[i].cpu().numpy()
+        if kind == "c2c":
+            ref = np.fft.fft(x.astype(np.complex128))
+        elif kind == "r2c":
+            ref = np.fft.rfft(x.astype(np.float64))
+        else:
+            ref = np.fft.rfftn(x.astype(np.float64))
+        got = ys[i].cpu().numpy()
+        err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        key = "%s_%s" % (kind, np.dtype(dt).name)
+        worst[key] = max(worst.get(key, 0.0), err)
+
+    # e2e: inputs copied in from pinned host memory, the group run, outputs
+    # copied back, every step
+    h_in = torch.empty(in_buf.numel(), dtype=torch.uint8, pin_memory=True)
+    h_in.copy_(in_buf)
+    h_out = torch.empty(out_buf.numel(), dtype=torch.uint8, pin_memory=True)
+    g = groups["persistent"]
+    for _ in range(2):
+        in_buf.copy_(h_in, non_blocking=True)
+        g()
+        h_out.copy_(out_buf, non_blocking=True)
+    torch.cuda.synchronize(dev)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    e2e_steps = max(3, min(args.steps, 5))
+    a.record(stream)
+    for _ in range(e2e_steps):
+        in_buf.copy_(h_in, non_blocking=True)
+        g()
+        h_out.copy_(out_buf, non_blocking=True)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    g.status()
+    e2e_ms = a.elapsed_time(b) / e2e_steps
+    e2e_ok = torch.equal(h_out, out_buf.cpu())
+
+    learned = learned_planner_report() if not args.no_learned else None
+    nprime = sum(1 for k, _, n in items[:-1] if not isinstance(n, tuple) and fftj.tune.is_prime(n))
+    if rank == 0:
+        out = {
+            "metric": UNEVEN_METRIC, "value": round(value, 1), "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic: iid standard normal (seeded torch generator)",
+            "config": {
+                "workload": "%d transforms, N log-uniform on [64, 2^20] (%d prime, the rest snapped up to "
+                            "13-smooth), half C64, a fifth real-input rfft, plus one F32 256^3 rfft"
+                            % (len(items) - 1, nprime),
+                "plans_seconds": round(t_plan, 1), "plans": len(plans),
+                "input_gb": round(in_buf.numel() / 1e9, 2), "output_gb": round(out_buf.numel() / 1e9, 2),
+                "l2": "inputs larger than L2 (%.1f GB)" % (in_buf.numel() / 1e9),
+                "modes": modes, "rel_l2_vs_fp64_worst": {k: float("%.3g" % v) for k, v in worst.items()},
+                "learned_planner": learned},
+            "e2e": {"value": round(step_flops / (e2e_ms * 1e-3) / 1e9, 1), "unit": "GFLOP/s",
+                    "h2d_bytes_per_step": int(in_buf.numel()), "d2h_bytes_per_step": int(out_buf.numel()),
+                    "ms_per_step": round(e2e_ms, 3), "outputs_checked": bool(e2e_ok),
+                    "schedule": "one H2D copy of the input arena, the persistent group, one D2H copy"},
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -383,6 +616,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--only", default=None,
                     help="run one part only, e.g. c32:262144 (profiling a single plan)")
+    ap.add_argument("--workload", default="mixed", choices=["mixed", "uneven"],
+                    help="mixed: the mixed-radix/prime batch (default); uneven: 10,000 uneven transforms "
+                         "as one group, plus the learned planner's regret")
+    ap.add_argument("--count", type=int, default=UNEVEN_COUNT, help="transforms of the uneven workload")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned planner report")
     args = ap.parse_args()
     if args.only:
         dt, n = args.only.split(":")
@@ -391,6 +629,8 @@ def main():
         STEP_FLOPS = sum(flops(nn, BATCH) for _, nn in PARTS)
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "uneven":
+        run_uneven(args)
     else:
         run_ours(args)
 

@@ -441,6 +441,22 @@ i64 largest_divisor_le(i64 n, i64 cap) {
   return 1;
 }
 
+// Fewest threads per tile column a pass of radix R needs: every sub-stage's
+// butterflies fit the per-thread register budget (max(1, 16/r) butterflies,
+// <= 16 elements per thread).
+i64 min_threads_per_column(i64 R) {
+  int subs[kMaxSub + 4];
+  const int ns = sub_radices(R, subs, kMaxSub + 4);
+  i64 tf = (R + 15) / 16;
+  for (int i = 0; i < ns; ++i) {
+    const int r = subs[i];
+    if (r <= 1) continue;
+    const i64 cap = std::max(1, 16 / r);
+    tf = std::max(tf, (R / r + cap - 1) / cap);
+  }
+  return tf;
+}
+
 // Passes of a length-n axis: one pass when the whole transform fits a tile
 // and the axis is contiguous; otherwise the fewest passes whose radices keep
 // >= min_run contiguous elements per tile row. Heap-free; returns the pass
@@ -456,12 +472,16 @@ int pass_radices(i64 n, bool f64, bool strided, i64* Rs, int cap) {
   // one pass holds the whole transform in a tile of <= 16 elements per thread
   const i64 one_cap = std::min<i64>(cfg.tile_cap, 16 * (i64)cfg.threads_max);
   int k = 0;
-  if ((!strided && n <= one_cap) || n <= cfg.rmax_multi) {
+  if (((!strided && n <= one_cap) || n <= cfg.rmax_multi) && min_threads_per_column(n) <= cfg.threads_max) {
     Rs[0] = n;
     k = 1;
   } else {
-    for (int kk = 1; kk <= cap && kk < 16 && !k; ++kk)
-      if (split_bins(primes, np, kk, cfg.rmax_multi, Rs)) k = kk;
+    for (int kk = 1; kk <= cap && kk < 16 && !k; ++kk) {
+      if (!split_bins(primes, np, kk, cfg.rmax_multi, Rs)) continue;
+      bool fits = true;
+      for (int i = 0; i < kk; ++i) fits = fits && min_threads_per_column(Rs[i]) <= cfg.threads_max;
+      if (fits) k = kk;
+    }
     if (!k) return 0;
   }
   // schedule options: more passes than the fewest, then a permutation

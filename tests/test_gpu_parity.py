@@ -411,3 +411,20 @@ def test_resample_routes(fftj):
     assert fftj.plan_fft(np.float64, 10006).route == "ResamplePlan"
     assert fftj.plan_fft(np.float32, 10007).route == "ResamplePlan"
     assert fftj.plan_fft(np.float64, 997).route == "ResamplePlan"
+
+
+@pytest.mark.parametrize("T", T_LIST)
+@pytest.mark.parametrize("n", [3969, 6864, 3696, 7150, 3549, 6237, 9 * 11 * 13 * 7])
+def test_odd_radix_lengths_that_need_two_passes(fftj, orc, T, n):
+    """Lengths whose odd radices need more threads per column than one CTA
+    has (e.g. 3969 = 3^4 7^2) run as two passes; forward, inverse and the
+    oracle agree."""
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((2, n)) + 1j * rng.standard_normal((2, n))
+    y = host(fftj.plan_fft(T, n, batch=2)(dev(x, T)))
+    ref = np.fft.fft(x, axis=-1)
+    assert rel_l2(y, ref) <= parity_tol(T, n), (n, rel_l2(y, ref) / EPS[T])
+    yo = orc.Plan1D(T, n, "fft")(x[0])
+    assert rel_l2(y[0], yo) <= parity_tol(T, n)
+    xi = host(fftj.plan_ifft(T, n, batch=2)(dev(y, T)))
+    assert rel_l2(xi, x) <= 2 * parity_tol(T, n)

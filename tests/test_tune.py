@@ -99,3 +99,21 @@ def test_mlp_restatement_gradient_by_finite_differences():
         e[i] = 1e-6
         num = (M.loss_and_grad(p + e, X, y)[0] - M.loss_and_grad(p - e, X, y)[0]) / 2e-6
         assert abs(num - g[i]) <= 1e-6 + 1e-5 * abs(num), i
+
+
+def test_every_smooth_length_plans_by_default(T):
+    """Every 13-smooth length up to 2^20 has a default schedule (c2c and r2c,
+    both dtypes, with and without the 256-thread cap of persistent groups).
+    Lengths such as 3969 = 3^4 7^2 once failed: their single pass needed more
+    threads per column than a CTA may have, so they now take two passes."""
+    smooth = [n for n in range(2, (1 << 20) + 1) if T.is_smooth13(n)]
+    assert len(smooth) == 4166
+    for dt in (np.float32, np.float64):
+        for tmax in (0, 256):
+            for n in smooth:
+                T.plan_info(T.query("c2c", dt, n), (0, 0, 0, 0, 0, tmax))
+            for n in smooth[::7]:
+                if n % 2 == 0:
+                    T.plan_info(T.query("r2c", dt, n), (0, 0, 0, 0, 0, tmax))
+    inf = T.plan_info(T.query("c2c", np.float64, 3969))
+    assert inf.npasses == 2
