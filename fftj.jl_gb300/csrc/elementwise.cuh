@@ -150,7 +150,7 @@ __device__ __forceinline__ void copy_at(const CopyParams& cp, const void* __rest
     const Cx<T> a = ldd<CG>(X + j);
     Cx<T> bb = ldd<CG>(X + (h - j));
     bb.y = -bb.y;
-    const T pre = (T)cp.pre;
+    const T pre = half_or_one<T>(cp.pre);  // 1/2 (irfft) or 1 (brfft)
     const T xer = (a.x + bb.x) * pre, xei = (a.y + bb.y) * pre;
     const T xdr = (a.x - bb.x) * pre, xdi = (a.y - bb.y) * pre;
     const Cx<T> w = reinterpret_cast<const Cx<T>*>(cp.tab)[j];

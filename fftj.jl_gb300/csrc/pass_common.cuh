@@ -49,6 +49,15 @@ __device__ __forceinline__ V ldd(const V* p) {
   else return __ldg(p);
 }
 
+// Predicates and factors from double kernel parameters, formed with integer
+// operations on the double's bits. A floating compare or conversion of a
+// double parameter that the compiler re-evaluates per element (it does, to
+// spare predicate registers) runs on the FP64 pipe, 1/64 of the FP32 rate on
+// GB300: in an F32 pass that kept the FP64 pipe 47% busy.
+__device__ __forceinline__ bool not_one(double x) { return __double_as_longlong(x) != 0x3FF0000000000000ll; }
+template <typename T>
+__device__ __forceinline__ T half_or_one(double x) { return not_one(x) ? (T)0.5 : (T)1; }
+
 // Shared-memory padding: one element per 16 (8-byte) or 8 (16-byte) elements,
 // so power-of-two strides spread over the banks.
 template <typename T>
@@ -299,7 +308,7 @@ __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in,
     const Cx<T> a = ldd<CG>(X + g);
     Cx<T> bb = ldd<CG>(X + (h - g));
     bb.y = -bb.y;
-    const T pre = (T)pp.ld_pre;
+    const T pre = half_or_one<T>(pp.ld_pre);  // 1/2 (irfft) or 1 (brfft)
     const Cx<T> xe = mk<T>((a.x + bb.x) * pre, (a.y + bb.y) * pre);
     const Cx<T> xd = mk<T>((a.x - bb.x) * pre, (a.y - bb.y) * pre);
     const Cx<T> w = __ldg(reinterpret_cast<const Cx<T>*>(pp.ld_tab) + g);
@@ -515,7 +524,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
 
   // ---- store: shared -> HBM with the outer twiddle w_ncur^(p*j) and scale.
   // The twiddle loads of all of a thread's elements are issued first.
-  const bool scaled = pp.scale != 1.0;
+  const bool scaled = not_one(pp.scale);
   const T sc = (T)pp.scale;
   const bool tw = pp.tw_mode != 0;
   Cx<T> w[EPT];
@@ -616,7 +625,7 @@ __device__ __forceinline__ Cx<T> load_elem_off(const PassParams& pp, const void*
     const Cx<T> a = __ldg(X + g);
     Cx<T> bb = __ldg(X + (h - g));
     bb.y = -bb.y;
-    const T pre = (T)pp.ld_pre;
+    const T pre = half_or_one<T>(pp.ld_pre);  // 1/2 (irfft) or 1 (brfft)
     const Cx<T> xe = mk<T>((a.x + bb.x) * pre, (a.y + bb.y) * pre);
     const Cx<T> xd = mk<T>((a.x - bb.x) * pre, (a.y - bb.y) * pre);
     const Cx<T> w = __ldg(reinterpret_cast<const Cx<T>*>(pp.ld_tab) + g);
@@ -770,9 +779,39 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
     }
   }
 
-  const bool scaled = pp.scale != 1.0;
+  const bool scaled = not_one(pp.scale);
   const T sc = (T)pp.scale;
   const bool tw = pp.tw_mode != 0;
+  if constexpr (MODE == 1 && sizeof(T) == 4) {
+    if (tw && R % nthr == 0) {
+      // ---- row store with outer twiddles, thread tid owning outputs
+      // j = tid + jj*nthr of every column c of the tile. Along c the twiddle
+      // w^((p0+c) j) advances by w^j: one complex multiply per element
+      // instead of a table lookup, re-seeded exactly every 8 columns (at most
+      // 7 steps of rounding). F32 only: F64 passes are FP64-pipe bound and
+      // the lookup costs them nothing while the multiply does.
+      if (b0 < pp.nbatch) {
+        Cx<T>* ob = out + b0 * pp.out_bstride + (int64_t)R * p0 + tid;
+        for (int j0 = 0; j0 < R; j0 += nthr) {
+          const uint32_t j = (uint32_t)(tid + j0);
+          const Cx<T> step = j ? outer_tw<T>(pp, j) : mk<T>(1, 0);
+          uint32_t e = (uint32_t)p0 * j;
+          Cx<T> w = mk<T>(1, 0);
+          const int a0 = (int)j * NB;
+#pragma unroll 8
+          for (int c = 0; c < NB; ++c) {
+            if ((c & 7) == 0) w = e ? outer_tw<T>(pp, e) : mk<T>(1, 0);
+            Cx<T> v = cmul(buf[pidx<T>(a0 + c)], w);
+            if (scaled) { v.x *= sc; v.y *= sc; }
+            ob[(int64_t)c * R + j0] = v;
+            w = cmul(w, step);
+            e += j;
+          }
+        }
+      }
+      return;
+    }
+  }
   if constexpr (MODE <= 1) {
     // ---- row store (lanes walk j): outputs contiguous along j (s == 1)
     const int dc = nthr / R, dj = nthr - (nthr / R) * R;
