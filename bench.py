@@ -607,6 +607,146 @@ def run_uneven(args):
         print(json.dumps(out))
 
 
+# ---------------------------------------------------------------------------
+# the other configurations of the transform path (`--workload configs`)
+
+CONFIG_CASES = [
+    # (label, kind, dtype, dims (column-major), batch, inputs)
+    ("c64_2^16_x64", "c2c", np.float64, (1 << 16,), 64, "uniform"),
+    ("c32_2^26", "c2c", np.float32, (1 << 26,), 1, "uniform"),
+    ("c64_2^24", "c2c", np.float64, (1 << 24,), 1, "uniform"),
+    ("rfft_f32_2^25_x4", "r2c", np.float32, (1 << 25,), 4, "uniform"),
+    ("irfft_f32_2^25_x4", "c2r", np.float32, (1 << 25,), 4, "uniform"),
+    ("c32_2^20_x64_stress", "c2c", np.float32, (1 << 20,), 64, "stress"),
+    ("c32_4096x4096_stress", "c2c", np.float32, (4096, 4096), 1, "stress"),
+    ("rfft_f32_256^3", "r2c", np.float32, (256, 256, 256), 1, "normal"),
+]
+
+
+def run_configs(args):
+    import torch
+
+    import fftj
+
+    world, rank, local = dist_setup()
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU (there is no CPU path)")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    fftj.build()
+    peak, peak_kind = measured_peaks()
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0xF17)
+    stream = torch.cuda.current_stream(dev)
+    results = {}
+    with ClockSampler(local) as clk:
+        for label, kind, dt, dims, batch, data in CONFIG_CASES:
+            p = fftj.Plan(dt, dims, kind=kind, batch=batch, direction=-1 if kind != "c2r" else 1)
+            shape, tdt = p.in_spec()
+            if data == "uniform":
+                if tdt.is_complex:
+                    x = torch.complex(torch.rand(shape, generator=gen, device=dev, dtype=_RDT(tdt)) * 2 - 1,
+                                      torch.rand(shape, generator=gen, device=dev, dtype=_RDT(tdt)) * 2 - 1)
+                else:
+                    x = torch.rand(shape, generator=gen, device=dev, dtype=tdt) * 2 - 1
+            else:
+                x = torch.randn(shape, generator=gen, device=dev, dtype=tdt)
+                if data == "stress":  # 1% of the entries (seeded choice) x 1e3
+                    flat = x.view(-1)
+                    idx = torch.randperm(flat.numel(), generator=gen, device=dev)[: flat.numel() // 100]
+                    flat[idx] *= 1e3
+            if kind == "c2r":  # a spectrum of real data: DC and Nyquist bins real
+                x[..., 0].imag.zero_()
+                x[..., -1].imag.zero_()
+            oshape, odt = p.out_spec()
+            y = torch.empty(oshape, dtype=odt, device=dev)
+            for _ in range(max(args.warmup, 3)):
+                p(y, x)
+            torch.cuda.synchronize(dev)
+            steps = max(3, min(args.steps, 20))
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(steps):
+                p(y, x)
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            ms = a.elapsed_time(b) / steps
+            n = int(np.prod(dims))
+            fl = (2.5 if kind != "c2c" else 5.0) * n * math.log2(n) * batch
+            io_bytes = x.numel() * x.element_size() + y.numel() * y.element_size()
+            inf = p.info
+            op_ms = p.profile_ops(y, x, reps=5)
+            esz = 16 if dt == np.float64 else 8
+            cplx = n * batch if kind == "c2c" else (n // dims[0]) * (dims[0] // 2) * batch
+            pass_bytes = 2.0 * cplx * esz   # one read + one write of the complex data
+            passes = [{"ms": round(t, 4), "gbs": round(pass_bytes / (t * 1e-3) / 1e9, 1),
+                       "frac": round(pass_bytes / (t * 1e-3) / 1e9 / peak, 3)} for t in op_ms]
+            res = {"ms": round(ms, 4), "gflops": round(fl / (ms * 1e-3) / 1e9, 1),
+                   "alg_gbs": round(io_bytes / (ms * 1e-3) / 1e9, 1), "route": p.route,
+                   "pass_radix": [int(v) for v in inf.pass_radix[:inf.npasses]],
+                   "ops": passes, "specialized_passes": int(inf.specialized_passes)}
+            # accuracy against FP64 (numpy): sampled rows, or the whole array
+            xs = x.cpu().numpy()
+            ys = y.cpu().numpy()
+            if kind == "c2c" and len(dims) == 1:
+                rows = [0, batch - 1] if batch > 1 else None
+                xr = xs[rows] if rows else xs
+                yr = ys[rows] if rows else ys
+                if n <= (1 << 22):
+                    ref = np.fft.fft(xr.astype(np.complex128), axis=-1)
+                    res["rel_l2_vs_fp64"] = float("%.3g" % (np.linalg.norm(yr - ref) / np.linalg.norm(ref)))
+                else:  # long single transforms: Parseval
+                    px = np.sum(np.abs(xr.astype(np.complex128)) ** 2) * n
+                    py = np.sum(np.abs(yr.astype(np.complex128)) ** 2)
+                    res["parseval_rel"] = float("%.3g" % (abs(py - px) / px))
+            elif kind == "c2c":
+                ref = np.fft.fftn(xs.astype(np.complex128))
+                res["rel_l2_vs_fp64"] = float("%.3g" % (np.linalg.norm(ys - ref) / np.linalg.norm(ref)))
+            elif kind == "r2c" and len(dims) == 3:
+                ref = np.fft.rfftn(xs.astype(np.float64))
+                res["rel_l2_vs_fp64"] = float("%.3g" % (np.linalg.norm(ys - ref) / np.linalg.norm(ref)))
+            elif kind == "r2c":
+                ref = np.fft.rfft(xs[:1].astype(np.float64), axis=-1)
+                res["rel_l2_vs_fp64"] = float("%.3g" % (np.linalg.norm(ys[:1] - ref) / np.linalg.norm(ref)))
+            else:
+                ref = np.fft.irfft(xs[:1].astype(np.complex128), n=n, axis=-1)
+                res["rel_l2_vs_fp64"] = float("%.3g" % (np.linalg.norm(ys[:1] - ref) / np.linalg.norm(ref)))
+            results[label] = res
+            del x, y, p
+            torch.cuda.empty_cache()
+    cpu = None
+    if not args.no_cpu:
+        # the FFTJ-restated CPU plan on the host cores for the C64 2^16 x64 case
+        from oracle import oracle as O
+        O.build()
+        nt = O.max_threads()
+        po = O.Plan1D(np.float64, 1 << 16, "fft", nthreads=nt)
+        rng = np.random.default_rng(0xF17)
+        xb = rng.uniform(-1, 1, (64, 1 << 16)) + 1j * rng.uniform(-1, 1, (64, 1 << 16))
+        po(xb[:2])
+        t0 = time.perf_counter()
+        po(xb)
+        dt_cpu = time.perf_counter() - t0
+        fl = 5.0 * (1 << 16) * 16 * 64
+        cpu = {"value": round(fl / dt_cpu / 1e9, 2), "unit": "GFLOP/s", "cores": nt, "kind": "port",
+               "sample": "C64 2^16 x64 (FFTJ-restated C++ plans, %d threads)" % nt}
+    if rank == 0:
+        out = {"metric": "per-configuration GFLOP/s and per-pass HBM GB/s", "unit": "GFLOP/s",
+               "n_gpus": world, "dtype": "f32+f64", "data": "synthetic (seeded torch generator)",
+               "peak_hbm_gbs": peak, "peak_source": peak_kind,
+               "config": {"note": "per-pass GB/s = one read + one write of the complex data / op time "
+                                  "(CUDA events between the plan's launches); real transforms count 2.5 N log2 N",
+                          "cases": results},
+               "cpu_baseline": cpu, "clocks": clk.summary()}
+        print(json.dumps(out))
+
+
+def _RDT(ct):
+    import torch
+    return {torch.complex64: torch.float32, torch.complex128: torch.float64}[ct]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -616,7 +756,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--only", default=None,
                     help="run one part only, e.g. c32:262144 (profiling a single plan)")
-    ap.add_argument("--workload", default="mixed", choices=["mixed", "uneven"],
+    ap.add_argument("--workload", default="mixed", choices=["mixed", "uneven", "configs"],
                     help="mixed: the mixed-radix/prime batch (default); uneven: 10,000 uneven transforms "
                          "as one group, plus the learned planner's regret")
     ap.add_argument("--count", type=int, default=UNEVEN_COUNT, help="transforms of the uneven workload")
@@ -631,6 +771,8 @@ def main():
         run_reference(args)
     elif args.workload == "uneven":
         run_uneven(args)
+    elif args.workload == "configs":
+        run_configs(args)
     else:
         run_ours(args)
 

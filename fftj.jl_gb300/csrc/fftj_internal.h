@@ -170,6 +170,7 @@ int pass_geometry(PassParams& pp, bool f64, int64_t R, int64_t m, int64_t s, int
                   int64_t ibs, int64_t obs);
 void outer_twiddle_layout(PassParams& pp, bool f64);
 const void* pick_pass_kernel(bool f64, int dir, const PassParams& pp);
+bool stage_inner_twiddles(const PassParams& pp, bool recipe);
 void set_error(const char* msg);
 
 template <typename T>

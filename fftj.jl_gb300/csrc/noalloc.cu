@@ -144,7 +144,7 @@ static int run_noalloc(int64_t n, int64_t batch, int dir, double scale, const vo
   for (int i = 0; i < npass; ++i) {
     void* dst = (i + 1 == npass) ? d_out : (void*)data;
     const void* fn = pick_pass_kernel(f64, dir, pp[i]);
-    pp[i].smem_tw_elems = fn ? pp[i].R : 0;
+    pp[i].smem_tw_elems = stage_inner_twiddles(pp[i], fn != nullptr) ? pp[i].R : 0;
     if (prepare_pass<T>(pp[i], dir, fn) != cudaSuccess ||
         launch_pass<T>(pp[i], dir, fn, src, dst, st) != cudaSuccess) {
       set_error("fftj_execute_noalloc_c2c: pass launch failed");

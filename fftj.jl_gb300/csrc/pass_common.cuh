@@ -697,12 +697,16 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
   // the pass's inner twiddles w_R^t are staged in shared memory right after
   // the tile (smem_elems), so sub-stages read them with 32-bit shared
   // addresses: no per-element global index arithmetic
-  Cx<T>* twS = buf + pp.smem_elems;
-  {
-    const Cx<T>* twG = reinterpret_cast<const Cx<T>*>(pp.twR) + tid;
+  // (large tables -- R beyond the planner's staging limit -- are read from
+  // global memory instead, where they stay L1/L2-resident: staging them
+  // would copy as many bytes per tile as the tile's data)
+  const Cx<T>* twR = reinterpret_cast<const Cx<T>*>(pp.twR);
+  if (pp.smem_tw_elems >= R) {
+    Cx<T>* twS = buf + pp.smem_elems;
+    const Cx<T>* twG = twR + tid;
     for (int t = tid; t < R; t += nthr, twG += nthr) twS[t] = __ldg(twG);
+    twR = twS;
   }
-  const Cx<T>* twR = twS;
 
   if constexpr (MODE == 0) {
     // ---- row load (lanes walk j): e = tid + i*nthr -> (c, j), c = column
@@ -860,6 +864,13 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
     if (colok) {
       Cx<T>* ob = out + batch * pp.out_bstride + (int64_t)R * pp.s * pcol + q0 + ql;
       const int64_t jstep = (int64_t)S * pp.s;
+      const uint32_t estep = (uint32_t)pcol * (uint32_t)S;
+      // F32: along a butterfly's outputs the outer twiddle w^(pcol (k + j S))
+      // advances by w^(pcol S), one complex multiply per output instead of a
+      // table lookup (at most rL - 1 <= 15 steps of rounding). F64 passes are
+      // FP64-pipe bound and keep the lookups.
+      constexpr bool kRecur = sizeof(T) == 4;
+      const Cx<T> wstep = (kRecur && tw && estep != 0) ? outer_tw<T>(pp, estep) : mk<T>(1, 0);
 #pragma unroll
       for (int i = 0; i < IPT; ++i) {
         const int k = kg + i * TF;
@@ -867,11 +878,18 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
           Dft<T, DIR, rL>::run(v[i]);
           Cx<T>* o = ob + (int64_t)k * pp.s;
           uint32_t e = (uint32_t)pcol * (uint32_t)k;
-          const uint32_t estep = (uint32_t)pcol * (uint32_t)S;
+          Cx<T> w = (kRecur && tw && e != 0) ? outer_tw<T>(pp, e) : mk<T>(1, 0);
 #pragma unroll
           for (int j = 0; j < rL; ++j) {
             Cx<T> x = v[i][j];
-            if (tw && e != 0) x = cmul(x, outer_tw<T>(pp, e));
+            if (kRecur) {
+              if (tw) {
+                x = cmul(x, w);
+                w = cmul(w, wstep);
+              }
+            } else if (tw && e != 0) {
+              x = cmul(x, outer_tw<T>(pp, e));
+            }
             if (scaled) { x.x *= sc; x.y *= sc; }
             *o = x;
             o += jstep;

@@ -655,6 +655,12 @@ const void* pick_pass_kernel(bool f64, int dir, const PassParams& pp) {
   return f64 ? pick_pass_kernel_t<double>(dir, pp) : pick_pass_kernel_t<float>(dir, pp);
 }
 
+// Recipe kernels stage the pass's inner twiddles w_R^t in shared memory
+// when the table is small next to the tile; beyond kStageTwiddleMax entries
+// they read it from global memory (L1/L2-resident).
+constexpr int kStageTwiddleMax = 1024;
+bool stage_inner_twiddles(const PassParams& pp, bool recipe) { return recipe && pp.R <= kStageTwiddleMax; }
+
 void set_error(const char* msg) { g_err = msg; }
 
 }  // namespace fftj
@@ -1211,7 +1217,7 @@ int finalize_passes(fftj_plan_s* P) {
   for (auto& op : P->ops) {
     if (op.kind != OP_PASS) continue;
     op.kfn = pick_pass_kernel(sizeof(T) == 8, op.dir, op.pp);
-    op.pp.smem_tw_elems = op.kfn ? op.pp.R : 0;
+    op.pp.smem_tw_elems = stage_inner_twiddles(op.pp, op.kfn != nullptr) ? op.pp.R : 0;
     if (P->dry) continue;
     if (prepare_pass<T>(op.pp, op.dir, op.kfn) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
   }
@@ -1359,6 +1365,32 @@ int fftj_plan_c2r_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, i
   return FFTJ_OK;
 }
 
+// Launch op i of a plan (src/dst resolved from the plan's buffer ids).
+static cudaError_t launch_op(fftj_plan_s* P, size_t i, void* const* bufs, bool via_ws, cudaStream_t st) {
+  const Op& op = P->ops[i];
+  const void* src = bufs[op.src];
+  void* dst = via_ws ? P->ws[0].p : bufs[op.dst];
+  cudaError_t e = cudaSuccess;
+  if (P->dtype == FFTJ_F32) {
+    switch (op.kind) {
+      case OP_PASS: e = launch_pass<float>(op.pp, op.dir, op.kfn, src, dst, st); break;
+      case OP_INTERP: e = launch_interp<float>(op.ip, src, dst, st); break;
+      case OP_RPOST: e = launch_real_post<float>(op.rp, src, dst, st); break;
+      case OP_COPY: e = launch_copy<float>(op.cp, src, dst, st); break;
+      case OP_SOLVE: e = launch_solve<float>(op.sv, src, dst, st); break;
+    }
+  } else {
+    switch (op.kind) {
+      case OP_PASS: e = launch_pass<double>(op.pp, op.dir, op.kfn, src, dst, st); break;
+      case OP_INTERP: e = launch_interp<double>(op.ip, src, dst, st); break;
+      case OP_RPOST: e = launch_real_post<double>(op.rp, src, dst, st); break;
+      case OP_COPY: e = launch_copy<double>(op.cp, src, dst, st); break;
+      case OP_SOLVE: e = launch_solve<double>(op.sv, src, dst, st); break;
+    }
+  }
+  return e;
+}
+
 int fftj_execute(fftj_plan plan, const void* d_in, void* d_out, void* stream) {
   if (!plan) return fail(FFTJ_ERR_ARG, "null plan");
   if (!d_in || !d_out) return fail(FFTJ_ERR_ARG, "null data pointer");
@@ -1368,33 +1400,46 @@ int fftj_execute(fftj_plan plan, const void* d_in, void* d_out, void* stream) {
   void* bufs[4] = {const_cast<void*>(d_in), d_out, P->ws[0].p, P->ws[1].p};
   const bool via_ws = P->ops.size() == 1 && !P->inplace_safe && d_in == d_out;
   for (size_t i = 0; i < P->ops.size(); ++i) {
-    const Op& op = P->ops[i];
-    const void* src = bufs[op.src];
-    void* dst = via_ws ? P->ws[0].p : bufs[op.dst];
-    cudaError_t e = cudaSuccess;
-    if (P->dtype == FFTJ_F32) {
-      switch (op.kind) {
-        case OP_PASS: e = launch_pass<float>(op.pp, op.dir, op.kfn, src, dst, st); break;
-        case OP_INTERP: e = launch_interp<float>(op.ip, src, dst, st); break;
-        case OP_RPOST: e = launch_real_post<float>(op.rp, src, dst, st); break;
-        case OP_COPY: e = launch_copy<float>(op.cp, src, dst, st); break;
-        case OP_SOLVE: e = launch_solve<float>(op.sv, src, dst, st); break;
-      }
-    } else {
-      switch (op.kind) {
-        case OP_PASS: e = launch_pass<double>(op.pp, op.dir, op.kfn, src, dst, st); break;
-        case OP_INTERP: e = launch_interp<double>(op.ip, src, dst, st); break;
-        case OP_RPOST: e = launch_real_post<double>(op.rp, src, dst, st); break;
-        case OP_COPY: e = launch_copy<double>(op.cp, src, dst, st); break;
-        case OP_SOLVE: e = launch_solve<double>(op.sv, src, dst, st); break;
-      }
-    }
+    const cudaError_t e = launch_op(P, i, bufs, via_ws, st);
     if (e != cudaSuccess) return fail(FFTJ_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
   }
   if (via_ws) {
     cudaError_t e = cudaMemcpyAsync(d_out, P->ws[0].p, P->ops[0].dst_bytes, cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return fail(FFTJ_ERR_CUDA, std::string("copy failed: ") + cudaGetErrorString(e));
   }
+  g_err.clear();
+  return FFTJ_OK;
+}
+
+int fftj_profile_ops(fftj_plan plan, const void* d_in, void* d_out, void* stream, int reps, float* ms, int cap) {
+  if (!plan || !d_in || !d_out || !ms || reps < 1) return fail(FFTJ_ERR_ARG, "null argument or reps < 1");
+  if (plan->dry) return fail(FFTJ_ERR_ARG, "a dry plan cannot execute");
+  if (d_in == d_out) return fail(FFTJ_ERR_ARG, "profiling needs distinct input and output buffers");
+  fftj_plan_s* P = plan;
+  const size_t k = P->ops.size();
+  if ((size_t)cap < k) return fail(FFTJ_ERR_ARG, "cap smaller than the plan's op count");
+  cudaStream_t st = (cudaStream_t)stream;
+  void* bufs[4] = {const_cast<void*>(d_in), d_out, P->ws[0].p, P->ws[1].p};
+  std::vector<cudaEvent_t> ev(k + 1);
+  for (auto& e : ev) cudaEventCreate(&e);
+  std::vector<double> acc(k, 0.0);
+  int rc = FFTJ_OK;
+  for (int r = 0; r < reps && rc == FFTJ_OK; ++r) {
+    cudaEventRecord(ev[0], st);
+    for (size_t i = 0; i < k && rc == FFTJ_OK; ++i) {
+      if (launch_op(P, i, bufs, false, st) != cudaSuccess) rc = fail(FFTJ_ERR_CUDA, "kernel launch failed");
+      cudaEventRecord(ev[i + 1], st);
+    }
+    if (rc == FFTJ_OK && cudaEventSynchronize(ev[k]) != cudaSuccess) rc = fail(FFTJ_ERR_CUDA, "execution failed");
+    for (size_t i = 0; i < k && rc == FFTJ_OK; ++i) {
+      float t = 0;
+      cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+      acc[i] += t;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (rc) return rc;
+  for (size_t i = 0; i < k; ++i) ms[i] = (float)(acc[i] / reps);
   g_err.clear();
   return FFTJ_OK;
 }

@@ -90,7 +90,7 @@ EXPORTS = [
     "fftj_mlp_create", "fftj_mlp_destroy", "fftj_mlp_num_params", "fftj_mlp_get_params",
     "fftj_mlp_set_params", "fftj_mlp_grad", "fftj_mlp_train", "fftj_mlp_predict",
     "fftj_group_create", "fftj_group_execute", "fftj_group_status", "fftj_group_get_info",
-    "fftj_group_set_wait_limit", "fftj_group_debug_stall", "fftj_group_destroy",
+    "fftj_group_set_wait_limit", "fftj_group_debug_stall", "fftj_group_destroy", "fftj_profile_ops",
 ]
 
 
@@ -143,6 +143,7 @@ def lib():
         L.fftj_group_set_wait_limit.argtypes = [vp, ctypes.c_uint32]
         L.fftj_group_debug_stall.argtypes = [vp, i32]
         L.fftj_group_destroy.argtypes = [vp]
+        L.fftj_profile_ops.argtypes = [vp, vp, vp, vp, i32, PF, i32]
         L.fftj_last_error_string.restype = ctypes.c_char_p
         L.fftj_version.restype = ctypes.c_char_p
         for name in EXPORTS:
@@ -273,6 +274,17 @@ class Plan:
 
     def __mul__(self, x):
         return self(x)
+
+    def profile_ops(self, y, x, reps=10):
+        """Mean milliseconds of each op (pass / elementwise kernel) of the plan."""
+        self._validate(x, self.in_spec(), "input")
+        self._validate(y, self.out_spec(), "output")
+        k = int(self.info.nops)
+        ms = (ctypes.c_float * k)()
+        stream = torch.cuda.current_stream(x.device).cuda_stream
+        _check(lib().fftj_profile_ops(self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                      ctypes.c_void_p(stream), int(reps), ms, k))
+        return list(ms)
 
     def __del__(self):
         h = getattr(self, "_h", None)

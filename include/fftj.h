@@ -200,6 +200,15 @@ int fftj_plan_c2r(fftj_plan* out, int dtype, int rank, const int64_t* dims, int6
  */
 int fftj_execute(fftj_plan plan, const void* d_in, void* d_out, void* stream);
 
+/*
+ * Time each op (pass or elementwise kernel) of a plan: `reps` executions on
+ * `stream`, CUDA events between consecutive ops; ms[i] = mean milliseconds
+ * of op i (cap >= the plan's op count, fftj_plan_info_t.nops). No
+ * counterpart in the reference (a measurement aid: per-pass HBM rates).
+ * Needs d_in != d_out.
+ */
+int fftj_profile_ops(fftj_plan plan, const void* d_in, void* d_out, void* stream, int reps, float* ms, int cap);
+
 /* Size and algorithm of a plan (FFTJ: size(p) and the plan type). */
 int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info);
 
