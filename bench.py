@@ -641,6 +641,8 @@ def run_configs(args):
     results = {}
     with ClockSampler(local) as clk:
         for label, kind, dt, dims, batch, data in CONFIG_CASES:
+            if args.case and label not in args.case.split(","):
+                continue
             p = fftj.Plan(dt, dims, kind=kind, batch=batch, direction=-1 if kind != "c2r" else 1)
             shape, tdt = p.in_spec()
             if data == "uniform":
@@ -761,6 +763,7 @@ def main():
                          "as one group, plus the learned planner's regret")
     ap.add_argument("--count", type=int, default=UNEVEN_COUNT, help="transforms of the uneven workload")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned planner report")
+    ap.add_argument("--case", default=None, help="configs workload: only these cases (comma-separated labels)")
     args = ap.parse_args()
     if args.only:
         dt, n = args.only.split(":")

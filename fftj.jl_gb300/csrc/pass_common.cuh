@@ -363,10 +363,17 @@ struct Recipe {
 };
 
 // compile-time sub-stage: the maps of substage<> with constant r, S, R/r, Tf
+// Padded index of x + j*J: when J is a multiple of the padding period,
+// pidx(x + j J) = pidx(x) + j (J + J / period), so a butterfly's accesses are
+// one base index plus constant steps (no per-access shift and add).
+template <typename T>
+__host__ __device__ constexpr int pad_period() { return sizeof(T) == 4 ? 16 : 8; }
+
 template <typename T, int DIR, int r, int S, int Rr, int TF>
 __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b, const int kg, const int NB,
                                             const Cx<T>* __restrict__ twR) {
   constexpr int IPT = (Rr + TF - 1) / TF;
+  constexpr int PP = pad_period<T>();
   const int jstride_in = Rr * NB;
   const int jstride_out = S * NB;
   Cx<T> v[IPT][r];
@@ -375,8 +382,14 @@ __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b
     const int k = kg + i * TF;
     if ((i + 1) * TF <= Rr || k < Rr) {
       const int a = k * NB + b;
+      if constexpr (Rr % PP == 0) {
+        const int base = pidx<T>(a), step = jstride_in + jstride_in / PP;
 #pragma unroll
-      for (int j = 0; j < r; ++j) v[i][j] = buf[pidx<T>(a + j * jstride_in)];
+        for (int j = 0; j < r; ++j) v[i][j] = buf[base + j * step];
+      } else {
+#pragma unroll
+        for (int j = 0; j < r; ++j) v[i][j] = buf[pidx<T>(a + j * jstride_in)];
+      }
     }
   }
   __syncthreads();
@@ -388,20 +401,26 @@ __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b
       const int q = k - p * S;
       Dft<T, DIR, r>::run(v[i]);
       const int a = (r * S * p + q) * NB + b;
-      buf[pidx<T>(a)] = v[i][0];
+      const int base = pidx<T>(a);
+      const int step = (S % PP == 0) ? jstride_out + jstride_out / PP : 0;
+      // position of output j: a constant step when S is a multiple of the
+      // padding period, else the padded index of a + j * S * NB
+#define FFTJ_OUT_AT(j) ((S % PP == 0) ? base + (j) * step : pidx<T>(a + (j) * jstride_out))
+      buf[base] = v[i][0];
       if (Rr == S) {
         // last sub-stage of the pass (L = r): no twiddle
 #pragma unroll
-        for (int j = 1; j < r; ++j) buf[pidx<T>(a + j * jstride_out)] = v[i][j];
+        for (int j = 1; j < r; ++j) buf[FFTJ_OUT_AT(j)] = v[i][j];
       } else {
         const int tstep = p * S;
 #pragma unroll
         for (int j = 1; j < r; ++j) {
           Cx<T> w = v[i][j];
           if (p != 0) w = cmul(w, twR[j * tstep]);
-          buf[pidx<T>(a + j * jstride_out)] = w;
+          buf[FFTJ_OUT_AT(j)] = w;
         }
       }
+#undef FFTJ_OUT_AT
     }
   }
   __syncthreads();
