@@ -113,6 +113,20 @@ def dist_setup():
     return world, rank, local
 
 
+def replica_reduce(ms, units, pg=None, device="cpu"):
+    """Whole-job view of a replicated workload (each rank runs its own copy,
+    no collective on the data path): the job took the slowest rank's time and
+    processed every rank's units. Returns (max ms, summed units)."""
+    if pg is None:
+        return float(ms), float(units)
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    pg.all_reduce(u, op=pg.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
 # ---------------------------------------------------------------------------
 # reference arm: FFTJ's algorithm on the host cores (oracle restatement)
 
@@ -222,12 +236,8 @@ def run_ours(args):
             step()
         e1.record(stream)
         barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    if pg is not None:
-        t = torch.tensor([ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
-    value = STEP_FLOPS * world / (ms * 1e-3) / 1e9
+    ms, job_flops = replica_reduce(e0.elapsed_time(e1) / args.steps, STEP_FLOPS, pg, dev)
+    value = job_flops / (ms * 1e-3) / 1e9
 
     # ---- per-part breakdown and the dominant kernel's roofline (live, CUDA
     # events on the launching stream)
@@ -327,12 +337,8 @@ def run_ours(args):
         stream.wait_event(e)
     b.record(stream)
     barrier()
-    e2e_ms = a.elapsed_time(b) / e2e_steps
-    if pg is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = STEP_FLOPS * world / (e2e_ms * 1e-3) / 1e9
+    e2e_ms, job_flops = replica_reduce(a.elapsed_time(b) / e2e_steps, STEP_FLOPS, pg, dev)
+    e2e_value = job_flops / (e2e_ms * 1e-3) / 1e9
     # the last step's spectra arrived on the host intact
     e2e_ok = all(torch.equal(h, y.cpu()) for h, y in zip(hy, ys))
 
