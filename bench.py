@@ -624,7 +624,11 @@ CONFIG_CASES = [
     ("rfft_f32_2^25_x4", "r2c", np.float32, (1 << 25,), 4, "uniform"),
     ("irfft_f32_2^25_x4", "c2r", np.float32, (1 << 25,), 4, "uniform"),
     ("c32_2^20_x64_stress", "c2c", np.float32, (1 << 20,), 64, "stress"),
+    ("c32_2^20_x64_stress_fp16split", "c2c", np.float32, (1 << 20,), 64, "stress", 1),
+    ("c32_2^20_x64_stress_bf16split", "c2c", np.float32, (1 << 20,), 64, "stress", 2),
     ("c32_4096x4096_stress", "c2c", np.float32, (4096, 4096), 1, "stress"),
+    ("c32_4096x4096_stress_fp16split", "c2c", np.float32, (4096, 4096), 1, "stress", 1),
+    ("c32_4096x4096_stress_bf16split", "c2c", np.float32, (4096, 4096), 1, "stress", 2),
     ("rfft_f32_256^3", "r2c", np.float32, (256, 256, 256), 1, "normal"),
 ]
 
@@ -646,10 +650,13 @@ def run_configs(args):
     stream = torch.cuda.current_stream(dev)
     results = {}
     with ClockSampler(local) as clk:
-        for label, kind, dt, dims, batch, data in CONFIG_CASES:
+        for case in CONFIG_CASES:
+            label, kind, dt, dims, batch, data = case[:6]
+            precision = case[6] if len(case) > 6 else 0
             if args.case and label not in args.case.split(","):
                 continue
-            p = fftj.Plan(dt, dims, kind=kind, batch=batch, direction=-1 if kind != "c2r" else 1)
+            p = fftj.Plan(dt, dims, kind=kind, batch=batch, direction=-1 if kind != "c2r" else 1,
+                          opts={"precision": precision})
             shape, tdt = p.in_spec()
             if data == "uniform":
                 if tdt.is_complex:
@@ -693,7 +700,9 @@ def run_configs(args):
             res = {"ms": round(ms, 4), "gflops": round(fl / (ms * 1e-3) / 1e9, 1),
                    "alg_gbs": round(io_bytes / (ms * 1e-3) / 1e9, 1), "route": p.route,
                    "pass_radix": [int(v) for v in inf.pass_radix[:inf.npasses]],
-                   "ops": passes, "specialized_passes": int(inf.specialized_passes)}
+                   "ops": passes, "specialized_passes": int(inf.specialized_passes),
+                   "precision": ["fp32", "fp16 hi+lo tensor-core radix-16", "bf16 hi+lo tensor-core radix-16"][precision],
+                   "tc_substages": int(inf.tc_substages)}
             # accuracy against FP64 (numpy): sampled rows, or the whole array
             xs = x.cpu().numpy()
             ys = y.cpu().numpy()

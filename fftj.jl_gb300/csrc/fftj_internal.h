@@ -73,6 +73,7 @@ struct PassParams {
   double scale;            // applied on store when != 1
   int smem_elems;          // padded elements per buffer
   int smem_tw_elems;       // extra shared elements (recipe kernels stage w_R^t there)
+  int tc;                  // radix-16 sub-stages on tensor cores: 0 off, 1 FP16 hi+lo, 2 BF16 hi+lo (F32)
   int threads;
   int Tf;                  // threads per tile column (threads = NB * Tf)
   int ept;                 // elements per thread per column (ceil(R / Tf))
@@ -159,6 +160,7 @@ struct SchedOpts {
   int tf_mult = 0;
   int route = 0;
   int threads_max = 0;
+  int precision = 0;
   bool dry = false;
 };
 extern thread_local SchedOpts g_sched;
@@ -171,6 +173,8 @@ int pass_geometry(PassParams& pp, bool f64, int64_t R, int64_t m, int64_t s, int
 void outer_twiddle_layout(PassParams& pp, bool f64);
 const void* pick_pass_kernel(bool f64, int dir, const PassParams& pp);
 bool stage_inner_twiddles(const PassParams& pp, bool recipe);
+bool tc16_substage_fits(const PassParams& pp, int i);
+bool has_tc16_substage(const PassParams& pp);
 void set_error(const char* msg);
 
 template <typename T>

@@ -285,10 +285,14 @@ int build_persistent(fftj_group_s* g) {
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
     return gfail(FFTJ_ERR_CUDA, "persistent group: device query failed");
-  if (g->smem + sizeof(GroupOp) + 64 > (size_t)optin)
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, (const void*)k_group) != cudaSuccess)
+    return gfail(FFTJ_ERR_CUDA, "persistent group: kernel attribute query failed");
+  const int maxdyn = optin - (int)fa.sharedSizeBytes;
+  if (maxdyn <= 0 || g->smem > (size_t)maxdyn)
     return gfail(FFTJ_ERR_UNSUPPORTED, "persistent group: a pass tile exceeds shared memory");
-  if (cudaFuncSetAttribute((const void*)k_group, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           optin - (int)sizeof(GroupOp) - 64) != cudaSuccess ||
+  if (cudaFuncSetAttribute((const void*)k_group, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) !=
+          cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_group, kGroupThreads, g->smem) != cudaSuccess ||
       per_sm < 1)
     return gfail(FFTJ_ERR_CUDA, "persistent group: kernel configuration failed");

@@ -79,10 +79,16 @@ cudaError_t prepare_pass(const PassParams& pp, int dir, const void* fn) {
   if (e != cudaSuccess) return e;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const size_t need = (size_t)(pp.smem_elems + pp.smem_tw_elems) * sizeof(Cx<T>);
-  if (need > (size_t)optin) return cudaErrorInvalidValue;
   const void* f = fn ? fn : (const void*)pass_fn<T>(dir, pp.load_op);
-  return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  // the dynamic limit is what the device allows per block minus the
+  // kernel's own static shared memory
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, f);
+  if (e != cudaSuccess) return e;
+  const int maxdyn = optin - (int)fa.sharedSizeBytes;
+  const size_t need = (size_t)(pp.smem_elems + pp.smem_tw_elems) * sizeof(Cx<T>);
+  if (maxdyn <= 0 || need > (size_t)maxdyn) return cudaErrorInvalidValue;
+  return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn);
 }
 
 template <typename T>

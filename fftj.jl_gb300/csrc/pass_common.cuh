@@ -1,6 +1,8 @@
 // Device building blocks of the pass kernels, shared by kernels.cu (the
 // generic pass) and recipes.cu (passes specialised at compile time).
 #pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "bfly_consts.h"
@@ -439,6 +441,187 @@ __device__ __forceinline__ void run_recipe(Recipe<Rs...>*, Cx<T>* buf, const int
 }
 
 // ---------------------------------------------------------------------------
+// Precision form of a radix-16 sub-stage (F32 passes, plan option
+// precision = 1 FP16 / 2 BF16): the 16-point DFTs of the whole tile as one
+// GEMM on the tensor cores. In real form a butterfly's outputs are
+// [Yr; Yi] = [[Cr, -Ci], [Ci, Cr]] [Xr; Xi] (32 x 32 times 32 x 1); a warp
+// multiplies it into n-tiles of 8 butterflies with mma.sync m16n8k16
+// (half-precision operands, FP32 accumulation). Operands are split into a
+// hi half and a lo half scaled up by 2^11 (FP16) or 2^8 (BF16) so that it
+// never goes subnormal; A_hi B_hi accumulates in one accumulator and
+// A_hi B_lo + A_lo B_hi in another, which is scaled back down (the lo*lo
+// product is dropped). Each butterfly (a GEMM column) is scaled by its own
+// power of two so that its largest input is below 1 (FP16 range) and
+// unscaled on the way out. Outputs get the sub-stage's twiddles in FP32 and
+// go to the same places as the FP32 sub-stage's.
+template <int KIND>  // 1: FP16 operands, 2: BF16 operands
+__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint32_t* b) {
+  if constexpr (KIND == 1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+  } else {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+  }
+}
+
+// lo halves are stored multiplied by kLoScale (2^mantissa bits of the half
+// type), so they stay normal numbers
+template <int KIND>
+__host__ __device__ constexpr float lo_scale() { return KIND == 1 ? 2048.f : 256.f; }
+
+// (x, y) -> packed hi halves and packed scaled lo halves
+template <int KIND>
+__device__ __forceinline__ void split_pair(float x, float y, uint32_t& hi, uint32_t& lo) {
+  constexpr float L = lo_scale<KIND>();
+  if constexpr (KIND == 1) {
+    const __half2 h = __floats2half2_rn(x, y);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn((x - hf.x) * L, (y - hf.y) * L);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+  } else {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x, y);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn((x - hf.x) * L, (y - hf.y) * L);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+  }
+}
+
+// Whether the tensor-core sub-stage applies: whole warps, butterflies in
+// n-tiles of 8, at most 4 n-tiles per warp (EPT <= 16 guarantees it).
+__device__ __forceinline__ bool tc16_fits(int nthr, int NB, int Rr) {
+  const int nbf = NB * Rr;
+  return (nthr & 31) == 0 && (nbf & 7) == 0 && (nbf >> 3) <= 4 * (nthr >> 5);
+}
+
+template <int DIR, int KIND>
+__device__ __noinline__ void substage_tc16(float2* __restrict__ buf, const int tid, const int nthr, const int NB,
+                                           const int Rr, const int S, const FastDiv fS, const FastDiv fNB,
+                                           const float2* __restrict__ twR) {
+  const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
+  const bool active = tid < nthr;
+  const int ntiles = (NB * Rr) >> 3;
+  const int g = lane >> 2, j0 = (lane & 3) * 2;
+  const int jstride = Rr * NB;
+  // ---- inputs X[j0], X[j0+1], X[j0+8], X[j0+9] of butterfly 8 tile + g
+  float xr[4][4], xi[4][4];
+  int ex[4];  // exponent of each n-tile's butterfly g: |x| < 2^ex
+#pragma unroll
+  for (int it = 0; it < 4; ++it) {
+    const int tile = warp + it * nwarps;
+    float mx = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      xr[it][q] = 0.f;
+      xi[it][q] = 0.f;
+    }
+    if (active && tile < ntiles) {
+      const int u = tile * 8 + g;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = j0 + (q & 1) + (q >> 1) * 8;
+        const float2 v = buf[pidx<float>(u + j * jstride)];
+        xr[it][q] = v.x;
+        xi[it][q] = v.y;
+        mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+      }
+    }
+    // the four lanes 4g .. 4g+3 hold butterfly g's 16 inputs
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
+    ex[it] = 0;
+    if (mx > 0.f) frexpf(mx, &ex[it]);
+  }
+  __syncthreads();  // every input is in registers before any output is written
+  // ---- DFT matrix fragments (row block mt: 0 = Yr, 1 = Yi; column block
+  // kt: 0 = Xr, 1 = Xi), split into hi and scaled lo
+  // A thread's entries are w_16^(row col) for row in {g, g+8} and col in
+  // {j0, j0+1, j0+8, j0+9}: two roots w_16^(g j0), w_16^(g (j0+1)) and sign
+  // flips, since w_16^8 = -1 and (g + 8 dr)(c + 8 dc) = g c + 8 (dr c + dc g)
+  // modulo 16.
+  float wc[2], ws[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    float sn, cs;
+    sincospif((float)((g * (j0 + h)) & 15) * 0.125f, &sn, &cs);
+    wc[h] = cs;
+    ws[h] = DIR * sn;
+  }
+  uint32_t ahi[2][2][4], alo[2][2][4];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt)
+#pragma unroll
+      for (int rg = 0; rg < 4; ++rg) {
+        // register rg holds elements (row, col) and (row, col + 1),
+        // row = g + 8 dr, col = j0 + 8 dc
+        const int dr = rg & 1, dc = rg >> 1;
+        float val[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const float sg = ((dr * (j0 + h) + dc * g) & 1) ? -1.f : 1.f;
+          const float cr = sg * wc[h], ci = sg * ws[h];
+          val[h] = mt == 0 ? (kt == 0 ? cr : -ci) : (kt == 0 ? ci : cr);
+        }
+        split_pair<KIND>(val[0], val[1], ahi[mt][kt][rg], alo[mt][kt][rg]);
+      }
+  constexpr float kInvLo = 1.f / lo_scale<KIND>();
+  // ---- products and outputs
+#pragma unroll
+  for (int it = 0; it < 4; ++it) {
+    const int tile = warp + it * nwarps;
+    if (!active || tile >= ntiles) continue;  // warp-uniform
+    const float scale = ldexpf(1.f, -ex[it]);
+    uint32_t bhi[2][2], blo[2][2];
+    split_pair<KIND>(xr[it][0] * scale, xr[it][1] * scale, bhi[0][0], blo[0][0]);
+    split_pair<KIND>(xr[it][2] * scale, xr[it][3] * scale, bhi[0][1], blo[0][1]);
+    split_pair<KIND>(xi[it][0] * scale, xi[it][1] * scale, bhi[1][0], blo[1][0]);
+    split_pair<KIND>(xi[it][2] * scale, xi[it][3] * scale, bhi[1][1], blo[1][1]);
+    float acc[2][4], accl[2][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[mt][c] = accl[mt][c] = 0.f;
+#pragma unroll
+      for (int kt = 0; kt < 2; ++kt) {
+        mma16816<KIND>(acc[mt], ahi[mt][kt], bhi[kt]);
+        mma16816<KIND>(accl[mt], ahi[mt][kt], blo[kt]);
+        mma16816<KIND>(accl[mt], alo[mt][kt], bhi[kt]);
+      }
+    }
+    // the unscale exponents of the output butterflies j0 and j0 + 1 live in
+    // lanes 4 j0 and 4 (j0 + 1)
+    const int e0 = __shfl_sync(0xffffffffu, ex[it], j0 * 4);
+    const int e1 = __shfl_sync(0xffffffffu, ex[it], j0 * 4 + 4);
+    // accumulator c holds output row g + 8 (c >> 1) of butterfly
+    // 8 tile + j0 + (c & 1)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int m = g + (c >> 1) * 8;
+      const int u = tile * 8 + j0 + (c & 1);
+      const int k = (int)fNB.div((uint32_t)u);
+      const int bcol = u - k * NB;
+      const int p = (int)fS.div((uint32_t)k);
+      const int q = k - p * S;
+      const float un = ldexpf(1.f, (c & 1) ? e1 : e0);
+      float2 y = make_float2(fmaf(accl[0][c], kInvLo, acc[0][c]) * un, fmaf(accl[1][c], kInvLo, acc[1][c]) * un);
+      if (p != 0 && m != 0) y = cmul(y, twR[m * p * S]);
+      buf[pidx<float>((16 * S * p + m * S + q) * NB + bcol)] = y;
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
 // One Stockham pass over one tile (the kernel comment in kernels.cu gives
 // the maps). Rec is RuntimeRecipe (radix sequence read from pp.sub) or a
 // Recipe<r...> fixed at compile time.
@@ -535,7 +718,18 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
         case 8: substage<T, DIR, 8>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
         case 11: substage<T, DIR, 11>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
         case 13: substage<T, DIR, 13>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
-        case 16: substage<T, DIR, 16>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
+        case 16:
+          if constexpr (sizeof(T) == 4) {
+            if (pp.tc && tc16_fits(nthr, NB, ss.Rr)) {
+              if (pp.tc == 1)
+                substage_tc16<DIR, 1>(buf, tid, nthr, NB, ss.Rr, ss.S, ss.fS, pp.fNB, twR);
+              else
+                substage_tc16<DIR, 2>(buf, tid, nthr, NB, ss.Rr, ss.S, ss.fS, pp.fNB, twR);
+              break;
+            }
+          }
+          substage<T, DIR, 16>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR);
+          break;
         default: break;
       }
     }

@@ -655,6 +655,19 @@ const void* pick_pass_kernel(bool f64, int dir, const PassParams& pp) {
   return f64 ? pick_pass_kernel_t<double>(dir, pp) : pick_pass_kernel_t<float>(dir, pp);
 }
 
+// Sub-stage i of a pass runs on the tensor cores in the precision form (the
+// host copy of the device condition tc16_fits: whole warps, butterflies in
+// n-tiles of 8, at most 4 n-tiles per warp).
+bool tc16_substage_fits(const PassParams& pp, int i) {
+  const int nbf = pp.NB * pp.sub[i].Rr;
+  return pp.sub[i].r == 16 && pp.threads % 32 == 0 && nbf % 8 == 0 && nbf / 8 <= 4 * (pp.threads / 32);
+}
+bool has_tc16_substage(const PassParams& pp) {
+  for (int i = 0; i < pp.nsub; ++i)
+    if (tc16_substage_fits(pp, i)) return true;
+  return false;
+}
+
 // Recipe kernels stage the pass's inner twiddles w_R^t in shared memory
 // when the table is small next to the tile; beyond kStageTwiddleMax entries
 // they read it from global memory (L1/L2-resident).
@@ -760,6 +773,7 @@ int build_axis_passes(fftj_plan_s* P, i64 n, i64 Bi, i64 nbatch, i64 ibs, i64 ob
     }
     pp.scale = (pi + 1 == Rs.size()) ? scale : 1.0;
     pp.load_op = LOAD_PLAIN;
+    pp.tc = f64 ? 0 : g_sched.precision;
     op.dst_bytes = (size_t)(nbatch * obs) * sizeof(T) * 2;
     out_ops->push_back(op);
     P->pass_R.push_back((int)R);
@@ -1216,7 +1230,10 @@ template <typename T>
 int finalize_passes(fftj_plan_s* P) {
   for (auto& op : P->ops) {
     if (op.kind != OP_PASS) continue;
-    op.kfn = pick_pass_kernel(sizeof(T) == 8, op.dir, op.pp);
+    // the precision form's tensor-core sub-stage lives in the run-time
+    // kernel; passes without a radix-16 sub-stage keep their recipe kernel
+    if (op.pp.tc && !has_tc16_substage(op.pp)) op.pp.tc = 0;
+    op.kfn = op.pp.tc ? nullptr : pick_pass_kernel(sizeof(T) == 8, op.dir, op.pp);
     op.pp.smem_tw_elems = stage_inner_twiddles(op.pp, op.kfn != nullptr) ? op.pp.R : 0;
     if (P->dry) continue;
     if (prepare_pass<T>(op.pp, op.dir, op.kfn) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
@@ -1251,6 +1268,7 @@ struct SchedScope {
     g_sched.route = o->route;
     g_sched.threads_max = o->threads_max;
     g_sched.dry = o->dry != 0;
+    g_sched.precision = (o->precision >= 0 && o->precision <= 2) ? o->precision : 0;
   }
   ~SchedScope() { g_sched = SchedOpts(); }
 };
@@ -1475,6 +1493,8 @@ int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info) {
     if (op.kind == OP_PASS) {
       const PassParams& pp = op.pp;
       if (op.kfn) info->specialized_passes++;
+      if (pp.tc)
+        for (int i = 0; i < pp.nsub; ++i) info->tc_substages += tc16_substage_fits(pp, i) ? 1 : 0;
       if (pi < 8) {
         info->pass_tile[pi] = pp.NB * pp.R;
         info->pass_threads[pi] = pp.threads;
@@ -1482,7 +1502,7 @@ int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info) {
       }
       pi++;
       for (int64_t v : {(int64_t)pp.R, (int64_t)pp.P, (int64_t)pp.Q, (int64_t)pp.NBt, (int64_t)pp.Tf,
-                        (int64_t)pp.threads, (int64_t)pp.nsub, (int64_t)pp.tw_mode, (int64_t)pp.load_op,
+                        (int64_t)pp.threads, (int64_t)pp.nsub, (int64_t)pp.tw_mode, (int64_t)pp.load_op, (int64_t)pp.tc,
                         (int64_t)(uintptr_t)op.kfn})
         mix(v);
       for (int i = 0; i < pp.nsub; ++i) mix(pp.sub[i].r);

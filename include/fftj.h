@@ -71,6 +71,7 @@ typedef struct {
   int64_t pass_ctas[8];   /* CTAs (tiles) of each pass */
   int nops;               /* kernel launches per execution (passes + elementwise ops) */
   int dry;                /* 1: planned without tables or workspace (cannot execute) */
+  int tc_substages;       /* radix-16 sub-stages run on tensor cores (opts.precision != 0) */
 } fftj_plan_info_t;
 
 /*
@@ -89,7 +90,8 @@ typedef struct {
   int32_t route;         /* non-smooth lengths: 0 planner, 1 resampling, 2 Gaussian (HvdH) */
   int32_t threads_max;   /* cap on threads per CTA (0 = 512 F32 / 256 F64) */
   int32_t dry;           /* 1: plan the schedule only (no tables, no workspace, cannot execute) */
-  int32_t reserved;
+  int32_t precision;     /* F32 radix-16 sub-stages: 0 FP32 butterflies, 1 FP16 hi+lo tensor-core GEMM,
+                            2 BF16 hi+lo tensor-core GEMM (FP32 accumulation, FP32 twiddles) */
 } fftj_plan_opts_t;
 
 int fftj_plan_c2c_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch,
