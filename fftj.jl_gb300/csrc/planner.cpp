@@ -687,6 +687,18 @@ namespace {
 namespace {
 
 // upload a table of complex values (re, im pairs in double) as T
+// Host-built tables of the plan being built on this thread
+// (fftj_plan_c2c_from_tables): the roots w_N^e for e < N, and for a
+// resampled length the deconvolution and interpolation tables. omega_table
+// reads every twiddle table from the roots (n divides N) instead of
+// evaluating sincospi.
+struct HostTables {
+  const double* omega = nullptr;  // 2N values: re, im of w_N^e
+  i64 N = 0;
+  const fftj_resample_tables_t* rs = nullptr;
+};
+thread_local HostTables g_tables;
+
 // stand-in address of a table that a dry plan does not build
 const void* const kDryTable = reinterpret_cast<const void*>(uintptr_t(256));
 
@@ -725,7 +737,17 @@ template <typename T>
 const void* omega_table(fftj_plan_s* P, i64 n, i64 count, i64 stride, int dir) {
   if (g_sched.dry) return kDryTable;
   std::vector<double> ri(2 * count);
-  for (i64 e = 0; e < count; ++e) omega(e * stride, n, dir, &ri[2 * e], &ri[2 * e + 1]);
+  if (g_tables.omega && g_tables.N % n == 0) {
+    // w_n^k = w_N^(k N / n), read from the caller's roots
+    const i64 f = g_tables.N / n;
+    for (i64 e = 0; e < count; ++e) {
+      const i64 k = (i64)(((__int128)e * stride) % n) * f;
+      ri[2 * e] = g_tables.omega[2 * k];
+      ri[2 * e + 1] = g_tables.omega[2 * k + 1];
+    }
+  } else {
+    for (i64 e = 0; e < count; ++e) omega(e * stride, n, dir, &ri[2 * e], &ri[2 * e + 1]);
+  }
   return upload_cplx<T>(P, ri);
 }
 
@@ -892,13 +914,28 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
     return FFTJ_OK;
   }
   // odd non-smooth lengths FFTJ sends to Gaussian resampling (HvdH)
-  const bool hv_ok = g_sched.route == 2 ? (n % 2 == 1 && n >= 64) : (g_sched.route == 0 && use_hvdh(sizeof(T) == 8, n));
+  const bool hv_ok = !g_tables.rs && (g_sched.route == 2 ? (n % 2 == 1 && n >= 64)
+                                                         : (g_sched.route == 0 && use_hvdh(sizeof(T) == 8, n)));
   if (hv_ok) {
     Hvdh hv = hvdh_parts(n, sizeof(T) == 8, scale);
     if (hv.ok) return build_c2c_hvdh<T>(P, hv, batch, idist, odist, dir, ops, route);
   }
-  // non-smooth: resample onto m (src/resample.jl:258-276)
-  Resample rs = resample_parts(n, sizeof(T) == 8, scale);
+  // non-smooth: resample onto m (src/resample.jl:258-276), from the caller's
+  // tables when it supplied them
+  Resample rs;
+  if (g_tables.rs) {
+    const fftj_resample_tables_t* t = g_tables.rs;
+    rs.n = n;
+    rs.m = t->m;
+    rs.w = t->w;
+    rs.h = t->w / 2;
+    rs.beta = 0;
+    rs.corr.assign(t->corr, t->corr + n);
+    rs.wt.assign(t->wt, t->wt + n * t->w);
+    rs.l0.assign(t->l0, t->l0 + n);
+  } else {
+    rs = resample_parts(n, sizeof(T) == 8, scale);
+  }
   P->resample_m = rs.m;
   P->resample_w = rs.w;
   std::vector<Op> tmp;
@@ -1407,6 +1444,36 @@ static cudaError_t launch_op(fftj_plan_s* P, size_t i, void* const* bufs, bool v
     }
   }
   return e;
+}
+
+int fftj_plan_c2c_from_tables(fftj_plan* out, int dtype, int64_t n, int64_t batch, int dir, double scale,
+                              const double* omega, int64_t N, const fftj_resample_tables_t* rs) {
+  if (!out) return fail(FFTJ_ERR_ARG, "null plan pointer");
+  *out = nullptr;
+  if (n < 1 || batch < 1) return fail(FFTJ_ERR_ARG, "transform length and batch must be positive");
+  if (dir != -1 && dir != 1) return fail(FFTJ_ERR_ARG, "dir must be -1 or +1");
+  if (!omega) return fail(FFTJ_ERR_ARG, "null root table");
+  std::vector<int> primes;
+  const bool smooth = smooth13(n, &primes);
+  if (smooth) {
+    if (rs) return fail(FFTJ_ERR_ARG, "resampling tables given for a 13-smooth length");
+    if (N != n) return fail(FFTJ_ERR_DIM, "a 13-smooth length takes the roots of w_n (N = n)");
+  } else {
+    if (!rs || !rs->corr || !rs->wt || !rs->l0) return fail(FFTJ_ERR_ARG, "a non-smooth length needs resampling tables");
+    std::vector<int> pm;
+    if (rs->m < n || !smooth13(rs->m, &pm)) return fail(FFTJ_ERR_ARG, "the resampled grid m must be 13-smooth and >= n");
+    if (N != rs->m) return fail(FFTJ_ERR_DIM, "a resampled length takes the roots of w_m (N = m)");
+    if (rs->w < 1 || rs->w > 64) return fail(FFTJ_ERR_ARG, "interpolation taps must be 1..64");
+    for (i64 k = 0; k < n; ++k)
+      if (rs->l0[k] < -rs->m || rs->l0[k] >= rs->m) return fail(FFTJ_ERR_ARG, "l0 entries must lie in [-m, m)");
+  }
+  g_tables.omega = omega;
+  g_tables.N = N;
+  g_tables.rs = rs;
+  // smooth lengths apply the scale in the last pass; resampled ones carry it in corr
+  const int rc = fftj_plan_c2c_ex(out, dtype, 1, &n, batch, 0, 0, dir, smooth ? scale : 1.0, nullptr);
+  g_tables = HostTables();
+  return rc;
 }
 
 int fftj_execute(fftj_plan plan, const void* d_in, void* d_out, void* stream) {

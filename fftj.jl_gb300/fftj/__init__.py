@@ -21,7 +21,7 @@ import torch
 from . import _build
 
 __all__ = [
-    "plan_fft", "plan_ifft", "plan_bfft", "plan_fft_", "plan_ifft_", "plan_bfft_",
+    "plan_fft", "plan_ifft", "plan_bfft", "plan_fft_", "plan_ifft_", "plan_bfft_", "plan_from_tables",
     "plan_rfft", "plan_irfft", "plan_brfft",
     "fft", "ifft", "bfft", "fft_", "ifft_", "bfft_", "rfft", "irfft", "brfft",
     "mul_", "inv", "size", "Plan", "InplacePlan", "Scaled",
@@ -72,6 +72,12 @@ class TuneQuery(ctypes.Structure):
 NFEATURES = 28
 
 
+class ResampleTables(ctypes.Structure):
+    """fftj_resample_tables_t: host-built resampling tables."""
+    _fields_ = [("m", ctypes.c_int64), ("w", ctypes.c_int64), ("corr", ctypes.POINTER(ctypes.c_double)),
+                ("wt", ctypes.POINTER(ctypes.c_double)), ("l0", ctypes.POINTER(ctypes.c_int32))]
+
+
 class GroupInfo(ctypes.Structure):
     """fftj_group_info_t."""
     _fields_ = [(k, ctypes.c_int) for k in
@@ -91,6 +97,7 @@ EXPORTS = [
     "fftj_mlp_set_params", "fftj_mlp_grad", "fftj_mlp_train", "fftj_mlp_predict",
     "fftj_group_create", "fftj_group_execute", "fftj_group_status", "fftj_group_get_info",
     "fftj_group_set_wait_limit", "fftj_group_debug_stall", "fftj_group_destroy", "fftj_profile_ops",
+    "fftj_plan_c2c_from_tables",
 ]
 
 
@@ -144,6 +151,8 @@ def lib():
         L.fftj_group_debug_stall.argtypes = [vp, i32]
         L.fftj_group_destroy.argtypes = [vp]
         L.fftj_profile_ops.argtypes = [vp, vp, vp, vp, i32, PF, i32]
+        L.fftj_plan_c2c_from_tables.argtypes = [ctypes.POINTER(vp), i32, i64, i64, i32, ctypes.c_double, PD,
+                                                i64, ctypes.POINTER(ResampleTables)]
         L.fftj_last_error_string.restype = ctypes.c_char_p
         L.fftj_version.restype = ctypes.c_char_p
         for name in EXPORTS:
@@ -345,6 +354,43 @@ class Group:
         if h is not None and h.value and _lib is not None:
             _lib.fftj_group_destroy(h)
             self._h = None
+
+
+def plan_from_tables(T, n, omega, resample=None, *, batch=1, direction=-1, scale=1.0):
+    """A 1-D complex plan whose device tables all come from the caller:
+    omega = exp(dir 2 pi i e / N), e < N (complex128; N = n for 13-smooth n,
+    else N = resample["m"]), resample = {"m", "w", "corr", "wt", "l0"} for
+    non-smooth n (scale folded into corr). Mirrors how FFTJ's Julia planner
+    would hand its own tables to the library."""
+    om = np.ascontiguousarray(np.asarray(omega, dtype=np.complex128)).view(np.float64)
+    keep = [om]
+    rp = None
+    if resample is not None:
+        corr = np.ascontiguousarray(resample["corr"], dtype=np.float64)
+        wt = np.ascontiguousarray(resample["wt"], dtype=np.float64)
+        l0 = np.ascontiguousarray(resample["l0"], dtype=np.int32)
+        keep += [corr, wt, l0]
+        rt = ResampleTables(int(resample["m"]), int(resample["w"]),
+                            corr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                            wt.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                            l0.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+        rp = ctypes.byref(rt)
+    p = Plan.__new__(Plan)
+    p.dt = _dtcode(T)
+    p.dims = (int(n),)
+    p.kind = "c2c"
+    p.direction = int(direction)
+    p.scale = float(scale)
+    p.batch = int(batch)
+    p.normalized = True
+    p.n = int(n)
+    p.opts = PlanOpts()
+    h = ctypes.c_void_p()
+    _check(lib().fftj_plan_c2c_from_tables(ctypes.byref(h), p.dt, int(n), int(batch), int(direction),
+                                           float(scale), om.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                           om.size // 2, rp))
+    p._h = h
+    return p
 
 
 class InplacePlan:

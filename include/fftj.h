@@ -196,6 +196,29 @@ int fftj_plan_c2r(fftj_plan* out, int dtype, int rank, const int64_t* dims, int6
                   int64_t idist, int64_t odist, int normalized);
 
 /*
+ * Plan from host-built tables: the caller (FFTJ's Julia planner) computes the
+ * twiddles and resampling weights, the library uploads them and derives every
+ * device table from them (no trigonometry of its own). Replaces the table
+ * construction of src/plan.jl:66-95 (make_stage twiddles from sincospi) and
+ * src/resample.jl:202-256 (_resample_parts) for 1-D complex plans.
+ *   omega: 2*N doubles, re/im of exp(dir * 2 pi i e / N) for e < N.
+ *   13-smooth n: N = n, rs = NULL; `scale` multiplies the result.
+ *   otherwise:   resampling with the caller's tables, N = rs->m; the scale
+ *                is folded into rs->corr (as _resample_parts does) and the
+ *                `scale` argument is ignored.
+ */
+typedef struct {
+  int64_t m;           /* resampled grid length: 13-smooth, >= n */
+  int64_t w;           /* interpolation taps per output (1..64) */
+  const double* corr;  /* n deconvolution factors, scale included */
+  const double* wt;    /* n * w interpolation weights */
+  const int32_t* l0;   /* n first grid rows (in [-m, m), wrapping mod m) */
+} fftj_resample_tables_t;
+
+int fftj_plan_c2c_from_tables(fftj_plan* out, int dtype, int64_t n, int64_t batch, int dir, double scale,
+                              const double* omega, int64_t N, const fftj_resample_tables_t* rs);
+
+/*
  * Apply a plan: FFTJ's p(y, x) / mul!(y, p, x) / p * x (src/api.jl:34-55,
  * src/plan.jl:359-396). d_in, d_out: device pointers; stream: a
  * cudaStream_t (NULL = legacy default stream). Asynchronous; no allocation.
