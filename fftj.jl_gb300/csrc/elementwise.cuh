@@ -94,7 +94,11 @@ __device__ __forceinline__ void solve_at(const SolveParams& sp, const Cx<T>* __r
     for (int k = B - 1; k > 0; --k) xp[k] = xp[k - 1];
     xp[0] = x;
     const int32_t o = __ldg(oi + i);
-    if (i < sp.H + sp.L && o >= 0) yb[o] = mk<T>(x.x * sc, x.y * sc);
+    if (i < sp.H + sp.L && o >= 0) {
+      Cx<T> v = mk<T>(x.x * sc, x.y * sc);
+      if (sp.tw) v = cmul(v, __ldg(reinterpret_cast<const Cx<T>*>(sp.tw) + (b % sp.tw_s) * (int64_t)o));
+      yb[o] = v;
+    }
   }
 }
 
@@ -144,6 +148,11 @@ __device__ __forceinline__ void copy_at(const CopyParams& cp, const void* __rest
   } else if (cp.mode == 3) {  // complex copy of the first n entries
     reinterpret_cast<Cx<T>*>(out)[b * cp.out_bstride + j] =
         ldd<CG>(reinterpret_cast<const Cx<T>*>(in) + b * cp.in_bstride + j);
+  } else if (cp.mode == 5) {  // decimation in time (FFTJ _split_gather!, src/composite.jl:245-252)
+    const int64_t sd = cp.nc, pl = cp.n / sd;
+    const int64_t r = j / pl, jj = j - r * pl;
+    reinterpret_cast<Cx<T>*>(out)[b * cp.out_bstride + j] =
+        ldd<CG>(reinterpret_cast<const Cx<T>*>(in) + b * cp.in_bstride + r + sd * jj);
   } else {  // irfft pre-pass (FFTJ src/real.jl:149-192) for a resampled inner transform
     const Cx<T>* X = reinterpret_cast<const Cx<T>*>(in) + b * cp.in_bstride;
     const int64_t h = cp.n;

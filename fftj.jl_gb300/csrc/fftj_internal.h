@@ -100,6 +100,8 @@ struct SolveParams {
   const void* uf;            // nchunk*R*(B+1): 1/U_ii, U_{i,i+1..i+B}
   const int32_t* oi;         // nchunk*R output index (-1: identity row)
   void* zw;                  // R * nbatch * nchunk forward-substitution scratch
+  const void* tw;            // split route: w_(tw_s * n)^(r * o) applied to output o of sub-transform b,
+  int64_t tw_s;              //   r = b mod tw_s (nullptr: none)
 };
 
 // Resampling interpolation: y[b*ody + k] = sum_i wt[k*w+i] g[b*m + (l0[k]+i) mod m]
@@ -121,9 +123,10 @@ struct RealPostParams {
 struct CopyParams {
   int64_t n, nbatch, in_bstride, out_bstride;
   // 0: real -> complex, 1: hermitian expand (n real), 2: complex -> real,
-  // 3: complex copy of n entries, 4: irfft pre-pass Z[k], k < n = h
+  // 3: complex copy of n entries, 4: irfft pre-pass Z[k], k < n = h,
+  // 5: decimation, row r of the output = x[r + s j], j < n / s (s = nc)
   int mode;
-  int64_t nc;          // complex length per batch (mode 1)
+  int64_t nc;          // complex length per batch (mode 1); s (mode 5)
   const void* tab;     // mode 4: e^{+2 pi i k / 2h}
   double pre;          // mode 4: pair factor (1/2 irfft, 1 brfft)
 };

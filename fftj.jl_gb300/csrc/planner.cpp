@@ -895,6 +895,72 @@ int build_c2c_hvdh(fftj_plan_s* P, const Hvdh& hv, i64 batch, i64 idist, i64 odi
   return FFTJ_OK;
 }
 
+// Split route for non-smooth n = s p with s its 7-smooth part and p odd
+// (FFTJ SplitPlan, src/composite.jl:136-301, used here also where FFTJ takes
+// CompositePlan): decimate in time, x_r[j] = x[r + s j]; transform the s
+// sequences of length p by Gaussian resampling (t ~ 1.008 p, instead of the
+// ~2n grid of full-length resampling); multiply output k1 of sequence r by
+// w_n^(r k1) in the banded solve; then length-s transforms along r (stride p)
+// give X[k1 + p k2] in natural order.
+i64 smooth7_part(i64 n) {
+  i64 s = 1;
+  for (int f : {2, 3, 5, 7})
+    while (n % (s * f) == 0) s *= f;
+  return s;
+}
+// FFTJ's thresholds for leaving full-length resampling (src/composite.jl:
+// 34-66, 157-161): a sizable smooth part (s >= 16, n >= 4096 F64 / 32768 F32)
+// with the odd part Gaussian-resampled from p >= 500 (_COMPOSITE_HV_MINP),
+// or a small one (s < 16) for even n >= 16384 F64 / 65536 F32 with an odd
+// part FFTJ would route to HvdH. Odd n reach this only below the HvdH
+// threshold (full-length HvdH is taken first on the GPU).
+bool use_split(bool f64, i64 n) {
+  const i64 s = smooth7_part(n), p = n / s;
+  if (s < 2 || p % 2 == 0) return false;
+  if (g_sched.route == 2) return p >= 64;
+  if (g_sched.route != 0) return false;
+  if (s >= 16) return n >= (f64 ? 4096 : 32768) && p >= 500;
+  return n % 2 == 0 && use_hvdh(f64, p) && n >= (f64 ? 16384 : 65536);
+}
+
+template <typename T>
+int build_c2c_split(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir, double scale,
+                    std::vector<Op>* ops, int* route) {
+  const i64 s = smooth7_part(n), p = n / s;
+  Hvdh hv = hvdh_parts(p, sizeof(T) == 8, 1.0);
+  if (!hv.ok) return fail(FFTJ_ERR_UNSUPPORTED, "no Gaussian resampling for the odd part");
+  Op dec;
+  dec.kind = OP_COPY;
+  std::memset(&dec.cp, 0, sizeof(dec.cp));
+  dec.cp.mode = 5;
+  dec.cp.n = n;
+  dec.cp.nc = s;
+  dec.cp.nbatch = batch;
+  dec.cp.in_bstride = idist;
+  dec.cp.out_bstride = n;
+  dec.dst_bytes = (size_t)(batch * n) * sizeof(T) * 2;
+  ops->push_back(dec);
+  int r = 0;
+  std::vector<Op> hops;
+  int rc = build_c2c_hvdh<T>(P, hv, batch * s, p, p, dir, &hops, &r);
+  if (rc) return rc;
+  SolveParams& sv = hops.back().sv;
+  sv.tw = omega_table<T>(P, n, n, 1, dir);
+  sv.tw_s = s;
+  if (!sv.tw) return fail(FFTJ_ERR_CUDA, "table upload failed");
+  for (auto& o : hops) ops->push_back(o);
+  std::vector<Op> sops;
+  rc = build_axis_passes<T>(P, s, p, batch, n, n, dir, scale, &sops);
+  if (rc) return rc;
+  sops.back().pp.out_bstride = odist;
+  sops.back().dst_bytes = (size_t)(batch * odist) * sizeof(T) * 2;
+  for (auto& o : sops) ops->push_back(o);
+  P->resample_m = hv.t;
+  P->resample_w = hv.w;
+  *route = FFTJ_ROUTE_SPLIT;
+  return FFTJ_OK;
+}
+
 // complex 1-D transform of length n (batch at idist/odist) appended to ops;
 // if load_op != PLAIN, the first pass uses it with the given parameters.
 template <typename T>
@@ -919,6 +985,13 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
   if (hv_ok) {
     Hvdh hv = hvdh_parts(n, sizeof(T) == 8, scale);
     if (hv.ok) return build_c2c_hvdh<T>(P, hv, batch, idist, odist, dir, ops, route);
+  }
+  // even non-smooth lengths whose odd part FFTJ would Gaussian-resample
+  if (!g_tables.rs && use_split(sizeof(T) == 8, n)) {
+    const size_t mark = ops->size();
+    const int rc = build_c2c_split<T>(P, n, batch, idist, odist, dir, scale, ops, route);
+    if (rc == FFTJ_OK) return rc;
+    ops->resize(mark);  // fall back to full-length resampling
   }
   // non-smooth: resample onto m (src/resample.jl:258-276), from the caller's
   // tables when it supplied them

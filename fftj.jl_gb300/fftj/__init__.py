@@ -41,7 +41,7 @@ class DimensionMismatch(ValueError):
     """FFTJ's DimensionMismatch (array sizes do not match the plan)."""
 
 
-ROUTES = {0: "FFTPlan", 1: "FourStepPlan", 2: "ResamplePlan", 3: "HvdhPlan", 4: "NdPlan"}
+ROUTES = {0: "FFTPlan", 1: "FourStepPlan", 2: "ResamplePlan", 3: "HvdhPlan", 4: "NdPlan", 5: "SplitPlan"}
 
 
 class PlanInfo(ctypes.Structure):

@@ -51,7 +51,8 @@ typedef enum {
   FFTJ_ROUTE_FOURSTEP = 1,  /* FourStepPlan: multi-pass out-of-cache length */
   FFTJ_ROUTE_RESAMPLE = 2,  /* ResamplePlan: non-smooth length */
   FFTJ_ROUTE_HVDH = 3,      /* HvdhPlan */
-  FFTJ_ROUTE_ND = 4         /* NdPlan / RfftNdPlan / IrfftNdPlan */
+  FFTJ_ROUTE_ND = 4,        /* NdPlan / RfftNdPlan / IrfftNdPlan */
+  FFTJ_ROUTE_SPLIT = 5      /* SplitPlan / CompositePlan: n = s p, s 7-smooth, p by Gaussian resampling */
 } fftj_route;
 
 typedef struct {

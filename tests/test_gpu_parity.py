@@ -428,3 +428,23 @@ def test_odd_radix_lengths_that_need_two_passes(fftj, orc, T, n):
     assert rel_l2(y[0], yo) <= parity_tol(T, n)
     xi = host(fftj.plan_ifft(T, n, batch=2)(dev(y, T)))
     assert rel_l2(xi, x) <= 2 * parity_tol(T, n)
+
+
+@pytest.mark.parametrize("T,n,B", [(np.float64, 2 * 10007, 2), (np.float64, 6 * 3001, 3), (np.float64, 16 * 509, 4),
+                                   (np.float64, 30 * 4099, 1), (np.float64, 1024 * 1009, 1),
+                                   (np.float32, 4 * 32771, 2), (np.float32, 64 * 1031, 1)])
+def test_split_route(fftj, T, n, B):
+    """Even non-smooth lengths n = s p (s 7-smooth, p odd and Gaussian-
+    resampled): decimation, s HvdH sub-transforms with the w_n^(r k1)
+    twiddles in their banded solve, length-s passes along r (FFTJ
+    SplitPlan / CompositePlan mathematics). Forward against FP64 numpy,
+    normalised inverse round trip."""
+    p = fftj.plan_fft(T, n, batch=B)
+    assert p.route == "SplitPlan", p.route
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((B, n)) + 1j * rng.standard_normal((B, n))
+    y = p(dev(x, T))
+    tol = parity_tol(T, n)
+    assert rel_l2(host(y), np.fft.fft(x, axis=-1)) <= tol
+    xi = host(fftj.plan_ifft(T, n, batch=B)(y))
+    assert rel_l2(xi, x) <= 2 * tol

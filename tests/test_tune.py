@@ -117,3 +117,17 @@ def test_every_smooth_length_plans_by_default(T):
                     T.plan_info(T.query("r2c", dt, n), (0, 0, 0, 0, 0, tmax))
     inf = T.plan_info(T.query("c2c", np.float64, 3969))
     assert inf.npasses == 2
+
+
+def test_split_route_choice(T):
+    """Even non-smooth lengths take the split route when their odd part is
+    one FFTJ would Gaussian-resample (F64 >= 1000, F32 >= 16384), else
+    full-length resampling; the route knob forces either."""
+    assert info(T, "c2c", np.float64, 2 * 10007).route == 5
+    assert info(T, "c2c", np.float64, 10006).route == 2               # n < 16384: resampling, as FFTJ
+    assert info(T, "c2c", np.float64, 16 * 509).route == 5            # s >= 16: FFTJ's composite lengths
+    assert info(T, "c2c", np.float32, 2 * 10007).route == 2          # odd part below the F32 threshold
+    assert info(T, "c2c", np.float32, 4 * 32771).route == 5
+    assert info(T, "c2c", np.float64, 2 * 10007, route=1).route == 2  # forced resampling
+    assert info(T, "c2c", np.float32, 2 * 10007, route=2).route == 5  # forced Gaussian (split)
+    assert info(T, "c2c", np.float64, 2 * 512).route in (0, 1)        # smooth: no split
