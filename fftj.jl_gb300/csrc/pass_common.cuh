@@ -686,7 +686,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
     } else {
       // lanes walk the tile's columns (contiguous p or q runs)
       const int64_t gcol = pp.s * pcol + q0 + ql;
-      const bool ok = batch < pp.nbatch;
+      const bool ok = batch < pp.nbatch && q0 + ql < pp.s;  // ragged lane tiles
 #pragma unroll
       for (int i = 0; i < EPT; ++i) {
         const int j = kg + i * Tf;
@@ -772,7 +772,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
       }
     }
   } else {
-    const bool ok = batch < pp.nbatch;
+    const bool ok = batch < pp.nbatch && q0 + ql < pp.s;
 #pragma unroll
     for (int i = 0; i < EPT; ++i) {
       const int j = kg + i * Tf;
@@ -906,7 +906,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
   const int pl = cq - cbt * P;
   const int64_t batch = b0 + cbt;
   const int64_t pcol = p0 + pl;
-  const bool colok = batch < pp.nbatch;
+  const bool colok = batch < pp.nbatch && q0 + ql < pp.s;  // ragged lane tiles
   // the pass's inner twiddles w_R^t are staged in shared memory right after
   // the tile (smem_elems), so sub-stages read them with 32-bit shared
   // addresses: no per-element global index arithmetic

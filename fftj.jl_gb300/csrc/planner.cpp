@@ -574,6 +574,9 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
       if (Pt == m) NBt = std::max<i64>(1, cols / m);
     } else {
       Qt = largest_divisor_le(s, cols);
+      // a stride with no good divisor (a large prime factor) gets ragged
+      // lane tiles: the last tile's lanes beyond s are masked
+      if (Qt * 2 < std::min<i64>(cols, s)) Qt = std::min<i64>(cols, s);
       if (Qt == s) {
         Pt = largest_divisor_le(m, cols / Qt);
         if (Pt == m) NBt = std::max<i64>(1, cols / (m * s));
@@ -590,7 +593,7 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
     pp.fP = FastDiv((uint32_t)Pt);
     pp.fR = FastDiv((uint32_t)R);
     pp.fNB = FastDiv((uint32_t)pp.NB);
-    pp.tiles_q = (uint32_t)(s / Qt);
+    pp.tiles_q = (uint32_t)((s + Qt - 1) / Qt);
     pp.tiles_p = (uint32_t)(m / Pt);
     pp.tiles_b = (uint32_t)((nbatch + NBt - 1) / NBt);
     pp.ftq = FastDiv(pp.tiles_q);
