@@ -45,60 +45,115 @@ __device__ __forceinline__ void interp_at(const InterpParams& ip, const Cx<T>* _
 template <typename T, int B, bool CG>
 __device__ __forceinline__ void solve_at(const SolveParams& sp, const Cx<T>* __restrict__ g,
                                          Cx<T>* __restrict__ y, const int64_t tid) {
+  // Rows go in blocks of K: a block's operands (input rows, LU factors,
+  // output indices) are loaded together, then its K dependent recurrence
+  // steps run from registers. Row pointers advance by increments (the
+  // kernel is a latency chain: every instruction of a row counts).
+  constexpr int K = 8;
   const int64_t nt = sp.nbatch * sp.nchunk;
   if (tid >= nt) return;
   const int64_t b = tid / sp.nchunk, ch = tid - b * sp.nchunk;
-  const int64_t R = sp.R, t = sp.t;
-  const T* lf = reinterpret_cast<const T*>(sp.lf) + ch * R * B;
-  const T* uf = reinterpret_cast<const T*>(sp.uf) + ch * R * (B + 1);
-  const int32_t* oi = sp.oi + ch * R;
-  Cx<T>* zw = reinterpret_cast<Cx<T>*>(sp.zw) + tid;
+  const int R = (int)sp.R, H = (int)sp.H, L = (int)sp.L;
+  const int t = (int)sp.t;
+  // factor tables are row-major across chunks: row i of chunk ch at
+  // i * nchunk + ch (adjacent lanes read adjacent entries)
+  const int64_t nc = sp.nchunk;
+  const T* lfp = reinterpret_cast<const T*>(sp.lf) + ch * B;
+  const T* ufp = reinterpret_cast<const T*>(sp.uf) + ch * (B + 1);
+  const int32_t* oip = sp.oi + ch;
+  const int64_t lstep = nc * B, ustep = nc * (B + 1);
+  Cx<T>* zwp = reinterpret_cast<Cx<T>*>(sp.zw) + tid;
   const Cx<T>* gb = g + b * sp.g_bstride;
-  int64_t q = ch * sp.L - sp.H;
-  q = ((q % t) + t) % t;
+  int q = (int)((((int64_t)ch * L - H) % t + t) % t);
   Cx<T> zp[B];
 #pragma unroll
   for (int k = 0; k < B; ++k) zp[k] = mk<T>(0, 0);  // zp[k] = z_{i-1-k}
-  for (int64_t i = 0; i < R; ++i) {
-    Cx<T> z = mk<T>(0, 0);
-    if (__ldg(oi + i) >= 0) z = ldd<CG>(gb + q);
+  for (int i0 = 0; i0 < R; i0 += K) {
+    Cx<T> gv[K];
+    T f[K][B];
 #pragma unroll
-    for (int k = 0; k < B; ++k) {
-      const T f = __ldg(lf + i * B + k);
-      z.x = fma(-f, zp[k].x, z.x);
-      z.y = fma(-f, zp[k].y, z.y);
+    for (int u = 0; u < K; ++u) {
+      gv[u] = mk<T>(0, 0);
+      if (i0 + u < R) {
+        int qq = q + u;
+        if (qq >= t) qq -= t;
+        const Cx<T> v = ldd<CG>(gb + qq);  // in range for every row: load, then mask
+        if (__ldg(oip + u * nc) >= 0) gv[u] = v;
+#pragma unroll
+        for (int k = 0; k < B; ++k) f[u][k] = __ldg(lfp + u * lstep + k);
+      }
     }
 #pragma unroll
-    for (int k = B - 1; k > 0; --k) zp[k] = zp[k - 1];
-    zp[0] = z;
-    zw[i * nt] = z;
-    if (++q == t) q = 0;
+    for (int u = 0; u < K; ++u) {
+      if (i0 + u < R) {
+        Cx<T> z = gv[u];
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+          z.x = fma(-f[u][k], zp[k].x, z.x);
+          z.y = fma(-f[u][k], zp[k].y, z.y);
+        }
+#pragma unroll
+        for (int k = B - 1; k > 0; --k) zp[k] = zp[k - 1];
+        zp[0] = z;
+        zwp[u * nt] = z;
+      }
+    }
+    q += K;
+    if (q >= t) q -= t;
+    lfp += K * lstep;
+    oip += K * nc;
+    zwp += K * nt;
   }
   Cx<T> xp[B];
 #pragma unroll
   for (int k = 0; k < B; ++k) xp[k] = mk<T>(0, 0);  // xp[k] = x_{i+1+k}
   const T sc = (T)sp.sc;
   Cx<T>* yb = y + b * sp.y_bstride;
-  for (int64_t i = R - 1; i >= sp.H; --i) {
-    Cx<T> x = zw[i * nt];
+  const Cx<T>* twb = sp.tw ? reinterpret_cast<const Cx<T>*>(sp.tw) + 0 : nullptr;
+  const int64_t twr = sp.tw ? (b % sp.tw_s) : 0;
+  // back substitution from row R-1 down to H
+  const Cx<T>* zr = reinterpret_cast<const Cx<T>*>(sp.zw) + tid + (int64_t)(R - 1) * nt;
+  const T* urp = reinterpret_cast<const T*>(sp.uf) + ch * (B + 1) + (int64_t)(R - 1) * ustep;
+  const int32_t* orp = sp.oi + ch + (int64_t)(R - 1) * nc;
+  for (int i0 = R - 1; i0 >= H; i0 -= K) {
+    Cx<T> zv[K];
+    T uu[K][B + 1];
+    int32_t ov[K];
 #pragma unroll
-    for (int j = 0; j < B; ++j) {
-      const T u = __ldg(uf + i * (B + 1) + 1 + j);
-      x.x = fma(-u, xp[j].x, x.x);
-      x.y = fma(-u, xp[j].y, x.y);
-    }
-    const T iu = __ldg(uf + i * (B + 1));
-    x.x *= iu;
-    x.y *= iu;
+    for (int u = 0; u < K; ++u) {
+      if (i0 - u >= H) {
+        zv[u] = zr[-(int64_t)u * nt];
 #pragma unroll
-    for (int k = B - 1; k > 0; --k) xp[k] = xp[k - 1];
-    xp[0] = x;
-    const int32_t o = __ldg(oi + i);
-    if (i < sp.H + sp.L && o >= 0) {
-      Cx<T> v = mk<T>(x.x * sc, x.y * sc);
-      if (sp.tw) v = cmul(v, __ldg(reinterpret_cast<const Cx<T>*>(sp.tw) + (b % sp.tw_s) * (int64_t)o));
-      yb[o] = v;
+        for (int j = 0; j <= B; ++j) uu[u][j] = __ldg(urp - u * ustep + j);
+        ov[u] = __ldg(orp - u * nc);
+      }
     }
+#pragma unroll
+    for (int u = 0; u < K; ++u) {
+      const int i = i0 - u;
+      if (i >= H) {
+        Cx<T> x = zv[u];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+          x.x = fma(-uu[u][1 + j], xp[j].x, x.x);
+          x.y = fma(-uu[u][1 + j], xp[j].y, x.y);
+        }
+        x.x *= uu[u][0];
+        x.y *= uu[u][0];
+#pragma unroll
+        for (int k = B - 1; k > 0; --k) xp[k] = xp[k - 1];
+        xp[0] = x;
+        const int32_t o = ov[u];
+        if (i < H + L && o >= 0) {
+          Cx<T> v = mk<T>(x.x * sc, x.y * sc);
+          if (twb) v = cmul(v, __ldg(twb + twr * o));
+          yb[o] = v;
+        }
+      }
+    }
+    zr -= K * nt;
+    urp -= K * ustep;
+    orp -= K * nc;
   }
 }
 

@@ -130,7 +130,9 @@ cudaError_t launch_copy(const CopyParams& cp, const void* in, void* out, cudaStr
 template <typename T>
 cudaError_t launch_solve(const SolveParams& sp, const void* g, void* y, cudaStream_t st) {
   const int64_t total = sp.nbatch * sp.nchunk;
-  const int th = 128;
+  // one warp per CTA: the solve is FP64-pipe bound and has few threads
+  // (batch x chunks), so small CTAs spread it over every SM
+  const int th = 32;
   const unsigned grid = (unsigned)((total + th - 1) / th);
   auto gg = reinterpret_cast<const Cx<T>*>(g);
   auto yy = reinterpret_cast<Cx<T>*>(y);

@@ -297,13 +297,15 @@ struct Hvdh {
   double alpha, a, b, sc;
   std::vector<double> wt;    // t*w spread weights
   std::vector<int32_t> l0;   // t: first input row of each spread output
-  std::vector<double> lf;    // nchunk*R*B forward multipliers (rows i-1 .. i-B)
-  std::vector<double> uf;    // nchunk*R*(B+1): 1/U_ii, U_{i,i+1..i+B}
-  std::vector<int32_t> oi;   // nchunk*R: output index of the row's unknown (-1: identity row)
+  // factor tables row-major across chunks (entry (i, ch) at i*nchunk + ch),
+  // so the solve's lanes -- consecutive chunks -- read adjacent entries
+  std::vector<double> lf;    // R*nchunk*B forward multipliers (rows i-1 .. i-B)
+  std::vector<double> uf;    // R*nchunk*(B+1): 1/U_ii, U_{i,i+1..i+B}
+  std::vector<int32_t> oi;   // R*nchunk: output index of the row's unknown (-1: identity row)
   bool ok = false;
 };
 
-Hvdh hvdh_parts(i64 n, bool f64, double scale) {
+Hvdh hvdh_parts(i64 n, bool f64, double scale, i64 nbatch) {
   Hvdh P;
   P.n = n;
   P.t = hvdh_t(n);
@@ -330,10 +332,14 @@ Hvdh hvdh_parts(i64 n, bool f64, double scale) {
     P.H = it != cache.end() ? it->second : (cache[key] = hvdh_halo(n, t, P.a, P.B, tol));
   }
   if (P.H < 0) return P;
-  // chunks: L rows (a divisor of t near 128), R = L + 2H rows each
+  // chunks: L rows (a divisor of t), R = L + 2H rows each. The solve runs
+  // one thread per (batch, chunk) along a dependent chain of R rows, so L
+  // trades halo work (2H / L) for threads: aim for ~40K threads, with L
+  // between max(32, 2H) and 128.
+  const double want = std::min(128.0, std::max({32.0, 2.0 * (double)P.H, (double)t * nbatch / 40000.0}));
   i64 L = 1;
   for (i64 d = 1; d <= 256; ++d)
-    if (t % d == 0 && std::abs((double)d - 128) <= std::abs((double)L - 128)) L = d;
+    if (t % d == 0 && std::abs((double)d - want) <= std::abs((double)L - want)) L = d;
   P.L = L;
   P.R = L + 2 * P.H;
   P.nchunk = t / L;
@@ -381,7 +387,7 @@ Hvdh hvdh_parts(i64 n, bool f64, double scale) {
     for (i64 i = 0; i < R; ++i) {
       const i64 q = qrow(i);
       if (ell[q] < 0) { A[i * (2 * B + 1) + B] = 1.0; continue; }
-      P.oi[ch * R + i] = (int32_t)((P.delta * ell[q]) % n);
+      P.oi[i * P.nchunk + ch] = (int32_t)((P.delta * ell[q]) % n);
       for (int k = -B; k <= B; ++k) {
         const i64 j = i + k;
         if (j < 0 || j >= R) continue;
@@ -398,7 +404,7 @@ Hvdh hvdh_parts(i64 n, bool f64, double scale) {
         if (j < 0) continue;
         const double piv = A[j * (2 * B + 1) + B];
         const double f = A[i * (2 * B + 1) + (j - i) + B] / piv;
-        P.lf[(ch * R + i) * B + (k - 1)] = f;
+        P.lf[(i * P.nchunk + ch) * B + (k - 1)] = f;
         if (f == 0) continue;
         for (int cc = 0; cc <= B; ++cc) {  // row j's U part: columns j .. j+B
           const i64 col = j + cc;
@@ -408,8 +414,8 @@ Hvdh hvdh_parts(i64 n, bool f64, double scale) {
         }
       }
       const double d = A[i * (2 * B + 1) + B];
-      P.uf[(ch * R + i) * (B + 1)] = 1.0 / d;
-      for (int j = 1; j <= B; ++j) P.uf[(ch * R + i) * (B + 1) + j] = A[i * (2 * B + 1) + B + j];
+      P.uf[(i * P.nchunk + ch) * (B + 1)] = 1.0 / d;
+      for (int j = 1; j <= B; ++j) P.uf[(i * P.nchunk + ch) * (B + 1) + j] = A[i * (2 * B + 1) + B + j];
     }
   }
   P.ok = true;
@@ -930,7 +936,7 @@ template <typename T>
 int build_c2c_split(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir, double scale,
                     std::vector<Op>* ops, int* route) {
   const i64 s = smooth7_part(n), p = n / s;
-  Hvdh hv = hvdh_parts(p, sizeof(T) == 8, 1.0);
+  Hvdh hv = hvdh_parts(p, sizeof(T) == 8, 1.0, batch * s);
   if (!hv.ok) return fail(FFTJ_ERR_UNSUPPORTED, "no Gaussian resampling for the odd part");
   Op dec;
   dec.kind = OP_COPY;
@@ -986,7 +992,7 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
   const bool hv_ok = !g_tables.rs && (g_sched.route == 2 ? (n % 2 == 1 && n >= 64)
                                                          : (g_sched.route == 0 && use_hvdh(sizeof(T) == 8, n)));
   if (hv_ok) {
-    Hvdh hv = hvdh_parts(n, sizeof(T) == 8, scale);
+    Hvdh hv = hvdh_parts(n, sizeof(T) == 8, scale, batch);
     if (hv.ok) return build_c2c_hvdh<T>(P, hv, batch, idist, odist, dir, ops, route);
   }
   // even non-smooth lengths whose odd part FFTJ would Gaussian-resample
