@@ -442,7 +442,7 @@ def learned_planner_report():
         t0 = time.perf_counter()
         tune.autotune(tq)
         t_exh += time.perf_counter() - t0
-    return {
+    report = {
         "held_in_problems": int(held_in.size), "held_out_problems": int(held_out.size),
         "timed_schedules": int(len(ds["ms"])),
         "mlp": "28 -> 64 -> 64 -> 1 ReLU FP32, Adam, trained by the library's CUDA kernels",
@@ -458,6 +458,31 @@ def learned_planner_report():
         "planning_ms_exhaustive": round(1e3 * t_exh / len(qs), 2),
         "feature_seconds": round(t_feat, 2),
     }
+    return report, model
+
+
+def choose_schedules(model, items):
+    """The model's schedule for every (kind, dtype, n) item: candidates and
+    their features from dry plans (host threads), one inference launch over
+    all of them, argmin per item."""
+    from concurrent.futures import ThreadPoolExecutor
+    from fftj import tune
+
+    def cand(it):
+        kind, dt, n = it
+        q = tune.query(kind, dt, n)
+        c = tune.candidates(q)
+        return c, tune.features(q, c)
+
+    with ThreadPoolExecutor(16) as ex:
+        per = list(ex.map(cand, items))
+    feats = np.concatenate([f for _, f in per])
+    pred = model.predict_log_ms(feats)
+    out, o = [], 0
+    for c, f in per:
+        out.append(c[int(np.argmin(pred[o:o + len(c)]))])
+        o += len(c)
+    return out
 
 
 def run_uneven(args):
@@ -586,7 +611,31 @@ def run_uneven(args):
     e2e_ms = a.elapsed_time(b) / e2e_steps
     e2e_ok = torch.equal(h_out, out_buf.cpu())
 
-    learned = learned_planner_report() if not args.no_learned else None
+    learned, model = learned_planner_report() if not args.no_learned else (None, None)
+    if model is not None:
+        # the whole batch with the planner's default schedules and with the
+        # model's, both as a CUDA-graph group (no thread cap)
+        from fftj import tune
+        t0 = time.perf_counter()
+        chosen = choose_schedules(model, items[:-1])
+        t_choose = time.perf_counter() - t0
+
+        def mk_opts(it, opts):
+            kind, dt, n = it
+            if kind == "r2c3d":
+                return fftj.Plan(dt, n, kind="r2c")
+            return fftj.Plan(dt, (n,), kind=kind, opts=dict(zip(tune.OPT_FIELDS, opts)) if opts else None)
+
+        for label, sched in (("default", [None] * (len(items) - 1)), ("learned", chosen)):
+            with ThreadPoolExecutor(16) as ex:
+                pl = list(ex.map(lambda a: mk_opts(*a), zip(items, sched + [None])))
+            g = fftj.Group(pl, xs, ys, mode="graph")
+            ms_g = time_mode(g, args.steps)
+            learned["graph_%s_schedules" % label] = {"ms": round(ms_g, 3),
+                                                     "gflops": round(step_flops / (ms_g * 1e-3) / 1e9, 1)}
+            del g, pl
+        learned["choose_seconds_10000"] = round(t_choose, 2)
+        learned["schedules_changed"] = int(sum(1 for c in chosen if any(c)))
     nprime = sum(1 for k, _, n in items[:-1] if not isinstance(n, tuple) and fftj.tune.is_prime(n))
     if rank == 0:
         out = {

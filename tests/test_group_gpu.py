@@ -25,6 +25,7 @@ ITEMS = [
     ("c2r", np.float32, 4096, 2, 1),       # irfft: fused pre-pass load
     ("c2c", np.float32, 1 << 20, 1, -1),   # the largest length of the uneven workload
     ("c2c", np.float64, 3 * 5 * 7 * 11 * 13, 1, -1),
+    ("c2c", np.float64, 2 * 10007, 2, -1),  # split route: decimation copy, twiddled banded solve
 ]
 
 
