@@ -990,46 +990,65 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
       }
     }
     __syncthreads();
-    if constexpr (NS > 2 || (NS == 2 && MODE == 1)) {
-      // middle sub-stages (all but the last when the store is fused)
-      run_mid_ct<T, DIR, TF, R, r0, (MODE == 2 ? 1 : 0), Rs...>(buf, b, kg, NB, twR);
+    if constexpr (NS > 2) {
+      // middle sub-stages (the last one is fused into the store)
+      run_mid_ct<T, DIR, TF, R, r0, 1, Rs...>(buf, b, kg, NB, twR);
     }
   }
 
   const bool scaled = not_one(pp.scale);
   const T sc = (T)pp.scale;
   const bool tw = pp.tw_mode != 0;
-  if constexpr (MODE == 1 && sizeof(T) == 4) {
-    if (tw && R % nthr == 0) {
-      // ---- row store with outer twiddles, thread tid owning outputs
-      // j = tid + jj*nthr of every column c of the tile. Along c the twiddle
-      // w^((p0+c) j) advances by w^j: one complex multiply per element
-      // instead of a table lookup, re-seeded exactly every 8 columns (at most
-      // 7 steps of rounding). F32 only: F64 passes are FP64-pipe bound and
-      // the lookup costs them nothing while the multiply does.
-      if (b0 < pp.nbatch) {
-        Cx<T>* ob = out + b0 * pp.out_bstride + (int64_t)R * p0 + tid;
-        for (int j0 = 0; j0 < R; j0 += nthr) {
-          const uint32_t j = (uint32_t)(tid + j0);
-          const Cx<T> step = j ? outer_tw<T>(pp, j) : mk<T>(1, 0);
-          uint32_t e = (uint32_t)p0 * j;
-          Cx<T> w = mk<T>(1, 0);
-          const int a0 = (int)j * NB;
-#pragma unroll 8
-          for (int c = 0; c < NB; ++c) {
-            if ((c & 7) == 0) w = e ? outer_tw<T>(pp, e) : mk<T>(1, 0);
-            Cx<T> v = cmul(buf[pidx<T>(a0 + c)], w);
-            if (scaled) { v.x *= sc; v.y *= sc; }
-            ob[(int64_t)c * R + j0] = v;
-            w = cmul(w, step);
-            e += j;
+  if constexpr (MODE == 1) {
+    // ---- fused last sub-stage (radix rL) + row store (s == 1). Butterfly
+    // u = c S + k takes k fastest across lanes, so for each output
+    // j = k + jj S the lanes of a warp write consecutive addresses of column
+    // c's output row. F32: the outer twiddle w^((p0 + c) j) advances along
+    // jj by w^((p0 + c) S), one complex multiply per output instead of a
+    // table lookup (at most rL - 1 <= 15 steps); F64 passes are FP64-pipe
+    // bound and keep the lookups.
+    static_assert(NS >= 2, "a first pass has at least two sub-stages");
+    constexpr int S = R / rL;
+    constexpr bool kRecur = sizeof(T) == 4;
+    const int nbf = NB * S;
+    if (b0 < pp.nbatch) {
+      Cx<T>* orow = out + b0 * pp.out_bstride + (int64_t)R * p0;
+      for (int u = tid; u < nbf; u += nthr) {
+        const int c = u / S;
+        const int k = u - c * S;
+        Cx<T> v[rL];
+#pragma unroll
+        for (int j = 0; j < rL; ++j) v[j] = buf[pidx<T>((k + j * S) * NB + c)];
+        Dft<T, DIR, rL>::run(v);
+        const uint32_t pc = (uint32_t)(p0 + c);
+        uint32_t e = pc * (uint32_t)k;
+        const uint32_t estep = pc * (uint32_t)S;
+        Cx<T> w = mk<T>(1, 0), wstep = mk<T>(1, 0);
+        if (kRecur && tw) {
+          if (e != 0) w = outer_tw<T>(pp, e);
+          if (estep != 0) wstep = outer_tw<T>(pp, estep);
+        }
+        Cx<T>* o = orow + (int64_t)R * c + k;
+#pragma unroll
+        for (int j = 0; j < rL; ++j) {
+          Cx<T> x = v[j];
+          if (kRecur) {
+            if (tw) {
+              x = cmul(x, w);
+              w = cmul(w, wstep);
+            }
+          } else if (tw && e != 0) {
+            x = cmul(x, outer_tw<T>(pp, e));
           }
+          if (scaled) { x.x *= sc; x.y *= sc; }
+          o[j * S] = x;
+          e += estep;
         }
       }
-      return;
     }
+    return;
   }
-  if constexpr (MODE <= 1) {
+  if constexpr (MODE == 0) {
     // ---- row store (lanes walk j): outputs contiguous along j (s == 1)
     const int dc = nthr / R, dj = nthr - (nthr / R) * R;
     int c = tid / R, j = tid - (tid / R) * R;
@@ -1049,8 +1068,8 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
 #pragma unroll
     for (int i = 0; i < EPT; ++i) {
       const int e = tid + i * nthr;
-      // MODE 0: column c is a batch entry; MODE 1: a butterfly p of batch b0
-      if (e < E && b0 + (MODE == 0 ? c : 0) < pp.nbatch) {
+      // column c is a batch entry
+      if (e < E && b0 + c < pp.nbatch) {
         Cx<T> v = buf[pidx<T>(j * NB + c)];
         if (tw) v = cmul(v, w[i]);
         if (scaled) { v.x *= sc; v.y *= sc; }
@@ -1060,7 +1079,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
       j += dj; c += dc;
       if (j >= R) { j -= R; c++; }
     }
-  } else {
+  } else if constexpr (MODE == 2) {
     // ---- fused last sub-stage (radix rL, L = rL, no inner twiddle) + store:
     // butterfly k (< S = R/rL) writes positions j*S + k of its column
     constexpr int S = R / rL;
