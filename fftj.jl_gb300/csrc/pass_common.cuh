@@ -921,7 +921,43 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
     twR = twS;
   }
 
-  if constexpr (MODE == 0) {
+  if constexpr (MODE == 0 && NS >= 2) {
+    // ---- fused row load + first sub-stage (radix r0, S = 1). Butterfly
+    // u = c Rr + k takes k fastest across lanes: its inputs k + j Rr of row
+    // c are read straight from HBM, consecutive lanes at consecutive
+    // addresses for each j.
+    constexpr int Rr = R / r0;
+    const int nbf = NB * Rr;
+    const int64_t bstr = LOADOP == LOAD_PLAIN ? pp.in_bstride : pp.ld_stride;
+    __syncthreads();  // staged twiddles visible
+    for (int u = tid; u < nbf; u += nthr) {
+      const int c = u / Rr;
+      const int k = u - c * Rr;
+      const int64_t bb = b0 + c;
+      Cx<T> v[r0];
+      if (bb < pp.nbatch) {
+#pragma unroll
+        for (int j = 0; j < r0; ++j) v[j] = load_elem_off<T, LOADOP>(pp, in, bb * bstr, k + j * Rr);
+      } else {
+#pragma unroll
+        for (int j = 0; j < r0; ++j) v[j] = mk<T>(0, 0);
+      }
+      Dft<T, DIR, r0>::run(v);
+      const int a = r0 * k * NB + c;
+      buf[pidx<T>(a)] = v[0];
+#pragma unroll
+      for (int j = 1; j < r0; ++j) {
+        Cx<T> w = v[j];
+        if (k != 0) w = cmul(w, twR[j * k]);
+        buf[pidx<T>(a + j * NB)] = w;
+      }
+    }
+    __syncthreads();
+    if constexpr (NS > 2) {
+      // middle sub-stages (the last one is fused into the row store)
+      run_mid_ct<T, DIR, TF, R, r0, 1, Rs...>(buf, b, kg, NB, twR);
+    }
+  } else if constexpr (MODE == 0) {
     // ---- row load (lanes walk j): e = tid + i*nthr -> (c, j), c = column
     Cx<T> v[EPT];
     const int dc = nthr / R, dj = nthr - (nthr / R) * R;
@@ -1048,7 +1084,30 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
     }
     return;
   }
-  if constexpr (MODE == 0) {
+  if constexpr (MODE == 0 && NS >= 2) {
+    // ---- fused last sub-stage (radix rL) + row store: butterfly u = c S + k
+    // with k fastest across lanes writes outputs k + jj S of row c, the
+    // lanes of a warp at consecutive addresses for each jj (one pass over
+    // whole transforms: no outer twiddle)
+    constexpr int S = R / rL;
+    const int nbf = NB * S;
+    for (int u = tid; u < nbf; u += nthr) {
+      const int c = u / S;
+      const int k = u - c * S;
+      if (b0 + c >= pp.nbatch) continue;
+      Cx<T> v[rL];
+#pragma unroll
+      for (int j = 0; j < rL; ++j) v[j] = buf[pidx<T>((k + j * S) * NB + c)];
+      Dft<T, DIR, rL>::run(v);
+      Cx<T>* o = out + (b0 + c) * pp.out_bstride + k;
+#pragma unroll
+      for (int j = 0; j < rL; ++j) {
+        Cx<T> x = v[j];
+        if (scaled) { x.x *= sc; x.y *= sc; }
+        o[j * S] = x;
+      }
+    }
+  } else if constexpr (MODE == 0) {
     // ---- row store (lanes walk j): outputs contiguous along j (s == 1)
     const int dc = nthr / R, dj = nthr - (nthr / R) * R;
     int c = tid / R, j = tid - (tid / R) * R;
