@@ -158,28 +158,36 @@ __device__ __forceinline__ void solve_at(const SolveParams& sp, const Cx<T>* __r
 }
 
 // rfft even post-pass (FFTJ src/real.jl:85-135): X[k] = xe + w (-i xo).
+// X[k] and X[h-k] both come from Z[k] and Z[h-k], so one thread makes the
+// pair (k = 0 .. h/2, k = 0 also writing X[h]) and each Z entry is read once.
+template <typename T>
+__device__ __forceinline__ Cx<T> real_post_one(Cx<T> a, Cx<T> bb, Cx<T> w) {
+  bb.y = -bb.y;  // conj Z[h - k]
+  const T half = (T)0.5;
+  const T xer = (a.x + bb.x) * half, xei = (a.y + bb.y) * half;
+  const T xor_ = (a.x - bb.x) * half, xoi = (a.y - bb.y) * half;
+  return mk<T>(xer + fma(w.x, xoi, w.y * xor_), xei + fma(w.y, xoi, -(w.x * xor_)));
+}
+
 template <typename T, bool CG>
 __device__ __forceinline__ void real_post_at(const RealPostParams& rp, const Cx<T>* __restrict__ z,
                                              Cx<T>* __restrict__ y, const int64_t idx) {
-  const int64_t h = rp.h;
-  if (idx >= (h + 1) * rp.nbatch) return;
-  const int64_t b = idx / (h + 1), k = idx - b * (h + 1);
+  const int64_t h = rp.h, nk = h / 2 + 1;
+  if (idx >= nk * rp.nbatch) return;
+  const int64_t b = idx / nk, k = idx - b * nk;
   const Cx<T>* Z = z + b * rp.z_bstride;
-  Cx<T> out;
-  if (k == 0 || k == h) {
+  Cx<T>* Y = y + b * rp.y_bstride;
+  const Cx<T>* tw = reinterpret_cast<const Cx<T>*>(rp.tw);
+  if (k == 0) {
     const Cx<T> z0 = ldd<CG>(Z);
-    out = mk<T>(k == 0 ? z0.x + z0.y : z0.x - z0.y, 0);
-  } else {
-    const Cx<T> a = ldd<CG>(Z + k);
-    Cx<T> bb = ldd<CG>(Z + (h - k));
-    bb.y = -bb.y;
-    const T half = (T)0.5;
-    const T xer = (a.x + bb.x) * half, xei = (a.y + bb.y) * half;
-    const T xor_ = (a.x - bb.x) * half, xoi = (a.y - bb.y) * half;
-    const Cx<T> w = __ldg(reinterpret_cast<const Cx<T>*>(rp.tw) + k);
-    out = mk<T>(xer + fma(w.x, xoi, w.y * xor_), xei + fma(w.y, xoi, -(w.x * xor_)));
+    Y[0] = mk<T>(z0.x + z0.y, 0);
+    Y[h] = mk<T>(z0.x - z0.y, 0);
+    return;
   }
-  y[b * rp.y_bstride + k] = out;
+  const Cx<T> a = ldd<CG>(Z + k);
+  const Cx<T> m = ldd<CG>(Z + (h - k));
+  Y[k] = real_post_one<T>(a, m, __ldg(tw + k));
+  if (h - k != k) Y[h - k] = real_post_one<T>(m, a, __ldg(tw + (h - k)));
 }
 
 // Odd-length real edges (FFTJ src/real.jl:136-140, 194-209).

@@ -208,7 +208,7 @@ uint32_t op_tiles(const Op& op) {
   switch (op.kind) {
     case OP_PASS: return op.pp.tiles_q * op.pp.tiles_p * op.pp.tiles_b;
     case OP_INTERP: return ew(op.ip.n * op.ip.nbatch * std::max<int64_t>(op.ip.inner, 1));
-    case OP_RPOST: return ew((op.rp.h + 1) * op.rp.nbatch);
+    case OP_RPOST: return ew((op.rp.h / 2 + 1) * op.rp.nbatch);
     case OP_COPY: return ew(op.cp.n * op.cp.nbatch);
     case OP_SOLVE: return ew(op.sv.nbatch * op.sv.nchunk);
   }

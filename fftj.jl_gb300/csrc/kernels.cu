@@ -112,7 +112,7 @@ cudaError_t launch_interp(const InterpParams& ip, const void* g, void* y, cudaSt
 
 template <typename T>
 cudaError_t launch_real_post(const RealPostParams& rp, const void* z, void* y, cudaStream_t st) {
-  const int64_t total = (rp.h + 1) * rp.nbatch;
+  const int64_t total = (rp.h / 2 + 1) * rp.nbatch;  // one thread per pair (k, h - k)
   const int th = 256;
   k_real_post<T><<<(unsigned)((total + th - 1) / th), th, 0, st>>>(rp, reinterpret_cast<const Cx<T>*>(z),
                                                                    reinterpret_cast<Cx<T>*>(y));

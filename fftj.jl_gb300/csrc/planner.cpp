@@ -1703,7 +1703,7 @@ int fftj_plan_features(fftj_plan plan, float* out, int cap) {
     } else {
       double total = 0;
       if (op.kind == OP_INTERP) total = (double)op.ip.n * op.ip.nbatch * std::max<int64_t>(op.ip.inner, 1);
-      else if (op.kind == OP_RPOST) total = (double)(op.rp.h + 1) * op.rp.nbatch;
+      else if (op.kind == OP_RPOST) total = (double)(op.rp.h / 2 + 1) * op.rp.nbatch;
       else if (op.kind == OP_COPY) total = (double)op.cp.n * op.cp.nbatch;
       else if (op.kind == OP_SOLVE) total = (double)op.sv.nbatch * op.sv.nchunk;
       ctas += std::ceil(total / 256.0);
