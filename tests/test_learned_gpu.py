@@ -126,3 +126,27 @@ def test_learned_planner_regret_on_held_out_lengths(T):
         learned.mean(), np.quantile(learned, 0.9), default.mean(), np.quantile(default, 0.9)))
     assert learned.mean() <= 1.10
     assert learned.mean() < default.mean()
+
+
+def test_cost_model_falls_back_to_the_exhaustive_tuner(T):
+    """A query whose schedules lie outside the training features (a length
+    beyond the 2^20 of the timing set) is planned by the exhaustive tuner;
+    one inside the range by the model."""
+    ds = load_dataset()
+    sel = np.isin(ds["qid"], np.unique(ds["qid"][ds["split"] == 0])[:300])
+    feats = np.zeros((int(sel.sum()), T.NFEATURES), dtype=np.float32)
+    rows = np.nonzero(sel)[0]
+    for q in np.unique(ds["qid"][rows]):
+        r = rows[ds["qid"][rows] == q]
+        kind = {0: "c2c", 1: "r2c", 2: "c2r"}[int(ds["kind"][r[0]])]
+        dt = np.float64 if ds["f64"][r[0]] else np.float32
+        tq = T.query(kind, dt, int(ds["n"][r[0]]), batch=int(ds["batch"][r[0]]))
+        feats[np.searchsorted(rows, r)] = T.features(tq, [tuple(int(v) for v in o) for o in ds["opts"][r]])
+    model = T.CostModel(seed=4)
+    model.fit(feats, ds["ms"][rows], epochs=60)
+    inside = T.query("c2c", np.float32, int(ds["n"][rows[0]]))
+    opts, how = model.choose(inside)
+    assert how == "model" and opts in T.candidates(inside)
+    outside = T.query("c2c", np.float32, 1 << 22)
+    opts, how = model.choose(outside)
+    assert how == "exhaustive" and opts in T.candidates(outside)
