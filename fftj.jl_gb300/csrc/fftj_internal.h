@@ -2,6 +2,7 @@
 // sm_103a kernels (kernels.cu).
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace fftj {
@@ -88,6 +89,11 @@ struct PassParams {
   double ld_pre;                 // C2R_PRE pair factor (1/2 or 1)
   int ld_w;                      // SPREAD: taps per grid row
   const int32_t* ld_l0;          // SPREAD: first input row of each grid row
+  // pipelined tensor-copy kernel (pass_tma.cuh)
+  int tma_rows;                  // tile rows per box copy (a divisor of R, <= 256)
+  int tma_buf;                   // elements per tile buffer (a multiple of 16)
+  int tma_extra_tx;              // test hook: bytes a tile's barrier expects beyond its copies (0)
+  uint64_t tma_wait_ns;          // bound of each wait for a tile's copies
 };
 
 // HvdH banded solve: thread per (batch, chunk of L rows + 2H halo rows).
@@ -137,10 +143,19 @@ struct RecipeEntry {
   int mode;      // 0 row load + row store, 1 fused load + row store, 2 fused both
   int radix[6];  // zero-terminated
   int Tf;        // threads per tile column the kernel was built for
+  int nb;        // tile columns the kernel was built for (0: any)
   const void* fn;
 };
 template <typename T, int DIR>
 const RecipeEntry* recipe_table(int* count);
+// Pipelined tensor-copy pass kernels (F32, LOAD_PLAIN, modes 1 and 2; nb =
+// the exact tile column count). Signature:
+// (PassParams, CUtensorMap, float2* out, unsigned* status).
+const RecipeEntry* tma_table(int dir, int* count);
+size_t tma_smem_bytes(const PassParams& pp);
+int tma_prepare(const void* fn, const PassParams& pp);
+cudaError_t tma_launch(const void* fn, const PassParams& pp, const CUtensorMap& map, void* out, unsigned* status,
+                       int grid, cudaStream_t st);
 
 // fn: a recipe kernel (RecipeEntry::fn) or nullptr for the generic kernel.
 // Planner pieces shared by the plan builder and the allocation-free entry
@@ -164,6 +179,7 @@ struct SchedOpts {
   int route = 0;
   int threads_max = 0;
   int precision = 0;
+  int plain_loads = 0;
   bool dry = false;
 };
 extern thread_local SchedOpts g_sched;

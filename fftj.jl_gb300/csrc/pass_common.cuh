@@ -371,7 +371,30 @@ struct Recipe {
 template <typename T>
 __host__ __device__ constexpr int pad_period() { return sizeof(T) == 4 ? 16 : 8; }
 
-template <typename T, int DIR, int r, int S, int Rr, int TF>
+// Tile positions when the tile's column count is a compile-time constant
+// NBC: element (row, column b < NBC) sits at pidx(row * NBC + b), computed
+// as a row part plus a column part, so that two rows a fixed distance apart
+// are a constant offset apart (immediate shared-memory offsets instead of a
+// shift and adds per access). NBC divides the padding period or is a
+// multiple of it.
+template <typename T, int NBC>
+struct Lay {
+  static constexpr int PP = pad_period<T>();
+  static_assert(NBC > 0 && (PP % NBC == 0 || NBC % PP == 0), "column count must divide the padding period or be a multiple of it");
+  static constexpr int RP = NBC >= PP ? 1 : PP / NBC;  // rows per padding period (a power of two)
+  static constexpr int LS = RP == 1 ? 0 : RP == 2 ? 1 : RP == 4 ? 2 : RP == 8 ? 3 : 4;
+  __device__ __forceinline__ static int col(int b) { return NBC >= PP ? b + b / PP : b; }
+  __device__ __forceinline__ static int row(int r) { return NBC >= PP ? r * (NBC + NBC / PP) : r * NBC + (r >> LS); }
+  // row(r0 + d) - row(r0): exact when d or r0 is a multiple of RP
+  __host__ __device__ static constexpr int step(int d) { return NBC >= PP ? d * (NBC + NBC / PP) : d * NBC + d / RP; }
+  __host__ __device__ static constexpr bool exact(int d) { return d % RP == 0; }
+};
+// the layout of NBC columns, or a placeholder when the count is a run-time
+// value (NBC == 0; the callers then take the pidx path)
+template <typename T, int NBC>
+using LayC = Lay<T, NBC == 0 ? 1 : NBC>;
+
+template <typename T, int DIR, int r, int S, int Rr, int TF, int NBC = 0>
 __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b, const int kg, const int NB,
                                             const Cx<T>* __restrict__ twR) {
   constexpr int IPT = (Rr + TF - 1) / TF;
@@ -384,7 +407,11 @@ __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b
     const int k = kg + i * TF;
     if ((i + 1) * TF <= Rr || k < Rr) {
       const int a = k * NB + b;
-      if constexpr (Rr % PP == 0) {
+      if constexpr (NBC > 0 && LayC<T, NBC>::exact(Rr)) {
+        const int base = LayC<T, NBC>::row(k) + LayC<T, NBC>::col(b);
+#pragma unroll
+        for (int j = 0; j < r; ++j) v[i][j] = buf[base + j * LayC<T, NBC>::step(Rr)];
+      } else if constexpr (Rr % PP == 0) {
         const int base = pidx<T>(a), step = jstride_in + jstride_in / PP;
 #pragma unroll
         for (int j = 0; j < r; ++j) v[i][j] = buf[base + j * step];
@@ -403,11 +430,17 @@ __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b
       const int q = k - p * S;
       Dft<T, DIR, r>::run(v[i]);
       const int a = (r * S * p + q) * NB + b;
-      const int base = pidx<T>(a);
+      // compile-time columns: rows r S p + q + j S are constant offsets apart
+      // when S is a multiple of the rows per padding period, or S == 1 and r
+      // is (then the first row r p is one)
+      constexpr bool kLay = NBC > 0 && (LayC<T, NBC>::exact(S) || (S == 1 && LayC<T, NBC>::exact(r)));
+      const int base = kLay ? LayC<T, NBC>::row(r * S * p + q) + LayC<T, NBC>::col(b) : pidx<T>(a);
       const int step = (S % PP == 0) ? jstride_out + jstride_out / PP : 0;
       // position of output j: a constant step when S is a multiple of the
       // padding period, else the padded index of a + j * S * NB
-#define FFTJ_OUT_AT(j) ((S % PP == 0) ? base + (j) * step : pidx<T>(a + (j) * jstride_out))
+#define FFTJ_OUT_AT(j)                                                               \
+  (kLay ? base + LayC<T, NBC>::step((j) * S)                           \
+        : (S % PP == 0) ? base + (j) * step : pidx<T>(a + (j) * jstride_out))
       buf[base] = v[i][0];
       if (Rr == S) {
         // last sub-stage of the pass (L = r): no twiddle
@@ -428,16 +461,16 @@ __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b
   __syncthreads();
 }
 
-template <typename T, int DIR, int TF, int R, int S, int r, int... rest>
+template <typename T, int DIR, int TF, int R, int S, int NBC, int r, int... rest>
 __device__ __forceinline__ void run_subs_ct(Cx<T>* buf, const int b, const int kg, const int NB,
                                             const Cx<T>* twR) {
-  substage_ct<T, DIR, r, S, R / r, TF>(buf, b, kg, NB, twR);
-  if constexpr (sizeof...(rest) > 0) run_subs_ct<T, DIR, TF, R, S * r, rest...>(buf, b, kg, NB, twR);
+  substage_ct<T, DIR, r, S, R / r, TF, NBC>(buf, b, kg, NB, twR);
+  if constexpr (sizeof...(rest) > 0) run_subs_ct<T, DIR, TF, R, S * r, NBC, rest...>(buf, b, kg, NB, twR);
 }
 template <typename T, int DIR, int... Rs>
 __device__ __forceinline__ void run_recipe(Recipe<Rs...>*, Cx<T>* buf, const int b, const int kg, const int NB,
                                            const Cx<T>* twR) {
-  run_subs_ct<T, DIR, Recipe<Rs...>::Tf, Recipe<Rs...>::R, 1, Rs...>(buf, b, kg, NB, twR);
+  run_subs_ct<T, DIR, Recipe<Rs...>::Tf, Recipe<Rs...>::R, 1, 0, Rs...>(buf, b, kg, NB, twR);
 }
 
 // ---------------------------------------------------------------------------
@@ -853,22 +886,153 @@ __device__ __forceinline__ Cx<T> load_elem_off(const PassParams& pp, const void*
 
 // sub-stages 2 .. NS-DROP of a recipe (the first ran fused with the load;
 // DROP = 1 leaves the last one to the fused store)
-template <typename T, int DIR, int TF, int R, int S, int DROP, int r, int... rest>
+template <typename T, int DIR, int TF, int R, int S, int DROP, int NBC, int r, int... rest>
 __device__ __forceinline__ void run_mid_skip(Cx<T>* buf, const int b, const int kg, const int NB,
                                              const Cx<T>* twR) {
   if constexpr (sizeof...(rest) >= DROP) {
     if constexpr (sizeof...(rest) == 0) {
-      substage_ct<T, DIR, r, S, R / r, TF>(buf, b, kg, NB, twR);
+      substage_ct<T, DIR, r, S, R / r, TF, NBC>(buf, b, kg, NB, twR);
     } else {
-      substage_ct<T, DIR, r, S, R / r, TF>(buf, b, kg, NB, twR);
-      run_mid_skip<T, DIR, TF, R, S * r, DROP, rest...>(buf, b, kg, NB, twR);
+      substage_ct<T, DIR, r, S, R / r, TF, NBC>(buf, b, kg, NB, twR);
+      run_mid_skip<T, DIR, TF, R, S * r, DROP, NBC, rest...>(buf, b, kg, NB, twR);
     }
   }
 }
-template <typename T, int DIR, int TF, int R, int S1, int DROP, int r0, int... rest>
+template <typename T, int DIR, int TF, int R, int S1, int DROP, int NBC, int r0, int... rest>
 __device__ __forceinline__ void run_mid_ct(Cx<T>* buf, const int b, const int kg, const int NB,
                                            const Cx<T>* twR) {
-  if constexpr (sizeof...(rest) > 0) run_mid_skip<T, DIR, TF, R, S1, DROP, rest...>(buf, b, kg, NB, twR);
+  if constexpr (sizeof...(rest) > 0) run_mid_skip<T, DIR, TF, R, S1, DROP, NBC, rest...>(buf, b, kg, NB, twR);
+}
+
+// Fused last sub-stage (radix rL) + HBM store of one tile of a multi-pass
+// transform: MODE 1 is the row store of a first pass (s == 1), MODE 2 the
+// strided store of a later pass. Shared by the one-tile-per-CTA recipe
+// kernels and the pipelined tensor-copy kernel (pass_tma.cuh).
+template <typename T, int DIR, int MODE, int NBC, int... Rs>
+__device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restrict__ out,
+                                           const Cx<T>* __restrict__ buf, const int tid, const int nthr,
+                                           const int kg, const int b, const int64_t b0, const int64_t p0,
+                                           const int64_t q0, const int ql, const int64_t batch,
+                                           const int64_t pcol, const bool colok) {
+  using Rec = Recipe<Rs...>;
+  constexpr int R = Rec::R, TF = Rec::Tf, NS = Rec::n;
+  constexpr int rad[] = {Rs...};
+  constexpr int rL = rad[NS - 1];
+  const int NB = NBC > 0 ? NBC : pp.NB;
+  const bool scaled = not_one(pp.scale);
+  const T sc = (T)pp.scale;
+  const bool tw = pp.tw_mode != 0;
+  if constexpr (MODE == 1) {
+    // ---- fused last sub-stage (radix rL) + row store (s == 1). Butterfly
+    // u = c S + k takes k fastest across lanes, so for each output
+    // j = k + jj S the lanes of a warp write consecutive addresses of column
+    // c's output row. F32: the outer twiddle w^((p0 + c) j) advances along
+    // jj by w^((p0 + c) S), one complex multiply per output instead of a
+    // table lookup (at most rL - 1 <= 15 steps); F64 passes are FP64-pipe
+    // bound and keep the lookups.
+    static_assert(NS >= 2, "a first pass has at least two sub-stages");
+    constexpr int S = R / rL;
+    constexpr bool kRecur = sizeof(T) == 4;
+    const int nbf = NB * S;
+    if (b0 < pp.nbatch) {
+      Cx<T>* orow = out + b0 * pp.out_bstride + (int64_t)R * p0;
+      for (int u = tid; u < nbf; u += nthr) {
+        const int c = u / S;
+        const int k = u - c * S;
+        Cx<T> v[rL];
+        if constexpr (NBC > 0 && LayC<T, NBC>::exact(S)) {
+          const int base = LayC<T, NBC>::row(k) + LayC<T, NBC>::col(c);
+#pragma unroll
+          for (int j = 0; j < rL; ++j) v[j] = buf[base + j * LayC<T, NBC>::step(S)];
+        } else {
+#pragma unroll
+          for (int j = 0; j < rL; ++j) v[j] = buf[pidx<T>((k + j * S) * NB + c)];
+        }
+        Dft<T, DIR, rL>::run(v);
+        const uint32_t pc = (uint32_t)(p0 + c);
+        uint32_t e = pc * (uint32_t)k;
+        const uint32_t estep = pc * (uint32_t)S;
+        Cx<T> w = mk<T>(1, 0), wstep = mk<T>(1, 0);
+        if (kRecur && tw) {
+          if (e != 0) w = outer_tw<T>(pp, e);
+          if (estep != 0) wstep = outer_tw<T>(pp, estep);
+        }
+        Cx<T>* o = orow + (int64_t)R * c + k;
+#pragma unroll
+        for (int j = 0; j < rL; ++j) {
+          Cx<T> x = v[j];
+          if (kRecur) {
+            if (tw) {
+              x = cmul(x, w);
+              w = cmul(w, wstep);
+            }
+          } else if (tw && e != 0) {
+            x = cmul(x, outer_tw<T>(pp, e));
+          }
+          if (scaled) { x.x *= sc; x.y *= sc; }
+          o[j * S] = x;
+          e += estep;
+        }
+      }
+    }
+  } else {
+    // ---- fused last sub-stage (radix rL, L = rL, no inner twiddle) + store:
+    // butterfly k (< S = R/rL) writes positions j*S + k of its column
+    constexpr int S = R / rL;
+    constexpr int IPT = (S + TF - 1) / TF;
+    Cx<T> v[IPT][rL];
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) {
+      const int k = kg + i * TF;
+      if ((i + 1) * TF <= S || k < S) {
+        if constexpr (NBC > 0 && LayC<T, NBC>::exact(S)) {
+          const int base = LayC<T, NBC>::row(k) + LayC<T, NBC>::col(b);
+#pragma unroll
+          for (int j = 0; j < rL; ++j) v[i][j] = buf[base + j * LayC<T, NBC>::step(S)];
+        } else {
+#pragma unroll
+          for (int j = 0; j < rL; ++j) v[i][j] = buf[pidx<T>((k + j * S) * NB + b)];
+        }
+      }
+    }
+    if (colok) {
+      Cx<T>* ob = out + batch * pp.out_bstride + (int64_t)R * pp.s * pcol + q0 + ql;
+      const int64_t jstep = (int64_t)S * pp.s;
+      const uint32_t estep = (uint32_t)pcol * (uint32_t)S;
+      // F32: along a butterfly's outputs the outer twiddle w^(pcol (k + j S))
+      // advances by w^(pcol S), one complex multiply per output instead of a
+      // table lookup (at most rL - 1 <= 15 steps of rounding). F64 passes are
+      // FP64-pipe bound and keep the lookups.
+      constexpr bool kRecur = sizeof(T) == 4;
+      const Cx<T> wstep = (kRecur && tw && estep != 0) ? outer_tw<T>(pp, estep) : mk<T>(1, 0);
+#pragma unroll
+      for (int i = 0; i < IPT; ++i) {
+        const int k = kg + i * TF;
+        if ((i + 1) * TF <= S || k < S) {
+          Dft<T, DIR, rL>::run(v[i]);
+          Cx<T>* o = ob + (int64_t)k * pp.s;
+          uint32_t e = (uint32_t)pcol * (uint32_t)k;
+          Cx<T> w = (kRecur && tw && e != 0) ? outer_tw<T>(pp, e) : mk<T>(1, 0);
+#pragma unroll
+          for (int j = 0; j < rL; ++j) {
+            Cx<T> x = v[i][j];
+            if (kRecur) {
+              if (tw) {
+                x = cmul(x, w);
+                w = cmul(w, wstep);
+              }
+            } else if (tw && e != 0) {
+              x = cmul(x, outer_tw<T>(pp, e));
+            }
+            if (scaled) { x.x *= sc; x.y *= sc; }
+            *o = x;
+            o += jstep;
+            e += estep;
+          }
+        }
+      }
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -879,7 +1043,7 @@ __device__ __forceinline__ void run_mid_ct(Cx<T>* buf, const int b, const int kg
 // (later passes: lanes walk the contiguous q columns on both sides).
 // No per-element 64-bit multiply or multiply-high: addresses and (column,
 // row) counters advance by additions.
-template <typename T, int DIR, int LOADOP, int MODE, int... Rs>
+template <typename T, int DIR, int LOADOP, int MODE, int NBC, int... Rs>
 __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __restrict__ in,
                                            Cx<T>* __restrict__ out) {
   using Rec = Recipe<Rs...>;
@@ -895,10 +1059,10 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
   const uint32_t tb = pp.ftp.div(t1);
   const uint32_t tp = t1 - tb * pp.tiles_p;
   const int64_t q0 = (int64_t)tq * pp.Q, p0 = (int64_t)tp * pp.P, b0 = (int64_t)tb * pp.NBt;
-  const int P = pp.P, Q = pp.Q, NB = pp.NB;
+  const int P = pp.P, Q = pp.Q, NB = NBC > 0 ? NBC : pp.NB;
   const int E = NB * R;
-  const int tid = threadIdx.x, nthr = blockDim.x;
-  const int kg = (int)pp.fNB.div((uint32_t)tid);
+  const int tid = threadIdx.x, nthr = NBC > 0 ? NBC * TF : (int)blockDim.x;
+  const int kg = NBC > 0 ? tid / NBC : (int)pp.fNB.div((uint32_t)tid);
   const int b = tid - kg * NB;
   const int cq = (int)pp.fQ.div((uint32_t)b);
   const int ql = b - cq * Q;
@@ -955,7 +1119,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
     __syncthreads();
     if constexpr (NS > 2) {
       // middle sub-stages (the last one is fused into the row store)
-      run_mid_ct<T, DIR, TF, R, r0, 1, Rs...>(buf, b, kg, NB, twR);
+      run_mid_ct<T, DIR, TF, R, r0, 1, NBC, Rs...>(buf, b, kg, NB, twR);
     }
   } else if constexpr (MODE == 0) {
     // ---- row load (lanes walk j): e = tid + i*nthr -> (c, j), c = column
@@ -985,7 +1149,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
       }
     }
     __syncthreads();
-    run_subs_ct<T, DIR, TF, R, 1, Rs...>(buf, b, kg, NB, twR);
+    run_subs_ct<T, DIR, TF, R, 1, NBC, Rs...>(buf, b, kg, NB, twR);
   } else {
     // ---- fused load + first sub-stage (radix r0, S = 1): butterfly k reads
     // column positions k + j*R/r0 straight from HBM
@@ -1016,74 +1180,33 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
       if ((i + 1) * TF <= Rr || k < Rr) {
         Dft<T, DIR, r0>::run(v[i]);
         const int a = r0 * k * NB + b;
-        buf[pidx<T>(a)] = v[i][0];
+        // compile-time columns: output rows r0 k + j are constant offsets
+        // from row r0 k (a multiple of the rows per padding period)
+        constexpr bool kLay = NBC > 0 && LayC<T, NBC>::exact(r0);
+        const int base = kLay ? LayC<T, NBC>::row(r0 * k) + LayC<T, NBC>::col(b) : pidx<T>(a);
+        buf[base] = v[i][0];
 #pragma unroll
         for (int j = 1; j < r0; ++j) {
           Cx<T> w = v[i][j];
           if (NS > 1 && k != 0) w = cmul(w, twR[j * k]);
-          buf[pidx<T>(a + j * NB)] = w;
+          buf[kLay ? base + LayC<T, NBC>::step(j) : pidx<T>(a + j * NB)] = w;
         }
       }
     }
     __syncthreads();
     if constexpr (NS > 2) {
       // middle sub-stages (the last one is fused into the store)
-      run_mid_ct<T, DIR, TF, R, r0, 1, Rs...>(buf, b, kg, NB, twR);
+      run_mid_ct<T, DIR, TF, R, r0, 1, NBC, Rs...>(buf, b, kg, NB, twR);
     }
   }
 
+  if constexpr (MODE == 1 || MODE == 2) {
+    store_last<T, DIR, MODE, NBC, Rs...>(pp, out, buf, tid, nthr, kg, b, b0, p0, q0, ql, batch, pcol, colok);
+    return;
+  }
   const bool scaled = not_one(pp.scale);
   const T sc = (T)pp.scale;
   const bool tw = pp.tw_mode != 0;
-  if constexpr (MODE == 1) {
-    // ---- fused last sub-stage (radix rL) + row store (s == 1). Butterfly
-    // u = c S + k takes k fastest across lanes, so for each output
-    // j = k + jj S the lanes of a warp write consecutive addresses of column
-    // c's output row. F32: the outer twiddle w^((p0 + c) j) advances along
-    // jj by w^((p0 + c) S), one complex multiply per output instead of a
-    // table lookup (at most rL - 1 <= 15 steps); F64 passes are FP64-pipe
-    // bound and keep the lookups.
-    static_assert(NS >= 2, "a first pass has at least two sub-stages");
-    constexpr int S = R / rL;
-    constexpr bool kRecur = sizeof(T) == 4;
-    const int nbf = NB * S;
-    if (b0 < pp.nbatch) {
-      Cx<T>* orow = out + b0 * pp.out_bstride + (int64_t)R * p0;
-      for (int u = tid; u < nbf; u += nthr) {
-        const int c = u / S;
-        const int k = u - c * S;
-        Cx<T> v[rL];
-#pragma unroll
-        for (int j = 0; j < rL; ++j) v[j] = buf[pidx<T>((k + j * S) * NB + c)];
-        Dft<T, DIR, rL>::run(v);
-        const uint32_t pc = (uint32_t)(p0 + c);
-        uint32_t e = pc * (uint32_t)k;
-        const uint32_t estep = pc * (uint32_t)S;
-        Cx<T> w = mk<T>(1, 0), wstep = mk<T>(1, 0);
-        if (kRecur && tw) {
-          if (e != 0) w = outer_tw<T>(pp, e);
-          if (estep != 0) wstep = outer_tw<T>(pp, estep);
-        }
-        Cx<T>* o = orow + (int64_t)R * c + k;
-#pragma unroll
-        for (int j = 0; j < rL; ++j) {
-          Cx<T> x = v[j];
-          if (kRecur) {
-            if (tw) {
-              x = cmul(x, w);
-              w = cmul(w, wstep);
-            }
-          } else if (tw && e != 0) {
-            x = cmul(x, outer_tw<T>(pp, e));
-          }
-          if (scaled) { x.x *= sc; x.y *= sc; }
-          o[j * S] = x;
-          e += estep;
-        }
-      }
-    }
-    return;
-  }
   if constexpr (MODE == 0 && NS >= 2) {
     // ---- fused last sub-stage (radix rL) + row store: butterfly u = c S + k
     // with k fastest across lanes writes outputs k + jj S of row c, the
@@ -1138,66 +1261,15 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
       j += dj; c += dc;
       if (j >= R) { j -= R; c++; }
     }
-  } else if constexpr (MODE == 2) {
-    // ---- fused last sub-stage (radix rL, L = rL, no inner twiddle) + store:
-    // butterfly k (< S = R/rL) writes positions j*S + k of its column
-    constexpr int S = R / rL;
-    constexpr int IPT = (S + TF - 1) / TF;
-    Cx<T> v[IPT][rL];
-#pragma unroll
-    for (int i = 0; i < IPT; ++i) {
-      const int k = kg + i * TF;
-      if ((i + 1) * TF <= S || k < S) {
-#pragma unroll
-        for (int j = 0; j < rL; ++j) v[i][j] = buf[pidx<T>((k + j * S) * NB + b)];
-      }
-    }
-    if (colok) {
-      Cx<T>* ob = out + batch * pp.out_bstride + (int64_t)R * pp.s * pcol + q0 + ql;
-      const int64_t jstep = (int64_t)S * pp.s;
-      const uint32_t estep = (uint32_t)pcol * (uint32_t)S;
-      // F32: along a butterfly's outputs the outer twiddle w^(pcol (k + j S))
-      // advances by w^(pcol S), one complex multiply per output instead of a
-      // table lookup (at most rL - 1 <= 15 steps of rounding). F64 passes are
-      // FP64-pipe bound and keep the lookups.
-      constexpr bool kRecur = sizeof(T) == 4;
-      const Cx<T> wstep = (kRecur && tw && estep != 0) ? outer_tw<T>(pp, estep) : mk<T>(1, 0);
-#pragma unroll
-      for (int i = 0; i < IPT; ++i) {
-        const int k = kg + i * TF;
-        if ((i + 1) * TF <= S || k < S) {
-          Dft<T, DIR, rL>::run(v[i]);
-          Cx<T>* o = ob + (int64_t)k * pp.s;
-          uint32_t e = (uint32_t)pcol * (uint32_t)k;
-          Cx<T> w = (kRecur && tw && e != 0) ? outer_tw<T>(pp, e) : mk<T>(1, 0);
-#pragma unroll
-          for (int j = 0; j < rL; ++j) {
-            Cx<T> x = v[i][j];
-            if (kRecur) {
-              if (tw) {
-                x = cmul(x, w);
-                w = cmul(w, wstep);
-              }
-            } else if (tw && e != 0) {
-              x = cmul(x, outer_tw<T>(pp, e));
-            }
-            if (scaled) { x.x *= sc; x.y *= sc; }
-            *o = x;
-            o += jstep;
-            e += estep;
-          }
-        }
-      }
-    }
   }
 }
 
-template <typename T, int DIR, int LOADOP, int MODE, class Rec>
+template <typename T, int DIR, int LOADOP, int MODE, int NBC, class Rec>
 struct FusedLaunch;
-template <typename T, int DIR, int LOADOP, int MODE, int... Rs>
-struct FusedLaunch<T, DIR, LOADOP, MODE, Recipe<Rs...>> {
+template <typename T, int DIR, int LOADOP, int MODE, int NBC, int... Rs>
+struct FusedLaunch<T, DIR, LOADOP, MODE, NBC, Recipe<Rs...>> {
   __device__ __forceinline__ static void run(const PassParams& pp, const void* in, Cx<T>* out) {
-    pass_fused<T, DIR, LOADOP, MODE, Rs...>(pp, in, out);
+    pass_fused<T, DIR, LOADOP, MODE, NBC, Rs...>(pp, in, out);
   }
 };
 

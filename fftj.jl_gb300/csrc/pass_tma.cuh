@@ -1,0 +1,213 @@
+// Pipelined pass kernel for F32 multi-pass transforms: the tile columns of a
+// pass are contiguous in HBM row by row (MODE 1: first passes, columns p;
+// MODE 2: later passes, columns q), so a tile is a box of a tensor and
+// arrives in shared memory by TMA tensor copies (cp.async.bulk.tensor)
+// completing on an mbarrier. Each CTA is persistent and double-buffered:
+// while it transforms tile i in one buffer, the copy of its next tile lands
+// in the other, so HBM reads overlap the in-CTA sub-stages instead of
+// waiting for them.
+//
+// Per tile the work is that of the one-tile-per-CTA recipe kernel
+// (pass_fused, the Stockham pass of FFTJ's src/stockham.jl:26-76 with radix
+// R): the first sub-stage reads the dense tile the copy left in shared memory
+// and writes it back in place in the padded layout, the middle sub-stages run
+// in shared memory, and the last one is fused into the HBM store with the
+// outer twiddle (store_last).
+//
+// Every wait is bounded: a copy that has not landed after the plan's wait
+// limit sets a status word the host reads (fftj_plan_status), and the CTA
+// waits (again bounded) for its copies in flight and returns.
+#pragma once
+#include <cuda.h>
+
+#include "pass_common.cuh"
+
+namespace fftj {
+
+__device__ __forceinline__ uint32_t sh_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sh_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sh_addr(bar)), "r"(bytes) : "memory");
+}
+// true once the barrier's phase of this parity has completed
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(sh_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ uint64_t ns_now() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits for the phase of the given parity; false after limit_ns nanoseconds.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+  if (mbar_test(bar, parity)) return true;
+  const uint64_t t0 = ns_now();
+  for (;;) {
+    for (int i = 0; i < 16; ++i)
+      if (mbar_test(bar, parity)) return true;
+    if (ns_now() - t0 > limit_ns) return false;
+  }
+}
+__device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(sh_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(sh_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load4(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                          int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(sh_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(sh_addr(bar))
+      : "memory");
+}
+
+// MODE 1: tile = P consecutive columns p (Q == 1, one batch entry), tensor
+// (p, j, batch); MODE 2: tile = Q consecutive columns q (P == 1, one batch
+// entry), tensor (q, p, j, batch). NBC = the tile's column count.
+template <int DIR, int MODE, int NBC, int... Rs>
+__device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap* map, Cx<float>* __restrict__ out,
+                                         unsigned* status) {
+  using T = float;
+  using Rec = Recipe<Rs...>;
+  using L = LayC<T, NBC>;
+  constexpr int R = Rec::R, TF = Rec::Tf, NS = Rec::n;
+  constexpr int rad[] = {Rs...};
+  constexpr int r0 = rad[0];
+  constexpr int Rr = R / r0;
+  constexpr int IPT = (Rr + TF - 1) / TF;
+  constexpr int NB = NBC;
+  constexpr int nthr = NBC * TF;
+  constexpr uint32_t kTx = (uint32_t)(NB * R * sizeof(Cx<T>));
+  static_assert(NS >= 2, "a pass of a multi-pass transform has at least two sub-stages");
+  // box copies land 16-byte aligned: dynamic shared memory starts 16-byte
+  // aligned and buffers are multiples of 128 bytes
+  extern __shared__ __align__(16) unsigned char tma_smem[];
+  Cx<T>* const sbase = reinterpret_cast<Cx<T>*>(tma_smem);
+  const int bufE = pp.tma_buf;  // elements per buffer, a multiple of 16 (128 bytes)
+  Cx<T>* const twS = sbase + 2 * bufE;
+  uint64_t* const bar = reinterpret_cast<uint64_t*>(twS + R);
+  const int tid = threadIdx.x;
+  const int kg = tid / NB;
+  const int b = tid - kg * NB;
+  const uint32_t ntiles = pp.tiles_q * pp.tiles_p * pp.tiles_b;
+  const int rows = pp.tma_rows;
+  const uint64_t limit = pp.tma_wait_ns;
+  {
+    const Cx<T>* twG = reinterpret_cast<const Cx<T>*>(pp.twR);
+    for (int t = tid; t < R; t += nthr) twS[t] = __ldg(twG + t);
+  }
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    mbar_init(bar + 1, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  // one thread arms the slot's barrier with the tile's bytes and issues the
+  // tile's box copies (R / rows boxes of NB x rows elements)
+  auto issue = [&](uint32_t tile, int slot) {
+    const uint32_t t1 = pp.ftq.div(tile);
+    const uint32_t tq = tile - t1 * pp.tiles_q;
+    const uint32_t tb = pp.ftp.div(t1);
+    const uint32_t tp = t1 - tb * pp.tiles_p;
+    Cx<T>* dst = sbase + slot * bufE;
+    mbar_arrive_expect_tx(bar + slot, kTx + (uint32_t)pp.tma_extra_tx);
+    for (int j0 = 0; j0 < R; j0 += rows) {
+      if constexpr (MODE == 1)
+        tma_load3(dst + j0 * NB, map, bar + slot, (int)(tp * (uint32_t)pp.P), j0, (int)tb);
+      else
+        tma_load4(dst + j0 * NB, map, bar + slot, (int)(tq * (uint32_t)pp.Q), (int)tp, j0, (int)tb);
+    }
+  };
+  if (tid == 0 && blockIdx.x < ntiles) issue(blockIdx.x, 0);
+  uint32_t it = 0;
+  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const int slot = (int)(it & 1);
+    Cx<T>* const buf = sbase + slot * bufE;
+    const uint32_t nxt = tile + gridDim.x;
+    if (tid == 0 && nxt < ntiles) {
+      // the other buffer was last read (generic proxy) before the barrier
+      // that ended the previous tile; order those reads before the copy
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(nxt, slot ^ 1);
+    }
+    const bool ok = mbar_wait(bar + slot, (it >> 1) & 1, limit);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicOr(status, 1u);
+        mbar_wait(bar + slot, (it >> 1) & 1, limit);
+        if (nxt < ntiles) mbar_wait(bar + (slot ^ 1), ((it + 1) >> 1) & 1, limit);
+      }
+      __syncthreads();
+      return;
+    }
+    const uint32_t t1 = pp.ftq.div(tile);
+    const uint32_t tq = tile - t1 * pp.tiles_q;
+    const uint32_t tb = pp.ftp.div(t1);
+    const uint32_t tp = t1 - tb * pp.tiles_p;
+    const int64_t q0 = (int64_t)tq * pp.Q, p0 = (int64_t)tp * pp.P, b0 = (int64_t)tb;
+    const int ql = MODE == 2 ? b : 0;
+    const int64_t pcol = MODE == 1 ? p0 + b : p0;
+    const bool colok = b0 < pp.nbatch && q0 + ql < pp.s;
+
+    // ---- first sub-stage (radix r0, S = 1) from the dense tile, written
+    // back in place in the padded layout
+    Cx<T> v[IPT][r0];
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) {
+      const int k = kg + i * TF;
+      if ((i + 1) * TF <= Rr || k < Rr) {
+        const Cx<T>* src = buf + k * NB + b;
+#pragma unroll
+        for (int j = 0; j < r0; ++j) v[i][j] = src[j * Rr * NB];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) {
+      const int k = kg + i * TF;
+      if ((i + 1) * TF <= Rr || k < Rr) {
+        Dft<T, DIR, r0>::run(v[i]);
+        constexpr bool kLay = L::exact(r0);
+        const int a = r0 * k * NB + b;
+        const int base = kLay ? L::row(r0 * k) + L::col(b) : pidx<T>(a);
+        buf[base] = v[i][0];
+#pragma unroll
+        for (int j = 1; j < r0; ++j) {
+          Cx<T> w = v[i][j];
+          if (k != 0) w = cmul(w, twS[j * k]);
+          buf[kLay ? base + L::step(j) : pidx<T>(a + j * NB)] = w;
+        }
+      }
+    }
+    __syncthreads();
+    if constexpr (NS > 2) run_mid_ct<T, DIR, TF, R, r0, 1, NBC, Rs...>(buf, b, kg, NB, twS);
+    store_last<T, DIR, MODE, NBC, Rs...>(pp, out, buf, tid, nthr, kg, b, b0, p0, q0, ql, b0, pcol, colok);
+    __syncthreads();  // the buffer is free for the copy after next
+  }
+}
+
+template <int DIR, int MODE, int NBC, class Rec>
+struct TmaLaunch;
+template <int DIR, int MODE, int NBC, int... Rs>
+struct TmaLaunch<DIR, MODE, NBC, Recipe<Rs...>> {
+  __device__ __forceinline__ static void run(const PassParams& pp, const CUtensorMap* map, Cx<float>* out,
+                                             unsigned* status) {
+    pass_tma<DIR, MODE, NBC, Rs...>(pp, map, out, status);
+  }
+};
+
+}  // namespace fftj

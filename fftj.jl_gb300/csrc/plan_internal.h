@@ -3,6 +3,7 @@
 // elementwise kernels) wired between the caller's in/out buffers and two
 // plan-owned workspaces.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <vector>
@@ -29,6 +30,13 @@ struct Op {
   fftj::CopyParams cp;
   fftj::SolveParams sv;
   size_t dst_bytes = 0;  // bytes written (for workspace sizing)
+  // pipelined tensor-copy kernel of an F32 pass (nullptr: none); its tensor
+  // map is encoded for the source address tmap_src on first use
+  const void* kfn_tma = nullptr;
+  int tma_mode = 0;  // 1: columns p (first pass), 2: columns q (later pass)
+  int tma_grid = 0;  // CTAs resident at once (the persistent grid)
+  CUtensorMap tmap;
+  const void* tmap_src = nullptr;
 };
 
 struct fftj_plan_s {
@@ -46,7 +54,10 @@ struct fftj_plan_s {
   bool dry = false;
   int npasses = 0;
   std::vector<int> pass_R;
+  int plain_loads = 0;            // opts.plain_loads
+  unsigned* d_status = nullptr;   // pipelined kernels' wait status (0: every wait ended)
   ~fftj_plan_s() {
+    if (d_status) cudaFree(d_status);
     for (auto& t : tables)
       if (t.p && t.bytes) cudaFree(t.p);
     for (auto& w : ws)

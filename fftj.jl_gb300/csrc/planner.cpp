@@ -648,15 +648,19 @@ const void* pick_pass_kernel_t(int dir, const PassParams& pp) {
   if (pp.load_rows && pp.store_rows && (pp.NBt == 1 || pp.out_bstride == (int64_t)pp.R)) mode = 0;
   else if (!pp.load_rows && pp.store_rows && pp.NBt == 1) mode = 1;
   else if (!pp.load_rows && !pp.store_rows) mode = 2;
-  for (int i = 0; i < count && mode >= 0; ++i) {
-    const RecipeEntry& e = tab[i];
-    if (e.mode != mode || e.load_op != pp.load_op || e.Tf != pp.Tf) continue;
-    int n = 0;
-    while (n < 6 && e.radix[n]) n++;
-    if (n != pp.nsub) continue;
-    bool same = true;
-    for (int j = 0; j < n; ++j) same = same && e.radix[j] == pp.sub[j].r;
-    if (same) return e.fn;
+  // a kernel built for the tile's exact column count first, then any
+  for (int want_nb = 1; want_nb >= 0; --want_nb) {
+    for (int i = 0; i < count && mode >= 0; ++i) {
+      const RecipeEntry& e = tab[i];
+      if (e.mode != mode || e.load_op != pp.load_op || e.Tf != pp.Tf) continue;
+      if (want_nb ? e.nb != pp.NB : e.nb != 0) continue;
+      int n = 0;
+      while (n < 6 && e.radix[n]) n++;
+      if (n != pp.nsub) continue;
+      bool same = true;
+      for (int j = 0; j < n; ++j) same = same && e.radix[j] == pp.sub[j].r;
+      if (same) return e.fn;
+    }
   }
   return nullptr;
 }
@@ -1345,8 +1349,100 @@ int check_dims(int rank, const int64_t* dims, std::vector<i64>* out) {
 // opt it into its shared memory.
 // Pick each pass's kernel (compile-time recipe or generic) and opt it into
 // its shared memory.
+// The pipelined tensor-copy kernel of an F32 pass, when the pass's tile is
+// a box of its input tensor: columns contiguous in HBM row by row (first
+// passes: P columns p, one batch entry; later passes: Q columns q, P = 1,
+// one batch entry), an even column count (16-byte box rows) and even
+// strides (16-byte tensor strides). The source address is checked at launch.
+void pick_tma(Op& op, bool dry) {
+  const PassParams& pp = op.pp;
+  if (pp.load_op != LOAD_PLAIN || pp.NBt != 1) return;
+  int mode = 0;
+  if (!pp.load_rows && pp.store_rows && pp.Q == 1) mode = 1;
+  else if (!pp.load_rows && !pp.store_rows && pp.P == 1) mode = 2;
+  if (!mode) return;
+  const i64 cols = mode == 1 ? pp.P : pp.Q;
+  if (cols != pp.NB || cols % 2 || cols > 256) return;
+  // the last pass of a two-sub-stage radix with 128-byte tile rows keeps
+  // plain loads: its in-CTA work is short, and four one-tile CTAs per SM
+  // keep more reads in flight than three pipelined ones (measured on the
+  // radix-256 last passes of 2^26 and 2^25 x 4: 0.92-0.96 vs 0.84-0.87 of HBM)
+  if (pp.m == 1 && pp.nsub == 2 && cols * 8 <= 128) return;
+  if ((mode == 1 ? pp.m : pp.s) % 2) return;
+  if (pp.nbatch > 1 && (pp.in_bstride % 2 || pp.in_bstride < pp.ncur)) return;
+  int count = 0;
+  const RecipeEntry* tab = tma_table(op.dir, &count);
+  const void* fn = nullptr;
+  for (int i = 0; i < count && !fn; ++i) {
+    const RecipeEntry& e = tab[i];
+    if (e.dir != op.dir || e.mode != mode || e.nb != pp.NB || e.Tf != pp.Tf) continue;
+    int n = 0;
+    while (n < 6 && e.radix[n]) n++;
+    bool same = n == pp.nsub;
+    for (int j = 0; j < n && same; ++j) same = e.radix[j] == pp.sub[j].r;
+    if (same) fn = e.fn;
+  }
+  if (!fn) return;
+  op.pp.tma_rows = (int)largest_divisor_le(pp.R, 256);
+  op.pp.tma_buf = (pp.smem_elems + 15) / 16 * 16;
+  op.pp.tma_wait_ns = 1000000000ull;
+  op.pp.tma_extra_tx = 0;
+  if (!dry) {
+    op.tma_grid = tma_prepare(fn, op.pp);
+    if (op.tma_grid <= 0) return;
+  }
+  op.kfn_tma = fn;
+  op.tma_mode = mode;
+  op.tmap_src = nullptr;
+}
+
+using TensorEncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+TensorEncodeFn tensor_encode_fn() {
+  static TensorEncodeFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (TensorEncodeFn) nullptr;
+    return (TensorEncodeFn)p;
+  }();
+  return fn;
+}
+
+// Tensor map of a pipelined pass's input at `src` (8-byte complex elements
+// copied as opaque 64-bit words): first passes (p, j, batch), later passes
+// (q, p, j, batch); boxes of one tile's columns x tma_rows rows.
+bool encode_tma(Op& op, const void* src) {
+  const TensorEncodeFn enc = tensor_encode_fn();
+  if (!enc) return false;
+  const PassParams& pp = op.pp;
+  const cuuint64_t bstr = (cuuint64_t)(pp.nbatch > 1 ? pp.in_bstride : pp.ncur) * 8;
+  cuuint64_t dims[4], strides[3];
+  cuuint32_t box[4], es[4] = {1, 1, 1, 1};
+  cuuint32_t rank;
+  if (op.tma_mode == 1) {
+    rank = 3;
+    dims[0] = (cuuint64_t)pp.m; dims[1] = (cuuint64_t)pp.R; dims[2] = (cuuint64_t)pp.nbatch;
+    strides[0] = (cuuint64_t)pp.m * 8; strides[1] = bstr;
+    box[0] = (cuuint32_t)pp.P; box[1] = (cuuint32_t)pp.tma_rows; box[2] = 1;
+  } else {
+    rank = 4;
+    dims[0] = (cuuint64_t)pp.s; dims[1] = (cuuint64_t)pp.m; dims[2] = (cuuint64_t)pp.R; dims[3] = (cuuint64_t)pp.nbatch;
+    strides[0] = (cuuint64_t)pp.s * 8; strides[1] = (cuuint64_t)(pp.m * pp.s) * 8; strides[2] = bstr;
+    box[0] = (cuuint32_t)pp.Q; box[1] = 1; box[2] = (cuuint32_t)pp.tma_rows; box[3] = 1;
+  }
+  return enc(&op.tmap, CU_TENSOR_MAP_DATA_TYPE_UINT64, rank, const_cast<void*>(src), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <typename T>
 int finalize_passes(fftj_plan_s* P) {
+  P->plain_loads = g_sched.plain_loads;
+  bool any_tma = false;
   for (auto& op : P->ops) {
     if (op.kind != OP_PASS) continue;
     // the precision form's tensor-core sub-stage lives in the run-time
@@ -1354,8 +1450,15 @@ int finalize_passes(fftj_plan_s* P) {
     if (op.pp.tc && !has_tc16_substage(op.pp)) op.pp.tc = 0;
     op.kfn = op.pp.tc ? nullptr : pick_pass_kernel(sizeof(T) == 8, op.dir, op.pp);
     op.pp.smem_tw_elems = stage_inner_twiddles(op.pp, op.kfn != nullptr) ? op.pp.R : 0;
+    if (sizeof(T) == 4 && op.kfn && !op.pp.tc && !P->plain_loads) pick_tma(op, P->dry);
+    any_tma = any_tma || op.kfn_tma != nullptr;
     if (P->dry) continue;
     if (prepare_pass<T>(op.pp, op.dir, op.kfn) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
+  }
+  if (any_tma && !P->dry) {
+    if (cudaMalloc(&P->d_status, sizeof(unsigned)) != cudaSuccess ||
+        cudaMemset(P->d_status, 0, sizeof(unsigned)) != cudaSuccess)
+      return fail(FFTJ_ERR_CUDA, "status word allocation failed");
   }
   return FFTJ_OK;
 }
@@ -1388,6 +1491,7 @@ struct SchedScope {
     g_sched.threads_max = o->threads_max;
     g_sched.dry = o->dry != 0;
     g_sched.precision = (o->precision >= 0 && o->precision <= 2) ? o->precision : 0;
+    g_sched.plain_loads = o->plain_loads != 0 ? 1 : 0;
   }
   ~SchedScope() { g_sched = SchedOpts(); }
 };
@@ -1504,10 +1608,19 @@ int fftj_plan_c2r_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, i
 
 // Launch op i of a plan (src/dst resolved from the plan's buffer ids).
 static cudaError_t launch_op(fftj_plan_s* P, size_t i, void* const* bufs, bool via_ws, cudaStream_t st) {
-  const Op& op = P->ops[i];
+  Op& op = P->ops[i];
   const void* src = bufs[op.src];
   void* dst = via_ws ? P->ws[0].p : bufs[op.dst];
   cudaError_t e = cudaSuccess;
+  // the pipelined tensor-copy kernel where the pass has one and the source
+  // is 16-byte aligned (a tensor map's base); its map is re-encoded when the
+  // source address changes
+  if (op.kind == OP_PASS && op.kfn_tma && P->d_status && ((uintptr_t)src & 15) == 0) {
+    if (op.tmap_src != src) {
+      op.tmap_src = encode_tma(op, src) ? src : nullptr;
+    }
+    if (op.tmap_src == src) return tma_launch(op.kfn_tma, op.pp, op.tmap, dst, P->d_status, op.tma_grid, st);
+  }
   if (P->dtype == FFTJ_F32) {
     switch (op.kind) {
       case OP_PASS: e = launch_pass<float>(op.pp, op.dir, op.kfn, src, dst, st); break;
@@ -1578,6 +1691,40 @@ int fftj_execute(fftj_plan plan, const void* d_in, void* d_out, void* stream) {
   return FFTJ_OK;
 }
 
+int fftj_plan_status(fftj_plan plan, void* stream) {
+  if (!plan) return fail(FFTJ_ERR_ARG, "null plan");
+  if (!plan->d_status) {
+    g_err.clear();
+    return FFTJ_OK;
+  }
+  if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "execution failed");
+  unsigned st = 0;
+  if (cudaMemcpy(&st, plan->d_status, sizeof(st), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(FFTJ_ERR_CUDA, "status read failed");
+  if (st) {
+    cudaMemset(plan->d_status, 0, sizeof(unsigned));
+    return fail(FFTJ_ERR_TIMEOUT, "a pipelined pass gave up waiting for a tile's tensor copy; its output is incomplete");
+  }
+  g_err.clear();
+  return FFTJ_OK;
+}
+
+int fftj_plan_set_wait_limit(fftj_plan plan, uint64_t ns) {
+  if (!plan) return fail(FFTJ_ERR_ARG, "null plan");
+  if (ns < 1000) return fail(FFTJ_ERR_ARG, "wait limit below 1 us");
+  for (auto& op : plan->ops) op.pp.tma_wait_ns = ns;
+  g_err.clear();
+  return FFTJ_OK;
+}
+
+int fftj_plan_debug_stall(fftj_plan plan, int extra_bytes) {
+  if (!plan) return fail(FFTJ_ERR_ARG, "null plan");
+  if (extra_bytes < 0 || extra_bytes > (1 << 20)) return fail(FFTJ_ERR_ARG, "extra bytes must be in [0, 2^20]");
+  for (auto& op : plan->ops) op.pp.tma_extra_tx = extra_bytes;
+  g_err.clear();
+  return FFTJ_OK;
+}
+
 int fftj_profile_ops(fftj_plan plan, const void* d_in, void* d_out, void* stream, int reps, float* ms, int cap) {
   if (!plan || !d_in || !d_out || !ms || reps < 1) return fail(FFTJ_ERR_ARG, "null argument or reps < 1");
   if (plan->dry) return fail(FFTJ_ERR_ARG, "a dry plan cannot execute");
@@ -1625,6 +1772,7 @@ int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info) {
   info->table_bytes = plan->table_bytes;
   info->nops = (int)plan->ops.size();
   info->dry = plan->dry ? 1 : 0;
+  for (const auto& op : plan->ops) info->tma_passes += op.kfn_tma != nullptr ? 1 : 0;
   // FNV-1a over everything that shapes the launches
   uint64_t h = 1469598103934665603ull;
   auto mix = [&](int64_t v) {
@@ -1652,7 +1800,7 @@ int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info) {
       pi++;
       for (int64_t v : {(int64_t)pp.R, (int64_t)pp.P, (int64_t)pp.Q, (int64_t)pp.NBt, (int64_t)pp.Tf,
                         (int64_t)pp.threads, (int64_t)pp.nsub, (int64_t)pp.tw_mode, (int64_t)pp.load_op, (int64_t)pp.tc,
-                        (int64_t)(uintptr_t)op.kfn})
+                        (int64_t)(uintptr_t)op.kfn, (int64_t)(uintptr_t)op.kfn_tma})
         mix(v);
       for (int i = 0; i < pp.nsub; ++i) mix(pp.sub[i].r);
     } else if (op.kind == OP_INTERP) {

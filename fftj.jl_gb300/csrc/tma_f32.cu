@@ -1,0 +1,59 @@
+// Pipelined tensor-copy pass kernels (pass_tma.cuh), F32, for the power-of-
+// two passes of multi-pass transforms at the planner's default tiles.
+#include <algorithm>
+
+#include "pass_tma.cuh"
+
+namespace fftj {
+
+// 256-thread tiles keep 3 CTAs per SM (registers <= 85); the 512-thread
+// radix-1024 tile runs one
+template <int DIR, int MODE, int NBC, class Rec>
+__global__ void __launch_bounds__(NBC * Rec::Tf, NBC * Rec::Tf <= 256 ? 3 : 1)
+    k_tma(const __grid_constant__ PassParams pp, const __grid_constant__ CUtensorMap map, Cx<float>* __restrict__ out,
+          unsigned* status) {
+  TmaLaunch<DIR, MODE, NBC, Rec>::run(pp, &map, out, status);
+}
+
+#define T_(DIR, MODE, NB, ...) \
+  {0, DIR, LOAD_PLAIN, MODE, {__VA_ARGS__}, Recipe<__VA_ARGS__>::Tf, NB, (const void*)k_tma<DIR, MODE, NB, Recipe<__VA_ARGS__>>},
+#define TT_(NB, ...)                                                                                \
+  T_(-1, 1, NB, __VA_ARGS__) T_(-1, 2, NB, __VA_ARGS__) T_(1, 1, NB, __VA_ARGS__) T_(1, 2, NB, __VA_ARGS__)
+
+static const RecipeEntry kTma[] = {
+    TT_(128, 8, 4) TT_(64, 8, 8) TT_(32, 16, 8) TT_(16, 16, 16) TT_(8, 8, 8, 8) TT_(8, 16, 8, 8)
+};
+
+const RecipeEntry* tma_table(int dir, int* count) {
+  (void)dir;
+  *count = (int)(sizeof(kTma) / sizeof(kTma[0]));
+  return kTma;
+}
+
+size_t tma_smem_bytes(const PassParams& pp) {
+  return (size_t)(2 * pp.tma_buf + pp.R) * sizeof(Cx<float>) + 2 * sizeof(uint64_t);
+}
+
+// Opts the kernel into the shared memory it needs and returns how many CTAs
+// of it fit the device at once (the persistent grid), 0 if none.
+int tma_prepare(const void* fn, const PassParams& pp) {
+  int dev = 0, optin = 0, nsm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  const size_t smem = tma_smem_bytes(pp);
+  if (smem > (size_t)optin) return 0;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, pp.threads, smem) != cudaSuccess) return 0;
+  return per_sm * nsm;
+}
+
+cudaError_t tma_launch(const void* fn, const PassParams& pp, const CUtensorMap& map, void* out, unsigned* status,
+                       int grid, cudaStream_t st) {
+  const uint32_t ntiles = pp.tiles_q * pp.tiles_p * pp.tiles_b;
+  const unsigned g = (unsigned)std::min<uint64_t>((uint64_t)grid, ntiles);
+  void* args[4] = {const_cast<PassParams*>(&pp), const_cast<CUtensorMap*>(&map), &out, &status};
+  return cudaLaunchKernel(fn, dim3(g), dim3(pp.threads), args, tma_smem_bytes(pp), st);
+}
+
+}  // namespace fftj

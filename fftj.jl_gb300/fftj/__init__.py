@@ -52,14 +52,15 @@ class PlanInfo(ctypes.Structure):
         ("table_bytes", ctypes.c_size_t), ("specialized_passes", ctypes.c_int),
         ("schedule_hash", ctypes.c_uint64), ("pass_tile", ctypes.c_int * 8),
         ("pass_threads", ctypes.c_int * 8), ("pass_ctas", ctypes.c_int64 * 8), ("nops", ctypes.c_int),
-        ("dry", ctypes.c_int), ("tc_substages", ctypes.c_int),
+        ("dry", ctypes.c_int), ("tc_substages", ctypes.c_int), ("tma_passes", ctypes.c_int),
     ]
 
 
 class PlanOpts(ctypes.Structure):
     """fftj_plan_opts_t: schedule options (all zero = the planner's default)."""
     _fields_ = [(k, ctypes.c_int32) for k in
-                ("tile", "extra_passes", "order", "tf_mult", "route", "threads_max", "dry", "precision")]
+                ("tile", "extra_passes", "order", "tf_mult", "route", "threads_max", "dry", "precision",
+                 "plain_loads")]
 
 
 class TuneQuery(ctypes.Structure):
@@ -97,7 +98,7 @@ EXPORTS = [
     "fftj_mlp_set_params", "fftj_mlp_grad", "fftj_mlp_train", "fftj_mlp_predict",
     "fftj_group_create", "fftj_group_execute", "fftj_group_status", "fftj_group_get_info",
     "fftj_group_set_wait_limit", "fftj_group_debug_stall", "fftj_group_destroy", "fftj_profile_ops",
-    "fftj_plan_c2c_from_tables",
+    "fftj_plan_c2c_from_tables", "fftj_plan_status", "fftj_plan_set_wait_limit", "fftj_plan_debug_stall",
 ]
 
 
@@ -153,6 +154,9 @@ def lib():
         L.fftj_profile_ops.argtypes = [vp, vp, vp, vp, i32, PF, i32]
         L.fftj_plan_c2c_from_tables.argtypes = [ctypes.POINTER(vp), i32, i64, i64, i32, ctypes.c_double, PD,
                                                 i64, ctypes.POINTER(ResampleTables)]
+        L.fftj_plan_status.argtypes = [vp, vp]
+        L.fftj_plan_set_wait_limit.argtypes = [vp, ctypes.c_uint64]
+        L.fftj_plan_debug_stall.argtypes = [vp, i32]
         L.fftj_last_error_string.restype = ctypes.c_char_p
         L.fftj_version.restype = ctypes.c_char_p
         for name in EXPORTS:
@@ -283,6 +287,21 @@ class Plan:
 
     def __mul__(self, x):
         return self(x)
+
+    def status(self, stream=None):
+        """Waits for the plan's work on `stream` (default: the current stream)
+        and raises FFTJError if a pipelined pass's bounded wait gave up."""
+        if stream is None:
+            stream = torch.cuda.current_stream().cuda_stream
+        _check(lib().fftj_plan_status(self._h, ctypes.c_void_p(stream)))
+
+    def set_wait_limit(self, ns):
+        """Bound of each pipelined pass's wait for a tile's copies (ns)."""
+        _check(lib().fftj_plan_set_wait_limit(self._h, int(ns)))
+
+    def debug_stall(self, extra_bytes):
+        """Test hook: tile barriers expect extra bytes, so waits run out."""
+        _check(lib().fftj_plan_debug_stall(self._h, int(extra_bytes)))
 
     def profile_ops(self, y, x, reps=10):
         """Mean milliseconds of each op (pass / elementwise kernel) of the plan."""

@@ -73,6 +73,7 @@ typedef struct {
   int nops;               /* kernel launches per execution (passes + elementwise ops) */
   int dry;                /* 1: planned without tables or workspace (cannot execute) */
   int tc_substages;       /* radix-16 sub-stages run on tensor cores (opts.precision != 0) */
+  int tma_passes;         /* passes with a pipelined tensor-copy kernel (used when the input is 16-byte aligned) */
 } fftj_plan_info_t;
 
 /*
@@ -93,6 +94,7 @@ typedef struct {
   int32_t dry;           /* 1: plan the schedule only (no tables, no workspace, cannot execute) */
   int32_t precision;     /* F32 radix-16 sub-stages: 0 FP32 butterflies, 1 FP16 hi+lo tensor-core GEMM,
                             2 BF16 hi+lo tensor-core GEMM (FP32 accumulation, FP32 twiddles) */
+  int32_t plain_loads;   /* 1: one-tile-per-CTA kernels only (no pipelined tensor-copy passes) */
 } fftj_plan_opts_t;
 
 int fftj_plan_c2c_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch,
@@ -237,6 +239,20 @@ int fftj_profile_ops(fftj_plan plan, const void* d_in, void* d_out, void* stream
 
 /* Size and algorithm of a plan (FFTJ: size(p) and the plan type). */
 int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info);
+
+/*
+ * Pipelined passes (F32 power-of-two passes of multi-pass transforms) wait
+ * for their tiles' tensor copies with a bounded wait. fftj_plan_status
+ * synchronises `stream` and returns FFTJ_ERR_TIMEOUT if a wait of an earlier
+ * execution gave up (the status is then cleared). No counterpart in the
+ * reference (host code has no device waits).
+ */
+int fftj_plan_status(fftj_plan plan, void* stream);
+/* Bound of each such wait in nanoseconds (default 1e9). */
+int fftj_plan_set_wait_limit(fftj_plan plan, uint64_t ns);
+/* Test hook: tile barriers expect `extra_bytes` more than their copies
+ * deliver, so every wait runs out (0 restores normal operation). */
+int fftj_plan_debug_stall(fftj_plan plan, int extra_bytes);
 
 /* Device workspace owned by the plan, in bytes. */
 int fftj_plan_workspace_bytes(fftj_plan plan, size_t* bytes);
