@@ -148,14 +148,14 @@ struct RecipeEntry {
 };
 template <typename T, int DIR>
 const RecipeEntry* recipe_table(int* count);
-// Pipelined tensor-copy pass kernels (F32, LOAD_PLAIN, modes 1 and 2; nb =
-// the exact tile column count). Signature:
-// (PassParams, CUtensorMap, float2* out, unsigned* status).
+// Pipelined tensor-copy pass kernels (F32, LOAD_PLAIN, modes 0, 1 and 2; nb
+// = the exact tile column count). Signature:
+// (PassParams, CUtensorMap, const float2* in, float2* out, unsigned* status).
 const RecipeEntry* tma_table(int dir, int* count);
 size_t tma_smem_bytes(const PassParams& pp);
 int tma_prepare(const void* fn, const PassParams& pp);
-cudaError_t tma_launch(const void* fn, const PassParams& pp, const CUtensorMap& map, void* out, unsigned* status,
-                       int grid, cudaStream_t st);
+cudaError_t tma_launch(const void* fn, const PassParams& pp, const CUtensorMap& map, const void* in, void* out,
+                       unsigned* status, int grid, cudaStream_t st);
 
 // fn: a recipe kernel (RecipeEntry::fn) or nullptr for the generic kernel.
 // Planner pieces shared by the plan builder and the allocation-free entry

@@ -904,9 +904,9 @@ __device__ __forceinline__ void run_mid_ct(Cx<T>* buf, const int b, const int kg
   if constexpr (sizeof...(rest) > 0) run_mid_skip<T, DIR, TF, R, S1, DROP, NBC, rest...>(buf, b, kg, NB, twR);
 }
 
-// Fused last sub-stage (radix rL) + HBM store of one tile of a multi-pass
-// transform: MODE 1 is the row store of a first pass (s == 1), MODE 2 the
-// strided store of a later pass. Shared by the one-tile-per-CTA recipe
+// Fused last sub-stage (radix rL) + HBM store of one tile: MODE 0 is the row
+// store of a single-pass transform, MODE 1 the row store of a first pass
+// (s == 1), MODE 2 the strided store of a later pass. Shared by the one-tile-per-CTA recipe
 // kernels and the pipelined tensor-copy kernel (pass_tma.cuh).
 template <typename T, int DIR, int MODE, int NBC, int... Rs>
 __device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restrict__ out,
@@ -922,7 +922,37 @@ __device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restri
   const bool scaled = not_one(pp.scale);
   const T sc = (T)pp.scale;
   const bool tw = pp.tw_mode != 0;
-  if constexpr (MODE == 1) {
+  if constexpr (MODE == 0) {
+    // ---- fused last sub-stage (radix rL) + row store: butterfly u = c S + k
+    // with k fastest across lanes writes outputs k + jj S of row c, the
+    // lanes of a warp at consecutive addresses for each jj (one pass over
+    // whole transforms: no outer twiddle)
+    (void)tw;
+    constexpr int S = R / rL;
+    const int nbf = NB * S;
+    for (int u = tid; u < nbf; u += nthr) {
+      const int c = u / S;
+      const int k = u - c * S;
+      if (b0 + c >= pp.nbatch) continue;
+      Cx<T> v[rL];
+      if constexpr (NBC > 0 && LayC<T, NBC>::exact(S)) {
+        const int base = LayC<T, NBC>::row(k) + LayC<T, NBC>::col(c);
+#pragma unroll
+        for (int j = 0; j < rL; ++j) v[j] = buf[base + j * LayC<T, NBC>::step(S)];
+      } else {
+#pragma unroll
+        for (int j = 0; j < rL; ++j) v[j] = buf[pidx<T>((k + j * S) * NB + c)];
+      }
+      Dft<T, DIR, rL>::run(v);
+      Cx<T>* o = out + (b0 + c) * pp.out_bstride + k;
+#pragma unroll
+      for (int j = 0; j < rL; ++j) {
+        Cx<T> x = v[j];
+        if (scaled) { x.x *= sc; x.y *= sc; }
+        o[j * S] = x;
+      }
+    }
+  } else if constexpr (MODE == 1) {
     // ---- fused last sub-stage (radix rL) + row store (s == 1). Butterfly
     // u = c S + k takes k fastest across lanes, so for each output
     // j = k + jj S the lanes of a warp write consecutive addresses of column
@@ -1208,28 +1238,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
   const T sc = (T)pp.scale;
   const bool tw = pp.tw_mode != 0;
   if constexpr (MODE == 0 && NS >= 2) {
-    // ---- fused last sub-stage (radix rL) + row store: butterfly u = c S + k
-    // with k fastest across lanes writes outputs k + jj S of row c, the
-    // lanes of a warp at consecutive addresses for each jj (one pass over
-    // whole transforms: no outer twiddle)
-    constexpr int S = R / rL;
-    const int nbf = NB * S;
-    for (int u = tid; u < nbf; u += nthr) {
-      const int c = u / S;
-      const int k = u - c * S;
-      if (b0 + c >= pp.nbatch) continue;
-      Cx<T> v[rL];
-#pragma unroll
-      for (int j = 0; j < rL; ++j) v[j] = buf[pidx<T>((k + j * S) * NB + c)];
-      Dft<T, DIR, rL>::run(v);
-      Cx<T>* o = out + (b0 + c) * pp.out_bstride + k;
-#pragma unroll
-      for (int j = 0; j < rL; ++j) {
-        Cx<T> x = v[j];
-        if (scaled) { x.x *= sc; x.y *= sc; }
-        o[j * S] = x;
-      }
-    }
+    store_last<T, DIR, MODE, NBC, Rs...>(pp, out, buf, tid, nthr, kg, b, b0, p0, q0, ql, batch, pcol, colok);
   } else if constexpr (MODE == 0) {
     // ---- row store (lanes walk j): outputs contiguous along j (s == 1)
     const int dc = nthr / R, dj = nthr - (nthr / R) * R;

@@ -59,6 +59,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64
     if (ns_now() - t0 > limit_ns) return false;
   }
 }
+// 1-D bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(sh_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(sh_addr(bar))
+      : "memory");
+}
 __device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
@@ -74,12 +81,18 @@ __device__ __forceinline__ void tma_load4(void* dst, const CUtensorMap* map, uin
       : "memory");
 }
 
-// MODE 1: tile = P consecutive columns p (Q == 1, one batch entry), tensor
-// (p, j, batch); MODE 2: tile = Q consecutive columns q (P == 1, one batch
-// entry), tensor (q, p, j, batch). NBC = the tile's column count.
+// MODE 0: tile = NB whole contiguous transforms (batch entries), one 1-D
+// bulk copy per entry; MODE 1: tile = P consecutive columns p (Q == 1, one
+// batch entry), tensor (p, j, batch); MODE 2: tile = Q consecutive columns q
+// (P == 1, one batch entry), tensor (q, p, j, batch). NBC = the tile's
+// column count. Passes of radix above 1024 read their inner twiddles from
+// global memory (L1-resident) instead of staging them.
+template <int R>
+__host__ __device__ constexpr bool tma_stages_twiddles() { return R <= 1024; }
+
 template <int DIR, int MODE, int NBC, int... Rs>
-__device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap* map, Cx<float>* __restrict__ out,
-                                         unsigned* status) {
+__device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap* map, const Cx<float>* in,
+                                         Cx<float>* __restrict__ out, unsigned* status) {
   using T = float;
   using Rec = Recipe<Rs...>;
   using L = LayC<T, NBC>;
@@ -91,21 +104,24 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
   constexpr int NB = NBC;
   constexpr int nthr = NBC * TF;
   constexpr uint32_t kTx = (uint32_t)(NB * R * sizeof(Cx<T>));
-  static_assert(NS >= 2, "a pass of a multi-pass transform has at least two sub-stages");
+  static_assert(NS >= 2, "the first and last sub-stages are separate");
+  static_assert(MODE != 0 || Rr % TF == 0, "single-pass tiles: whole butterfly rounds per thread");
   // box copies land 16-byte aligned: dynamic shared memory starts 16-byte
   // aligned and buffers are multiples of 128 bytes
   extern __shared__ __align__(16) unsigned char tma_smem[];
   Cx<T>* const sbase = reinterpret_cast<Cx<T>*>(tma_smem);
   const int bufE = pp.tma_buf;  // elements per buffer, a multiple of 16 (128 bytes)
+  constexpr bool kStageTw = tma_stages_twiddles<R>();
   Cx<T>* const twS = sbase + 2 * bufE;
-  uint64_t* const bar = reinterpret_cast<uint64_t*>(twS + R);
+  uint64_t* const bar = reinterpret_cast<uint64_t*>(twS + (kStageTw ? R : 0));
+  const Cx<T>* const tw = kStageTw ? twS : reinterpret_cast<const Cx<T>*>(pp.twR);
   const int tid = threadIdx.x;
   const int kg = tid / NB;
   const int b = tid - kg * NB;
   const uint32_t ntiles = pp.tiles_q * pp.tiles_p * pp.tiles_b;
   const int rows = pp.tma_rows;
   const uint64_t limit = pp.tma_wait_ns;
-  {
+  if constexpr (kStageTw) {
     const Cx<T>* twG = reinterpret_cast<const Cx<T>*>(pp.twR);
     for (int t = tid; t < R; t += nthr) twS[t] = __ldg(twG + t);
   }
@@ -124,12 +140,21 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
     const uint32_t tb = pp.ftp.div(t1);
     const uint32_t tp = t1 - tb * pp.tiles_p;
     Cx<T>* dst = sbase + slot * bufE;
-    mbar_arrive_expect_tx(bar + slot, kTx + (uint32_t)pp.tma_extra_tx);
-    for (int j0 = 0; j0 < R; j0 += rows) {
-      if constexpr (MODE == 1)
-        tma_load3(dst + j0 * NB, map, bar + slot, (int)(tp * (uint32_t)pp.P), j0, (int)tb);
-      else
-        tma_load4(dst + j0 * NB, map, bar + slot, (int)(tq * (uint32_t)pp.Q), (int)tp, j0, (int)tb);
+    if constexpr (MODE == 0) {
+      // the tile's batch entries that exist, each R contiguous elements
+      const int64_t b0 = (int64_t)tb * NB;
+      const int nv = (int)min((int64_t)NB, pp.nbatch - b0);
+      mbar_arrive_expect_tx(bar + slot, (uint32_t)(nv * R * sizeof(Cx<T>)) + (uint32_t)pp.tma_extra_tx);
+      for (int c = 0; c < nv; ++c)
+        bulk_load(dst + c * R, in + (b0 + c) * pp.in_bstride, (uint32_t)(R * sizeof(Cx<T>)), bar + slot);
+    } else {
+      mbar_arrive_expect_tx(bar + slot, kTx + (uint32_t)pp.tma_extra_tx);
+      for (int j0 = 0; j0 < R; j0 += rows) {
+        if constexpr (MODE == 1)
+          tma_load3(dst + j0 * NB, map, bar + slot, (int)(tp * (uint32_t)pp.P), j0, (int)tb);
+        else
+          tma_load4(dst + j0 * NB, map, bar + slot, (int)(tq * (uint32_t)pp.Q), (int)tp, j0, (int)tb);
+      }
     }
   };
   if (tid == 0 && blockIdx.x < ntiles) issue(blockIdx.x, 0);
@@ -158,43 +183,51 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
     const uint32_t tq = tile - t1 * pp.tiles_q;
     const uint32_t tb = pp.ftp.div(t1);
     const uint32_t tp = t1 - tb * pp.tiles_p;
-    const int64_t q0 = (int64_t)tq * pp.Q, p0 = (int64_t)tp * pp.P, b0 = (int64_t)tb;
+    const int64_t q0 = (int64_t)tq * pp.Q, p0 = (int64_t)tp * pp.P, b0 = (int64_t)tb * (MODE == 0 ? NB : 1);
     const int ql = MODE == 2 ? b : 0;
     const int64_t pcol = MODE == 1 ? p0 + b : p0;
     const bool colok = b0 < pp.nbatch && q0 + ql < pp.s;
 
     // ---- first sub-stage (radix r0, S = 1) from the dense tile, written
     // back in place in the padded layout
+    // butterfly (column c, k): MODE 0 takes k fastest across lanes (entries
+    // are rows [c][j] of the dense tile), modes 1 and 2 the column (rows
+    // [j][c]); both read consecutive addresses across a warp
     Cx<T> v[IPT][r0];
 #pragma unroll
     for (int i = 0; i < IPT; ++i) {
-      const int k = kg + i * TF;
-      if ((i + 1) * TF <= Rr || k < Rr) {
-        const Cx<T>* src = buf + k * NB + b;
+      const int u = tid + i * nthr;
+      const int c = MODE == 0 ? u / Rr : b;
+      const int k = MODE == 0 ? u - c * Rr : kg + i * TF;
+      if (MODE == 0 || (i + 1) * TF <= Rr || k < Rr) {
+        const Cx<T>* src = MODE == 0 ? buf + c * R + k : buf + k * NB + b;
+        constexpr int js = MODE == 0 ? Rr : Rr * NB;
 #pragma unroll
-        for (int j = 0; j < r0; ++j) v[i][j] = src[j * Rr * NB];
+        for (int j = 0; j < r0; ++j) v[i][j] = src[j * js];
       }
     }
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < IPT; ++i) {
-      const int k = kg + i * TF;
-      if ((i + 1) * TF <= Rr || k < Rr) {
+      const int u = tid + i * nthr;
+      const int c = MODE == 0 ? u / Rr : b;
+      const int k = MODE == 0 ? u - c * Rr : kg + i * TF;
+      if (MODE == 0 || (i + 1) * TF <= Rr || k < Rr) {
         Dft<T, DIR, r0>::run(v[i]);
         constexpr bool kLay = L::exact(r0);
-        const int a = r0 * k * NB + b;
-        const int base = kLay ? L::row(r0 * k) + L::col(b) : pidx<T>(a);
+        const int a = r0 * k * NB + c;
+        const int base = kLay ? L::row(r0 * k) + L::col(c) : pidx<T>(a);
         buf[base] = v[i][0];
 #pragma unroll
         for (int j = 1; j < r0; ++j) {
           Cx<T> w = v[i][j];
-          if (k != 0) w = cmul(w, twS[j * k]);
+          if (k != 0) w = cmul(w, tw[j * k]);
           buf[kLay ? base + L::step(j) : pidx<T>(a + j * NB)] = w;
         }
       }
     }
     __syncthreads();
-    if constexpr (NS > 2) run_mid_ct<T, DIR, TF, R, r0, 1, NBC, Rs...>(buf, b, kg, NB, twS);
+    if constexpr (NS > 2) run_mid_ct<T, DIR, TF, R, r0, 1, NBC, Rs...>(buf, b, kg, NB, tw);
     store_last<T, DIR, MODE, NBC, Rs...>(pp, out, buf, tid, nthr, kg, b, b0, p0, q0, ql, b0, pcol, colok);
     __syncthreads();  // the buffer is free for the copy after next
   }
@@ -204,9 +237,9 @@ template <int DIR, int MODE, int NBC, class Rec>
 struct TmaLaunch;
 template <int DIR, int MODE, int NBC, int... Rs>
 struct TmaLaunch<DIR, MODE, NBC, Recipe<Rs...>> {
-  __device__ __forceinline__ static void run(const PassParams& pp, const CUtensorMap* map, Cx<float>* out,
-                                             unsigned* status) {
-    pass_tma<DIR, MODE, NBC, Rs...>(pp, map, out, status);
+  __device__ __forceinline__ static void run(const PassParams& pp, const CUtensorMap* map, const Cx<float>* in,
+                                             Cx<float>* out, unsigned* status) {
+    pass_tma<DIR, MODE, NBC, Rs...>(pp, map, in, out, status);
   }
 };
 

@@ -1356,19 +1356,30 @@ int check_dims(int rank, const int64_t* dims, std::vector<i64>* out) {
 // strides (16-byte tensor strides). The source address is checked at launch.
 void pick_tma(Op& op, bool dry) {
   const PassParams& pp = op.pp;
-  if (pp.load_op != LOAD_PLAIN || pp.NBt != 1) return;
-  int mode = 0;
-  if (!pp.load_rows && pp.store_rows && pp.Q == 1) mode = 1;
-  else if (!pp.load_rows && !pp.store_rows && pp.P == 1) mode = 2;
-  if (!mode) return;
-  const i64 cols = mode == 1 ? pp.P : pp.Q;
-  if (cols != pp.NB || cols % 2 || cols > 256) return;
+  if (pp.load_op != LOAD_PLAIN) return;
+  int mode = -1;
+  if (pp.load_rows && pp.store_rows && pp.P == 1 && pp.Q == 1 && (pp.NBt == 1 || pp.out_bstride == (int64_t)pp.R)) {
+    // single pass over whole transforms: one 1-D bulk copy per batch entry
+    // (R contiguous elements, 16-byte aligned when R and the batch stride
+    // are even)
+    mode = 0;
+    if (pp.R % 2 || (pp.nbatch > 1 && pp.in_bstride % 2)) return;
+  } else if (pp.NBt != 1) {
+    return;
+  } else if (!pp.load_rows && pp.store_rows && pp.Q == 1) {
+    mode = 1;
+  } else if (!pp.load_rows && !pp.store_rows && pp.P == 1) {
+    mode = 2;
+  }
+  if (mode < 0) return;
+  const i64 cols = mode == 1 ? pp.P : mode == 2 ? pp.Q : 2;
+  if (mode && (cols != pp.NB || cols % 2 || cols > 256)) return;
   // the last pass of a two-sub-stage radix with 128-byte tile rows keeps
   // plain loads: its in-CTA work is short, and four one-tile CTAs per SM
   // keep more reads in flight than three pipelined ones (measured on the
   // radix-256 last passes of 2^26 and 2^25 x 4: 0.92-0.96 vs 0.84-0.87 of HBM)
   if (pp.m == 1 && pp.nsub == 2 && cols * 8 <= 128) return;
-  if ((mode == 1 ? pp.m : pp.s) % 2) return;
+  if (mode && (mode == 1 ? pp.m : pp.s) % 2) return;
   if (pp.nbatch > 1 && (pp.in_bstride % 2 || pp.in_bstride < pp.ncur)) return;
   int count = 0;
   const RecipeEntry* tab = tma_table(op.dir, &count);
@@ -1616,10 +1627,9 @@ static cudaError_t launch_op(fftj_plan_s* P, size_t i, void* const* bufs, bool v
   // is 16-byte aligned (a tensor map's base); its map is re-encoded when the
   // source address changes
   if (op.kind == OP_PASS && op.kfn_tma && P->d_status && ((uintptr_t)src & 15) == 0) {
-    if (op.tmap_src != src) {
-      op.tmap_src = encode_tma(op, src) ? src : nullptr;
-    }
-    if (op.tmap_src == src) return tma_launch(op.kfn_tma, op.pp, op.tmap, dst, P->d_status, op.tma_grid, st);
+    // single-pass tiles are 1-D bulk copies from `src` (no tensor map)
+    if (op.tmap_src != src) op.tmap_src = (op.tma_mode == 0 || encode_tma(op, src)) ? src : nullptr;
+    if (op.tmap_src == src) return tma_launch(op.kfn_tma, op.pp, op.tmap, src, dst, P->d_status, op.tma_grid, st);
   }
   if (P->dtype == FFTJ_F32) {
     switch (op.kind) {

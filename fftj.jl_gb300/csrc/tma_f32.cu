@@ -10,18 +10,22 @@ namespace fftj {
 // radix-1024 tile runs one
 template <int DIR, int MODE, int NBC, class Rec>
 __global__ void __launch_bounds__(NBC * Rec::Tf, NBC * Rec::Tf <= 256 ? 3 : 1)
-    k_tma(const __grid_constant__ PassParams pp, const __grid_constant__ CUtensorMap map, Cx<float>* __restrict__ out,
-          unsigned* status) {
-  TmaLaunch<DIR, MODE, NBC, Rec>::run(pp, &map, out, status);
+    k_tma(const __grid_constant__ PassParams pp, const __grid_constant__ CUtensorMap map,
+          const Cx<float>* __restrict__ in, Cx<float>* __restrict__ out, unsigned* status) {
+  TmaLaunch<DIR, MODE, NBC, Rec>::run(pp, &map, in, out, status);
 }
 
 #define T_(DIR, MODE, NB, ...) \
   {0, DIR, LOAD_PLAIN, MODE, {__VA_ARGS__}, Recipe<__VA_ARGS__>::Tf, NB, (const void*)k_tma<DIR, MODE, NB, Recipe<__VA_ARGS__>>},
 #define TT_(NB, ...)                                                                                \
   T_(-1, 1, NB, __VA_ARGS__) T_(-1, 2, NB, __VA_ARGS__) T_(1, 1, NB, __VA_ARGS__) T_(1, 2, NB, __VA_ARGS__)
+#define T0_(NB, ...) T_(-1, 0, NB, __VA_ARGS__) T_(1, 0, NB, __VA_ARGS__)
 
 static const RecipeEntry kTma[] = {
+    // passes of multi-pass transforms (first: mode 1, later: mode 2)
     TT_(128, 8, 4) TT_(64, 8, 8) TT_(32, 16, 8) TT_(16, 16, 16) TT_(8, 8, 8, 8) TT_(8, 16, 8, 8)
+    // single-pass transforms of three sub-stages at 4096-element tiles
+    T0_(1, 16, 16, 16) T0_(2, 16, 16, 8) T0_(4, 16, 8, 8) T0_(8, 8, 8, 8)
 };
 
 const RecipeEntry* tma_table(int dir, int* count) {
@@ -31,7 +35,8 @@ const RecipeEntry* tma_table(int dir, int* count) {
 }
 
 size_t tma_smem_bytes(const PassParams& pp) {
-  return (size_t)(2 * pp.tma_buf + pp.R) * sizeof(Cx<float>) + 2 * sizeof(uint64_t);
+  const int tw = pp.R <= 1024 ? pp.R : 0;  // tma_stages_twiddles
+  return (size_t)(2 * pp.tma_buf + tw) * sizeof(Cx<float>) + 2 * sizeof(uint64_t);
 }
 
 // Opts the kernel into the shared memory it needs and returns how many CTAs
@@ -48,11 +53,11 @@ int tma_prepare(const void* fn, const PassParams& pp) {
   return per_sm * nsm;
 }
 
-cudaError_t tma_launch(const void* fn, const PassParams& pp, const CUtensorMap& map, void* out, unsigned* status,
-                       int grid, cudaStream_t st) {
+cudaError_t tma_launch(const void* fn, const PassParams& pp, const CUtensorMap& map, const void* in, void* out,
+                       unsigned* status, int grid, cudaStream_t st) {
   const uint32_t ntiles = pp.tiles_q * pp.tiles_p * pp.tiles_b;
   const unsigned g = (unsigned)std::min<uint64_t>((uint64_t)grid, ntiles);
-  void* args[4] = {const_cast<PassParams*>(&pp), const_cast<CUtensorMap*>(&map), &out, &status};
+  void* args[5] = {const_cast<PassParams*>(&pp), const_cast<CUtensorMap*>(&map), &in, &out, &status};
   return cudaLaunchKernel(fn, dim3(g), dim3(pp.threads), args, tma_smem_bytes(pp), st);
 }
 

@@ -38,6 +38,10 @@ CASES = [
     ("c2c", (1 << 12, 1 << 12), 1, -1),  # 2-D: the strided axis as two radix-64 passes
     ("c2c", (1024, 1024), 2, 1),      # 2-D: strided radix-1024 pass
     ("r2c", (1 << 21,), 2, -1),       # rfft: half-length passes + post-pass
+    ("c2c", (4096,), 5, -1),          # single pass, radix 16*16*16, one transform per tile
+    ("c2c", (2048,), 37, -1),         # single pass, two per tile: the last tile holds one
+    ("c2c", (1024,), 13, 1),          # single pass, four per tile, backward
+    ("c2c", (512,), 9, -1),           # single pass, radix 8*8*8, eight per tile
 ]
 
 
