@@ -726,7 +726,7 @@ def run_configs(args):
             if args.case and label not in args.case.split(","):
                 continue
             p = fftj.Plan(dt, dims, kind=kind, batch=batch, direction=-1 if kind != "c2r" else 1,
-                          opts={"precision": precision})
+                          opts={"precision": precision, "plain_loads": 1 if args.plain_loads else 0})
             shape, tdt = p.in_spec()
             if data == "uniform":
                 if tdt.is_complex:
@@ -772,7 +772,7 @@ def run_configs(args):
                    "pass_radix": [int(v) for v in inf.pass_radix[:inf.npasses]],
                    "ops": passes, "specialized_passes": int(inf.specialized_passes),
                    "precision": ["fp32", "fp16 hi+lo tensor-core radix-16", "bf16 hi+lo tensor-core radix-16"][precision],
-                   "tc_substages": int(inf.tc_substages)}
+                   "tc_substages": int(inf.tc_substages), "tma_passes": int(inf.tma_passes)}
             # accuracy against FP64 (numpy): sampled rows, or the whole array
             xs = x.cpu().numpy()
             ys = y.cpu().numpy()
@@ -849,6 +849,8 @@ def main():
     ap.add_argument("--count", type=int, default=UNEVEN_COUNT, help="transforms of the uneven workload")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned planner report")
     ap.add_argument("--case", default=None, help="configs workload: only these cases (comma-separated labels)")
+    ap.add_argument("--plain-loads", action="store_true",
+                    help="configs workload: one-tile-per-CTA kernels only (no pipelined tensor-copy passes)")
     args = ap.parse_args()
     if args.only:
         dt, n = args.only.split(":")

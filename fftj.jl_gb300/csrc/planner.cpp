@@ -433,7 +433,7 @@ DtypeCfg dtype_cfg(bool f64) {
   // F32: 4096-element tiles (35 KB) give 4 CTAs of 256 threads per SM,
   // measured faster than 8192-element tiles at 2 CTAs per SM
   DtypeCfg c = f64 ? DtypeCfg{16, env_int("FFTJ_TILE_F64", 4096), 4096, 256, 1024, 4}
-                   : DtypeCfg{8, env_int("FFTJ_TILE_F32", 4096), 8192, 512, 1024, 8};
+                   : DtypeCfg{8, env_int("FFTJ_TILE_F32", 4096), 8192, 512, 1024, env_int("FFTJ_MIN_RUN_F32", 8)};
   if (g_sched.tile > 0) c.tile_max = std::min(std::max(g_sched.tile, 256), c.tile_cap);
   if (g_sched.threads_max > 0) c.threads_max = std::min(c.threads_max, std::max(g_sched.threads_max, 64));
   return c;
