@@ -186,8 +186,18 @@ __device__ __forceinline__ void real_post_at(const RealPostParams& rp, const Cx<
   }
   const Cx<T> a = ldd<CG>(Z + k);
   const Cx<T> m = ldd<CG>(Z + (h - k));
-  Y[k] = real_post_one<T>(a, m, __ldg(tw + k));
-  if (h - k != k) Y[h - k] = real_post_one<T>(m, a, __ldg(tw + (h - k)));
+  // w^k (k <= h/2) from the table or its two-level split; the mirror's
+  // twiddle is w^(h-k) = -conj(w^k) (n = 2h), exact in any precision
+  Cx<T> w;
+  if (rp.sh) {
+    const Cx<T> hi = __ldg(tw + (k >> rp.sh));
+    const Cx<T> lo = __ldg(reinterpret_cast<const Cx<T>*>(rp.tw2) + (k & ((1ll << rp.sh) - 1)));
+    w = cmul(hi, lo);
+  } else {
+    w = __ldg(tw + k);
+  }
+  Y[k] = real_post_one<T>(a, m, w);
+  if (h - k != k) Y[h - k] = real_post_one<T>(m, a, mk<T>(-w.x, w.y));
 }
 
 // Odd-length real edges (FFTJ src/real.jl:136-140, 194-209).

@@ -85,7 +85,9 @@ struct PassParams {
   int64_t ld_n, ld_m, ld_hp;     // DECONV: n, m, ceil(n/2); C2R_PRE: h = ld_n
   int64_t ld_stride;             // input batch stride of the raw input
   int64_t ld_inner;              // DECONV along a strided axis: inner stride (1 = contiguous)
-  const void* ld_tab;            // DECONV: corr[n]; C2R_PRE: w[h]
+  const void* ld_tab;            // DECONV: corr[n]; C2R_PRE: w[h], or hi[h >> ld_sh] when ld_sh > 0
+  const void* ld_tab2;           // C2R_PRE two-level: lo[2^ld_sh]
+  int ld_sh;                     // C2R_PRE: 0 one table, else the two-level split
   double ld_pre;                 // C2R_PRE pair factor (1/2 or 1)
   int ld_w;                      // SPREAD: taps per grid row
   const int32_t* ld_l0;          // SPREAD: first input row of each grid row
@@ -122,7 +124,9 @@ struct InterpParams {
 // rfft even post-pass: Y[k] (k = 0..h) from Z (length h) per batch.
 struct RealPostParams {
   int64_t h, nbatch, z_bstride, y_bstride;
-  const void* tw;  // e^{-2 pi i k/n}, k = 0..h
+  const void* tw;   // e^{-2 pi i k/n}, k = 0..h/2; or hi[k >> sh] when sh > 0
+  const void* tw2;  // two-level: lo[2^sh]
+  int sh;           // 0: one table, else w^k = hi[k >> sh] lo[k & (2^sh - 1)]
 };
 
 // Generic elementwise helpers for odd-length real transforms.

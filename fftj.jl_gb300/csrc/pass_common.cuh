@@ -253,6 +253,20 @@ __device__ __noinline__ void substage(Cx<T>* __restrict__ buf, const int b, cons
 // the group kernel uses it to keep its instantiation count small).
 constexpr int LOAD_RUNTIME = -1;
 
+// twiddle of the irfft pre-pass: one table w[g] (g < h), or for long
+// halves the two-level product hi[g >> sh] * lo[g & (2^sh - 1)] of two
+// L1/L2-resident tables (the single table would stream from HBM beside the
+// data)
+template <typename T>
+__device__ __forceinline__ Cx<T> c2r_twiddle(const PassParams& pp, int64_t g) {
+  if (pp.ld_sh) {
+    const Cx<T> hi = __ldg(reinterpret_cast<const Cx<T>*>(pp.ld_tab) + (g >> pp.ld_sh));
+    const Cx<T> lo = __ldg(reinterpret_cast<const Cx<T>*>(pp.ld_tab2) + (g & ((1ll << pp.ld_sh) - 1)));
+    return cmul(hi, lo);
+  }
+  return __ldg(reinterpret_cast<const Cx<T>*>(pp.ld_tab) + g);
+}
+
 template <typename T, int LOADOP, bool CG = false>
 __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in, int64_t b, int64_t g);
 
@@ -313,7 +327,7 @@ __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in,
     const T pre = half_or_one<T>(pp.ld_pre);  // 1/2 (irfft) or 1 (brfft)
     const Cx<T> xe = mk<T>((a.x + bb.x) * pre, (a.y + bb.y) * pre);
     const Cx<T> xd = mk<T>((a.x - bb.x) * pre, (a.y - bb.y) * pre);
-    const Cx<T> w = __ldg(reinterpret_cast<const Cx<T>*>(pp.ld_tab) + g);
+    const Cx<T> w = c2r_twiddle<T>(pp, g);
     const T tr = fma(w.x, xd.x, -(w.y * xd.y));
     const T ti = fma(w.x, xd.y, w.y * xd.x);
     return mk<T>(xe.x - ti, xe.y + tr);
@@ -874,7 +888,7 @@ __device__ __forceinline__ Cx<T> load_elem_off(const PassParams& pp, const void*
     const T pre = half_or_one<T>(pp.ld_pre);  // 1/2 (irfft) or 1 (brfft)
     const Cx<T> xe = mk<T>((a.x + bb.x) * pre, (a.y + bb.y) * pre);
     const Cx<T> xd = mk<T>((a.x - bb.x) * pre, (a.y - bb.y) * pre);
-    const Cx<T> w = __ldg(reinterpret_cast<const Cx<T>*>(pp.ld_tab) + g);
+    const Cx<T> w = c2r_twiddle<T>(pp, g);
     const T tr = fma(w.x, xd.x, -(w.y * xd.y));
     const T ti = fma(w.x, xd.y, w.y * xd.x);
     return mk<T>(xe.x - ti, xe.y + tr);
@@ -1083,7 +1097,18 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
   constexpr int EPT = (R + TF - 1) / TF;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* buf = reinterpret_cast<Cx<T>*>(smem_raw);
-  const uint32_t tile = blockIdx.x;
+  uint32_t tile = blockIdx.x;
+  if constexpr (LOADOP == LOAD_C2R_PRE && MODE == 1) {
+    // The pre-pass reads X[g] and X[h - g]: entry g of tile tp is read again
+    // as the mirror of tile tiles_p - 1 - tp (one column over). Launch order
+    // interleaves each tile with its mirror (0, n-1, 1, n-2, ...), so both
+    // reads of an entry are in flight together and the second hits L2.
+    // tiles_q == 1 in a first pass.
+    const uint32_t n = pp.tiles_p;
+    const uint32_t bt = pp.ftp.div(tile);
+    const uint32_t tl = tile - bt * n;
+    tile = bt * n + ((tl & 1) ? n - 1 - (tl >> 1) : (tl >> 1));
+  }
   const uint32_t t1 = pp.ftq.div(tile);
   const uint32_t tq = tile - t1 * pp.tiles_q;
   const uint32_t tb = pp.ftp.div(t1);

@@ -1161,9 +1161,28 @@ int build_r2c_1d(fftj_plan_s* P, i64 n, i64 nb, i64 idist, i64 odist, std::vecto
     post.rp.nbatch = nb;
     post.rp.z_bstride = h;
     post.rp.y_bstride = odist;
-    std::vector<double> tw(2 * (h + 1));
-    for (i64 k = 0; k <= h; ++k) omega(k, n, -1, &tw[2 * k], &tw[2 * k + 1]);
-    post.rp.tw = upload_cplx<T>(P, tw);
+    // twiddles w_n^k for k <= h/2 (the mirror's is -conj(w^k)): one table,
+    // or for long halves hi[k >> sh] lo[k & (2^sh - 1)] from two small
+    // tables (a table of h/2 entries would stream from HBM beside the data)
+    const i64 nk = h / 2 + 1;
+    post.rp.sh = 0;
+    post.rp.tw2 = nullptr;
+    if (nk > (1 << 16)) {
+      int sh = 0;
+      while (((i64)1 << (2 * sh)) < nk) sh++;
+      const i64 K = (i64)1 << sh, nh = (nk + K - 1) / K;
+      std::vector<double> hi(2 * nh), lo(2 * K);
+      for (i64 u = 0; u < nh; ++u) omega(u * K, n, -1, &hi[2 * u], &hi[2 * u + 1]);
+      for (i64 t = 0; t < K; ++t) omega(t, n, -1, &lo[2 * t], &lo[2 * t + 1]);
+      post.rp.tw = upload_cplx<T>(P, hi);
+      post.rp.tw2 = upload_cplx<T>(P, lo);
+      if (!post.rp.tw2) return fail(FFTJ_ERR_CUDA, "table upload failed");
+      post.rp.sh = sh;
+    } else {
+      std::vector<double> tw(2 * nk);
+      for (i64 k = 0; k < nk; ++k) omega(k, n, -1, &tw[2 * k], &tw[2 * k + 1]);
+      post.rp.tw = upload_cplx<T>(P, tw);
+    }
     if (!post.rp.tw) return fail(FFTJ_ERR_CUDA, "table upload failed");
     post.dst_bytes = (size_t)(nb * odist) * sizeof(T) * 2;
     for (auto& o : inner) ops->push_back(o);
@@ -1206,17 +1225,37 @@ int build_c2r_1d(fftj_plan_s* P, i64 n, i64 nb, i64 idist, i64 odist, bool norma
     const double sc = (normalized ? 1.0 / (double)h : 1.0) * extra_scale;
     int rc = build_c2c_1d<T>(P, h, nb, h, odist / 2, +1, sc, &inner, route);
     if (rc) return rc;
-    std::vector<double> tw(2 * h);
-    for (i64 k = 0; k < h; ++k) omega(k, n, +1, &tw[2 * k], &tw[2 * k + 1]);
-    const void* twd = upload_cplx<T>(P, tw);
-    if (!twd) return fail(FFTJ_ERR_CUDA, "table upload failed");
     PassParams& f = inner.front().pp;
-    if (inner.front().kind == OP_PASS && f.load_op == LOAD_PLAIN) {
+    const bool fused = inner.front().kind == OP_PASS && f.load_op == LOAD_PLAIN;
+    // the pre-pass twiddles w_n^k, k < h: one table, or for a fused pre-pass
+    // of a long half hi[k >> sh] lo[k & (2^sh - 1)] from two small tables
+    // (an h-entry table would stream from HBM beside the data)
+    const void* twd = nullptr;
+    const void* twd_lo = nullptr;
+    int sh = 0;
+    if (fused && h > (1 << 16)) {
+      while (((i64)1 << (2 * sh)) < h) sh++;
+      const i64 K = (i64)1 << sh, nh = (h + K - 1) / K;
+      std::vector<double> hi(2 * nh), lo(2 * K);
+      for (i64 u = 0; u < nh; ++u) omega(u * K, n, +1, &hi[2 * u], &hi[2 * u + 1]);
+      for (i64 t = 0; t < K; ++t) omega(t, n, +1, &lo[2 * t], &lo[2 * t + 1]);
+      twd = upload_cplx<T>(P, hi);
+      twd_lo = upload_cplx<T>(P, lo);
+      if (!twd || !twd_lo) return fail(FFTJ_ERR_CUDA, "table upload failed");
+    } else {
+      std::vector<double> tw(2 * h);
+      for (i64 k = 0; k < h; ++k) omega(k, n, +1, &tw[2 * k], &tw[2 * k + 1]);
+      twd = upload_cplx<T>(P, tw);
+      if (!twd) return fail(FFTJ_ERR_CUDA, "table upload failed");
+    }
+    if (fused) {
       // the pre-pass rides on the first pass's loads
       f.load_op = LOAD_C2R_PRE;
       f.ld_n = h;
       f.ld_stride = idist;
       f.ld_tab = twd;
+      f.ld_tab2 = twd_lo;
+      f.ld_sh = sh;
       f.ld_pre = normalized ? 0.5 : 1.0;
       for (auto& o : inner) ops->push_back(o);
       return FFTJ_OK;
