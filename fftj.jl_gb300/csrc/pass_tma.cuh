@@ -85,10 +85,11 @@ __device__ __forceinline__ void tma_load4(void* dst, const CUtensorMap* map, uin
 // bulk copy per entry; MODE 1: tile = P consecutive columns p (Q == 1, one
 // batch entry), tensor (p, j, batch); MODE 2: tile = Q consecutive columns q
 // (P == 1, one batch entry), tensor (q, p, j, batch). NBC = the tile's
-// column count. Passes of radix above 1024 read their inner twiddles from
-// global memory (L1-resident) instead of staging them.
+// column count. The pass's inner twiddles w_R^t are staged in shared memory
+// once per CTA (up to R = 4096, 32 KB: the radix-4096 single pass then runs
+// two CTAs per SM, measured faster than three reading them through L1).
 template <int R>
-__host__ __device__ constexpr bool tma_stages_twiddles() { return R <= 1024; }
+__host__ __device__ constexpr bool tma_stages_twiddles() { return R <= 4096; }
 
 template <int DIR, int MODE, int NBC, int... Rs>
 __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap* map, const Cx<float>* in,
