@@ -10,7 +10,7 @@
 // each on one stream with CUDA events: warm-up executions, then trials of
 // back-to-back executions long enough to cover launch latency; the figure is
 // the best trial's time per execution. The fastest candidate is the
-// exhaustive choice that the learned cost model is trained on and judged by.
+// exhaustive choice that the learned cost model is trained on and scored against.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -10,8 +10,8 @@ by the library's own CUDA kernels (fftj_mlp_*) on the tuner's timings, that
 predicts the fastest candidate of an unseen size from dry-planned schedule
 features (fftj_plan_features) without timing any of them. Regret of a
 choice = its measured time / the best measured time; the exhaustive tuner is
-the judge, and the fallback when a query lies outside the model's training
-range.
+the yardstick, and the fallback when a query lies outside the model's
+training range.
 
 It also defines the uneven batched workload: transforms with log-uniform
 lengths, a share of them prime, mixed dtypes and a share real-input.

@@ -1,4 +1,4 @@
-"""Measure the GB300 timing set the learned planner is trained and judged on.
+"""Measure the GB300 timing set the learned planner is trained and scored on.
 
 Draws distinct (kind, dtype, length) problems from the uneven workload's
 distribution (fftj.tune.uneven_workload: lengths log-uniform on [64, 2^20],

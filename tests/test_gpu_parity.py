@@ -144,7 +144,7 @@ def test_nd_nonsmooth_dims(fftj, orc, T, shape):
 
 
 # --------------------------------------------------------------------------
-# BASELINE configs at full size
+# the benchmark configurations at full size
 
 
 def test_config_c64_2e16_batch64(fftj, orc):
