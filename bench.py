@@ -837,7 +837,9 @@ def _RDT(ct):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 60 for the GPU workload, about 0.35 s timed so that the clock "
+                         "sampler sees it several times; 20 for the CPU reference arm)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -852,6 +854,8 @@ def main():
     ap.add_argument("--plain-loads", action="store_true",
                     help="configs workload: one-tile-per-CTA kernels only (no pipelined tensor-copy passes)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 20 if args.impl == "reference" or args.workload != "mixed" else 60
     if args.only:
         dt, n = args.only.split(":")
         global PARTS, STEP_FLOPS
