@@ -1,8 +1,10 @@
-// Pipelined pass kernel for F32 multi-pass transforms: the tile columns of a
-// pass are contiguous in HBM row by row (MODE 1: first passes, columns p;
-// MODE 2: later passes, columns q), so a tile is a box of a tensor and
-// arrives in shared memory by TMA tensor copies (cp.async.bulk.tensor)
-// completing on an mbarrier. Each CTA is persistent and double-buffered:
+// Pipelined pass kernel for F32 transforms: the tile columns of a pass of a
+// multi-pass transform are contiguous in HBM row by row (MODE 1: first
+// passes, columns p; MODE 2: later passes, columns q), so a tile is a box of
+// a tensor and arrives in shared memory by TMA tensor copies
+// (cp.async.bulk.tensor); a tile of a single-pass transform (MODE 0) is whole
+// contiguous transforms, one 1-D bulk copy (cp.async.bulk) each. The copies
+// complete on an mbarrier. Each CTA is persistent and double-buffered:
 // while it transforms tile i in one buffer, the copy of its next tile lands
 // in the other, so HBM reads overlap the in-CTA sub-stages instead of
 // waiting for them.

@@ -1,5 +1,7 @@
 // Pipelined tensor-copy pass kernels (pass_tma.cuh), F32, for the power-of-
-// two passes of multi-pass transforms at the planner's default tiles.
+// two passes of multi-pass transforms and the three-sub-stage single passes
+// at the planner's default tiles, with the host helpers that size and launch
+// them.
 #include <algorithm>
 
 #include "pass_tma.cuh"
