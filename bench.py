@@ -1,20 +1,28 @@
 """Benchmark of the FFTJ GB300 transform path.
 
-Workload (one step): the mixed-radix and prime-size configuration — forward
-ComplexF32 and ComplexF64 1-D FFTs at N = 42525 (3^5 5^2 7), N = 10007
-(prime, resampled onto 20480) and N = 2^18, batch 128 each, inputs iid
-standard complex normal from a fixed seed, resident in HBM.
+Default workload (one step): the batched uneven workload -- 10,000 forward
+transforms with lengths log-uniform on [64, 2^20] (15% moved up to the next
+prime, the rest up to the next 13-smooth length), half ComplexF64 and half
+ComplexF32, a fifth of them real-input rfft, plus one Float32 256^3 rfft;
+inputs iid standard normal from a fixed seed, 11.5 GB resident in HBM. The
+step is one persistent work-queue launch (every plan's passes and
+elementwise ops as queue items) captured in a CUDA graph.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload uneven|mixed|configs]
 
-Prints one JSON line. `value` is whole-job GFLOP/s in the 5 N log2 N
-convention with inputs on the device; `e2e` is the same metric through the
-public plan API with pinned host buffers copied in and out every step. Under
-torchrun every rank runs the full workload on its own GPU (replicas: the
-transforms are independent, no collective on the data path) and `value` sums
-the ranks. `--impl reference` times the reference's algorithm on the host
-cores instead: FFTJ restated in C++ (the oracle; Julia is not available), all
-host threads, on a bounded sample of the same workload.
+Prints one JSON line. `value` is whole-job GFLOP/s (5 N log2 N per complex
+transform, 2.5 N log2 N per real one) with inputs on the device; `e2e` is the
+same metric through the public API with pinned host arenas copied in and out
+every step. Under torchrun every rank runs the full workload on its own GPU
+(replicas: the transforms are independent, no collective on the data path)
+and `value` sums the ranks. `--impl reference` times the reference's
+algorithm on the host cores instead: FFTJ restated in C++ (the oracle; Julia
+is not available), all host threads, on a fixed sample of the same item list.
+
+`--workload mixed` is the mixed-radix and prime batch (C32 and C64 at
+N = 42525, 10007, 2^18, batch 128 each); `--workload configs` times the
+other configurations one by one with per-pass HBM rates.
 """
 import argparse
 import json
@@ -45,10 +53,10 @@ def flops(n, batch):
 
 STEP_FLOPS = sum(flops(n, BATCH) for _, n in PARTS)
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
-# part's pass kernels, averaged over its launches, from one ncu capture of
-# this workload on a GB300 (the launch list and the capture command are kept
-# with the profile summaries).
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of a
+# workload's dominant kernel, from one ncu capture on a GB300 (the capture
+# commands are kept with the profile summaries): the C64 2^18 pass kernels of
+# the mixed workload (averaged over their launches).
 NCU_TRAFFIC_PER_LAUNCH = {"c64_262144": 1025.6e6}
 # FP64 pipe busy fraction (sm__inst_executed_pipe_fp64, % of peak sustained
 # while active) of the same part's two pass kernels, averaged, from one ncu
@@ -166,7 +174,7 @@ def cpu_sample(steps_hint=1, max_seconds=20.0):
         nb, BATCH, nt)
 
 
-def run_reference(args):
+def run_reference_mixed(args):
     world, rank, _ = dist_setup()
     if rank != 0:
         return
@@ -190,7 +198,7 @@ def run_reference(args):
 
 # ---------------------------------------------------------------------------
 
-def run_ours(args):
+def run_mixed(args):
     import torch
     import fftj
 
@@ -402,15 +410,17 @@ def run_ours(args):
 
 
 # ---------------------------------------------------------------------------
-# the uneven batched workload (`--workload uneven`)
+# the batched uneven workload (default): 10,000 transforms + one 256^3 rfft
 
 UNEVEN_COUNT = 10000
-UNEVEN_METRIC = "uneven batch GFLOP/s (5N·log2N complex, 2.5N·log2N real)"
+UNEVEN_SEED = 5
+UNEVEN_METRIC = "FFT GFLOP/s (5N·log2N complex, 2.5N·log2N real), uneven batch of 10,000 transforms + 256^3 rfft"
+CPU_SAMPLE_STRIDE = 10   # the CPU arms time every 10th item (1,001 transforms incl. the 256^3 rfft)
 
 
-def uneven_items(count):
+def uneven_items(count, seed=UNEVEN_SEED):
     from fftj import tune
-    items = tune.uneven_workload(count, seed=5)
+    items = tune.uneven_workload(count, seed=seed)
     items.append(("r2c3d", np.float32, (256, 256, 256)))
     return items
 
@@ -420,13 +430,115 @@ def uneven_flops(kind, n):
     return (2.5 if kind.startswith("r2c") else 5.0) * nn * math.log2(nn)
 
 
+def uneven_io_bytes(kind, dt, n):
+    """(input, output) bytes of one item: its algorithmic bytes are one read
+    of the input and one write of the output."""
+    r = np.dtype(dt).itemsize
+    if kind == "c2c":
+        return 2 * r * n, 2 * r * n
+    if kind == "r2c":
+        return r * n, 2 * r * (n // 2 + 1)
+    d0 = n[0]
+    rest = int(np.prod(n[1:]))
+    return r * d0 * rest, 2 * r * (d0 // 2 + 1) * rest
+
+
+def uneven_config(items):
+    """The workload's description, computed from the item list alone (the
+    same dict on the GPU arm and the CPU reference arm)."""
+    from fftj import tune
+    body = items[:-1]
+    nprime = sum(1 for _, _, n in body if tune.is_prime(n))
+    nf64 = sum(1 for _, dt, _ in body if np.dtype(dt) == np.float64)
+    nreal = sum(1 for k, _, _ in body if k == "r2c")
+    ib = sum(uneven_io_bytes(*it)[0] for it in items)
+    ob = sum(uneven_io_bytes(*it)[1] for it in items)
+    return {
+        "workload": "uneven batch: %d forward transforms, N log-uniform on [64, 2^20] (%d prime, the "
+                    "rest snapped up to 13-smooth), %d ComplexF64 / %d ComplexF32, %d real-input rfft, plus one "
+                    "Float32 256^3 rfft" % (len(body), nprime, nf64, len(body) - nf64, nreal),
+        "items": len(items), "seed": UNEVEN_SEED,
+        "step_gflop": round(sum(uneven_flops(k, n) for k, _, n in items) / 1e9, 3),
+        "input_gb": round(ib / 1e9, 3), "output_gb": round(ob / 1e9, 3),
+        "l2": "inputs larger than L2 (%.1f GB of input per step; L2 129 MB)" % (ib / 1e9),
+    }
+
+
+def cpu_uneven(items, steps, warmup, stride=CPU_SAMPLE_STRIDE, nthreads=None):
+    """The FFTJ-restated CPU plans (the oracle: FFTJ's algorithms in C++, all
+    host threads inside each transform as FFTJ runs them, transforms one after
+    another as FFTJ's callers loop) on a fixed sample of the same item list:
+    every `stride`-th item. Returns (GFLOP/s, threads, sample text)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    O.build()
+    nt = nthreads or O.max_threads()
+    sample = items[::stride]
+
+    def mk(it):
+        kind, dt, n = it
+        if kind == "c2c":
+            return O.Plan1D(dt, n, "fft", nthreads=nt)
+        if kind == "r2c":
+            return O.PlanReal(dt, n, "rfft", nthreads=nt)
+        return O.PlanND(dt, n, "rfft", nthreads=nt)
+
+    keys = sorted({(k, np.dtype(d).name, n) for k, d, n in sample}, key=str)
+    with ThreadPoolExecutor(16) as ex:
+        made = dict(zip(keys, ex.map(lambda k: mk((k[0], np.dtype(k[1]).type, k[2])), keys)))
+    rng = np.random.default_rng(0xF17)
+    work = []
+    for kind, dt, n in sample:
+        if kind == "c2c":
+            x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / math.sqrt(2)
+            x = x.astype(np.complex64 if np.dtype(dt) == np.float32 else np.complex128)
+        elif kind == "r2c":
+            x = rng.standard_normal(n).astype(dt)
+        else:
+            x = rng.standard_normal(tuple(reversed(n))).astype(dt)
+        work.append((made[(kind, np.dtype(dt).name, n)], x))
+    fl = sum(uneven_flops(k, n) for k, _, n in sample)
+
+    def one():
+        t0 = time.perf_counter()
+        for p, x in work:
+            p(x)
+        return time.perf_counter() - t0
+
+    for _ in range(warmup):
+        one()
+    ts = [one() for _ in range(steps)]
+    desc = ("every %dth item of the same list (%d transforms, %.2f GFLOP per step incl. the 256^3 rfft): "
+            "FFTJ-restated C++ plans, %d threads inside each transform, transforms in sequence; %d timed steps"
+            % (stride, len(sample), fl / 1e9, nt, steps))
+    return fl * len(ts) / sum(ts) / 1e9, nt, desc
+
+
+def run_reference_uneven(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    items = uneven_items(args.count)
+    value, cores, desc = cpu_uneven(items, args.steps, args.warmup)
+    out = {
+        "impl": "reference", "metric": UNEVEN_METRIC, "value": round(value, 3), "unit": "GFLOP/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic: iid standard normal, seeded", "config": uneven_config(items),
+        "cpu_baseline": {"value": round(value, 3), "unit": "GFLOP/s", "cores": cores, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
 def learned_planner_report():
     """Train the cost model with the library's CUDA kernels on the committed
     GB300 timing set and score its choices on the held-out lengths."""
     from fftj import tune
     path = os.path.join(ROOT, "tests", "golden", "tune_gb300.npz")
     if not os.path.exists(path):
-        return None
+        return None, None
     z = np.load(path)
     ds = {k: z[k] for k in z.files}
     t0 = time.perf_counter()
@@ -449,7 +561,6 @@ def learned_planner_report():
     learned = tune.regrets(ds, held_out, lambda f, o: int(np.argmin(model.predict_log_ms(f))))
     default = tune.regrets(ds, held_out, lambda f, o: int(np.nonzero((o == 0).all(1))[0][0]))
     held_in_r = tune.regrets(ds, held_in, lambda f, o: int(np.argmin(model.predict_log_ms(f))))
-    # planning cost: exhaustive timing of every candidate vs scoring them
     qs = held_out[:20]
     t_model = t_exh = 0.0
     for q in qs:
@@ -506,6 +617,35 @@ def choose_schedules(model, items):
     return out
 
 
+def _arena(specs, dev):
+    """One contiguous device buffer holding every (shape, dtype) view, each
+    view 256-byte aligned. Returns (buffer, views, byte offsets + end)."""
+    import torch
+    offs, off = [], 0
+    for shape, dt in specs:
+        offs.append(off)
+        off += (int(np.prod(shape)) * torch.empty((), dtype=dt).element_size() + 255) // 256 * 256
+    buf = torch.empty(off, dtype=torch.uint8, device=dev)
+    views = []
+    for o, (shape, dt) in zip(offs, specs):
+        nb = int(np.prod(shape)) * torch.empty((), dtype=dt).element_size()
+        views.append(buf[o:o + nb].view(dt).view(shape))
+    return buf, views, offs + [off]
+
+
+def _chunks(offs, n, k):
+    """Split items [0, n) into k contiguous runs of about equal bytes."""
+    total = offs[n]
+    cuts = [0]
+    for c in range(1, k):
+        target = total * c / k
+        i = int(np.searchsorted(offs[:n + 1], target))
+        if cuts[-1] < i < n:
+            cuts.append(i)
+    cuts.append(n)
+    return [(a, b) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
+
+
 def run_uneven(args):
     import torch
     from concurrent.futures import ThreadPoolExecutor
@@ -517,81 +657,87 @@ def run_uneven(args):
         raise SystemExit("bench.py needs a CUDA GPU (there is no CPU path)")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
     fftj.build()
     items = uneven_items(args.count)
+    config = uneven_config(items)
     t0 = time.perf_counter()
 
-    def mk(it):
+    def mk(it, opts=None):
         kind, dt, n = it
         if kind == "r2c3d":
             # column-major dims, as FFTJ's plan_rfft(x) of a 256^3 array
             return fftj.Plan(dt, n, kind="r2c", opts={"threads_max": 256})
-        return fftj.Plan(dt, (n,), kind=kind, opts={"threads_max": 256})
+        o = {"threads_max": 256}
+        if opts:
+            o.update(opts)
+        return fftj.Plan(dt, (n,), kind=kind, opts=o)
 
     with ThreadPoolExecutor(16) as ex:
         plans = list(ex.map(mk, items))
     t_plan = time.perf_counter() - t0
-    # inputs and outputs live in two contiguous arenas (one copy each way e2e)
-    def nbytes(spec):
-        shape, dt = spec
-        return int(np.prod(shape)) * torch.empty((), dtype=dt).element_size()
-
-    def arena(specs):
-        offs, off = [], 0
-        for sp in specs:
-            offs.append(off)
-            off += (nbytes(sp) + 255) // 256 * 256
-        buf = torch.empty(off, dtype=torch.uint8, device=dev)
-        views = [buf[o:o + nbytes(sp)].view(sp[1]).view(sp[0]) for o, sp in zip(offs, specs)]
-        return buf, views
-
-    in_buf, xs = arena([p.in_spec() for p in plans])
-    out_buf, ys = arena([p.out_spec() for p in plans])
+    in_buf, xs, in_offs = _arena([p.in_spec() for p in plans], dev)
+    out_buf, ys, out_offs = _arena([p.out_spec() for p in plans], dev)
     gen = torch.Generator(device=dev)
-    gen.manual_seed(0xF17)
+    gen.manual_seed(0xF17 + rank)
     for x in xs:
         x.copy_(torch.randn(x.shape, dtype=x.dtype, device=dev, generator=gen))
     step_flops = sum(uneven_flops(k, n) for k, _, n in items)
-    groups = {}
-    for mode in ("persistent", "graph", "stream"):
-        groups[mode] = fftj.Group(plans, xs, ys, mode=mode)
+    alg_bytes = sum(sum(uneven_io_bytes(*it)) for it in items)
     stream = torch.cuda.current_stream(dev)
 
-    def time_mode(g, steps):
-        for _ in range(max(args.warmup, 3)):
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize(dev)
+
+    def time_group(g, steps, warm):
+        for _ in range(warm):
             g()
         g.status()
-        torch.cuda.synchronize(dev)
+        barrier()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
         for _ in range(steps):
             g()
         b.record(stream)
-        torch.cuda.synchronize(dev)
+        barrier()
         g.status()
         return a.elapsed_time(b) / steps
 
-    modes = {}
+    # ---- the step: one persistent work-queue launch in a CUDA graph
+    g_pers = fftj.Group(plans, xs, ys, mode="persistent")
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
+        g_pers()
+    g_pers.status()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        for mode in ("persistent", "graph", "stream"):
-            ms = time_mode(groups[mode], args.steps)
-            inf = groups[mode].info
-            modes[mode] = {"ms": round(ms, 3), "gflops": round(step_flops / (ms * 1e-3) / 1e9, 1),
-                           "kernels_per_step": int(inf.kernels)}
-            if mode == "persistent":
-                modes[mode].update({"ctas": int(inf.ctas), "queue_items": int(inf.nitems),
-                                    "smem_bytes": int(inf.smem_bytes)})
-            if mode == "graph":
-                modes[mode]["branches"] = int(inf.branches)
-    ms = modes["persistent"]["ms"]
-    value = step_flops * world / (ms * 1e-3) / 1e9
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            g_pers()
+        e1.record(stream)
+        barrier()
+    g_pers.status()
+    ms, job_flops = replica_reduce(e0.elapsed_time(e1) / args.steps, step_flops, pg, dev)
+    value = job_flops / (ms * 1e-3) / 1e9
+    inf = g_pers.info
+    modes = {"persistent": {"ms": round(ms, 3), "gflops": round(step_flops / (ms * 1e-3) / 1e9, 1),
+                            "kernels_per_step": int(inf.kernels), "ctas": int(inf.ctas),
+                            "queue_items": int(inf.nitems), "smem_bytes": int(inf.smem_bytes)}}
 
-    # outputs of the persistent form against numpy (a sample of transforms)
-    groups["persistent"]()
-    groups["persistent"].status()
+    # ---- outputs of the timed form against FP64 numpy (a sample of items)
     rng = np.random.default_rng(3)
-    check = sorted(set(rng.choice(len(items) - 1, 40, replace=False).tolist()) | {len(items) - 1})
+    check = sorted(set(rng.choice(len(items) - 1, min(40, len(items) - 1), replace=False).tolist())
+                   | {len(items) - 1})
     worst = {}
     for i in check:
         kind, dt, n = items[i]
@@ -607,80 +753,269 @@ def run_uneven(args):
         key = "%s_%s" % (kind, np.dtype(dt).name)
         worst[key] = max(worst.get(key, 0.0), err)
 
-    # e2e: inputs copied in from pinned host memory, the group run, outputs
-    # copied back, every step
+    # ---- the other group forms, and the step split by kind of transform
+    # (CUDA-graph groups of each subset)
+    if not args.quick:
+        g = fftj.Group(plans, xs, ys, mode="graph")
+        t = time_group(g, args.steps, warm)
+        modes["graph"] = {"ms": round(t, 3), "gflops": round(step_flops / (t * 1e-3) / 1e9, 1),
+                          "kernels_per_step": int(g.info.kernels), "branches": int(g.info.branches)}
+        del g
+        g = fftj.Group(plans, xs, ys, mode="stream")
+        t = time_group(g, 2, 1)
+        modes["stream"] = {"ms": round(t, 3), "gflops": round(step_flops / (t * 1e-3) / 1e9, 1),
+                           "kernels_per_step": int(g.info.kernels)}
+        del g
+    split = {}
+    cats = {}
+    for i, (kind, dt, n) in enumerate(items):
+        if kind == "r2c3d":
+            key = "rfft_f32_256^3"
+        else:
+            key = "%s_%s%s" % (kind, "f64" if np.dtype(dt) == np.float64 else "f32",
+                               "_prime" if fftj.tune.is_prime(n) else "")
+        cats.setdefault(key, []).append(i)
+    for key, idx in sorted(cats.items()):
+        for mode in ("persistent",) + (() if args.quick else ("graph",)):
+            g = fftj.Group([plans[i] for i in idx], [xs[i] for i in idx], [ys[i] for i in idx], mode=mode)
+            t = time_group(g, max(3, min(args.steps, 10)), 2)
+            fl = sum(uneven_flops(items[i][0], items[i][2]) for i in idx)
+            split.setdefault(key, {"transforms": len(idx), "gflop": round(fl / 1e9, 3)})
+            split[key][mode + "_ms"] = round(t, 3)
+            split[key][mode + "_gflops"] = round(fl / (t * 1e-3) / 1e9, 1)
+            del g
+
+    # ---- e2e through the public API: pinned host arenas copied in and out
+    # every step. The plans are split into contiguous chunks of about equal
+    # bytes, each a persistent group; chunk c's input copy (one stream),
+    # transform (the compute stream) and output copy (a third stream) are
+    # ordered by events, so copies of one chunk overlap the transforms of
+    # another.
     h_in = torch.empty(in_buf.numel(), dtype=torch.uint8, pin_memory=True)
     h_in.copy_(in_buf)
     h_out = torch.empty(out_buf.numel(), dtype=torch.uint8, pin_memory=True)
-    g = groups["persistent"]
+    n_items = len(items)
+    chunks = _chunks(in_offs, n_items, args.e2e_chunks)
+    cgroups = [fftj.Group(plans[a:b], xs[a:b], ys[a:b], mode="persistent") for a, b in chunks]
+    s_in = torch.cuda.Stream(dev)
+    s_out = torch.cuda.Stream(dev)
+    nc = len(chunks)
+    ev_h2d = [torch.cuda.Event() for _ in range(nc)]
+    ev_done = [torch.cuda.Event() for _ in range(nc)]
+    ev_d2h = [torch.cuda.Event() for _ in range(nc)]
+    for c in range(nc):
+        ev_done[c].record(stream)
+        ev_d2h[c].record(stream)
+
+    def e2e_step():
+        for c, (a, b) in enumerate(chunks):
+            s_in.wait_event(ev_done[c])      # the previous step's chunk c no longer reads its input
+            with torch.cuda.stream(s_in):
+                in_buf[in_offs[a]:in_offs[b]].copy_(h_in[in_offs[a]:in_offs[b]], non_blocking=True)
+            ev_h2d[c].record(s_in)
+        for c, (a, b) in enumerate(chunks):
+            stream.wait_event(ev_h2d[c])
+            stream.wait_event(ev_d2h[c])     # the previous step's chunk c output is on the host
+            cgroups[c]()
+            ev_done[c].record(stream)
+            s_out.wait_event(ev_done[c])
+            with torch.cuda.stream(s_out):
+                h_out[out_offs[a]:out_offs[b]].copy_(out_buf[out_offs[a]:out_offs[b]], non_blocking=True)
+            ev_d2h[c].record(s_out)
+
+    def drain():
+        for c in range(nc):
+            stream.wait_event(ev_d2h[c])
+
     for _ in range(2):
-        in_buf.copy_(h_in, non_blocking=True)
-        g()
-        h_out.copy_(out_buf, non_blocking=True)
-    torch.cuda.synchronize(dev)
+        e2e_step()
+    drain()
+    barrier()
     a = torch.cuda.Event(enable_timing=True)
     b = torch.cuda.Event(enable_timing=True)
-    e2e_steps = max(3, min(args.steps, 5))
+    e2e_steps = max(3, min(args.steps, 8))
     a.record(stream)
+    s_in.wait_event(a)
+    s_out.wait_event(a)
     for _ in range(e2e_steps):
-        in_buf.copy_(h_in, non_blocking=True)
-        g()
-        h_out.copy_(out_buf, non_blocking=True)
+        e2e_step()
+    drain()
     b.record(stream)
-    torch.cuda.synchronize(dev)
-    g.status()
-    e2e_ms = a.elapsed_time(b) / e2e_steps
-    e2e_ok = torch.equal(h_out, out_buf.cpu())
+    barrier()
+    for gq in cgroups:
+        gq.status()
+    e2e_ms, _ = replica_reduce(a.elapsed_time(b) / e2e_steps, step_flops, pg, dev)
+    e2e_value = job_flops / (e2e_ms * 1e-3) / 1e9
+    # the last step's outputs arrived on the host intact (64 windows of 1 MB)
+    win = 1 << 20
+    starts = np.random.default_rng(7).integers(0, max(1, out_buf.numel() - win), 64)
+    e2e_ok = all(torch.equal(h_out[s:s + win], out_buf[s:s + win].cpu()) for s in starts.tolist())
+    del cgroups
 
-    learned, model = learned_planner_report() if not args.no_learned else (None, None)
-    if model is not None:
-        # the whole batch with the planner's default schedules and with the
-        # model's, both as a CUDA-graph group (no thread cap)
-        from fftj import tune
-        t0 = time.perf_counter()
-        chosen = choose_schedules(model, items[:-1])
-        t_choose = time.perf_counter() - t0
+    # ---- roofline of the dominant kernel: the persistent kernel is the only
+    # kernel of the step; its algorithmic bytes are one read of every input
+    # and one write of every output
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    roofline = {
+        "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+        "frac": round(achieved / peak, 4), "traffic": NCU_TRAFFIC_PER_LAUNCH.get("k_group_uneven"),
+        "peak_source": peak_kind, "kernel": "k_group (persistent work queue, one launch per step)",
+        "alg_bytes_per_launch": int(alg_bytes),
+        "note": "algorithmic bytes = one read of each input + one write of each output; multi-pass "
+                "transforms re-read their data, and ComplexF64 passes are bound by the FP64 pipe, not HBM",
+    }
 
-        def mk_opts(it, opts):
-            kind, dt, n = it
-            if kind == "r2c3d":
-                return fftj.Plan(dt, n, kind="r2c")
-            return fftj.Plan(dt, (n,), kind=kind, opts=dict(zip(tune.OPT_FIELDS, opts)) if opts else None)
+    learned = None
+    if not args.no_learned and not args.quick:
+        learned, model = learned_planner_report()
+        if model is not None:
+            from fftj import tune
+            t0 = time.perf_counter()
+            chosen = choose_schedules(model, items[:-1])
+            t_choose = time.perf_counter() - t0
+            for label, sched in (("default", [None] * (len(items) - 1)), ("learned", chosen)):
+                def mk2(arg):
+                    it, opts = arg
+                    kind, dt, n = it
+                    if kind == "r2c3d":
+                        return fftj.Plan(dt, n, kind="r2c")
+                    return fftj.Plan(dt, (n,), kind=kind,
+                                     opts=dict(zip(tune.OPT_FIELDS, opts)) if opts else None)
+                with ThreadPoolExecutor(16) as ex:
+                    pl = list(ex.map(mk2, zip(items, sched + [None])))
+                g = fftj.Group(pl, xs, ys, mode="graph")
+                t = time_group(g, max(3, min(args.steps, 10)), 2)
+                learned["graph_%s_schedules" % label] = {"ms": round(t, 3),
+                                                         "gflops": round(step_flops / (t * 1e-3) / 1e9, 1)}
+                del g, pl
+            learned["choose_seconds_10000"] = round(t_choose, 2)
+            learned["schedules_changed"] = int(sum(1 for c in chosen if any(c)))
 
-        for label, sched in (("default", [None] * (len(items) - 1)), ("learned", chosen)):
-            with ThreadPoolExecutor(16) as ex:
-                pl = list(ex.map(lambda a: mk_opts(*a), zip(items, sched + [None])))
-            g = fftj.Group(pl, xs, ys, mode="graph")
-            ms_g = time_mode(g, args.steps)
-            learned["graph_%s_schedules" % label] = {"ms": round(ms_g, 3),
-                                                     "gflops": round(step_flops / (ms_g * 1e-3) / 1e9, 1)}
-            del g, pl
-        learned["choose_seconds_10000"] = round(t_choose, 2)
-        learned["schedules_changed"] = int(sum(1 for c in chosen if any(c)))
-    nprime = sum(1 for k, _, n in items[:-1] if not isinstance(n, tuple) and fftj.tune.is_prime(n))
+    extra = {}
+    if not args.quick:
+        extra["mixed_prime_batch128"] = mixed_parts_breakdown(dev)
+        extra["precision_form"] = precision_breakdown(dev)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, cores, desc = cpu_uneven(items, 1, 1)
+        cpu = {"value": round(v, 3), "unit": "GFLOP/s", "cores": cores, "kind": "port", "sample": desc}
+
     if rank == 0:
         out = {
             "metric": UNEVEN_METRIC, "value": round(value, 1), "unit": "GFLOP/s", "n_gpus": world,
-            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 3),
+            "steps": args.steps, "warmup": warm, "ms_per_step": round(ms, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic: iid standard normal (seeded torch generator)",
-            "config": {
-                "workload": "%d transforms, N log-uniform on [64, 2^20] (%d prime, the rest snapped up to "
-                            "13-smooth), half C64, a fifth real-input rfft, plus one F32 256^3 rfft"
-                            % (len(items) - 1, nprime),
-                "plans_seconds": round(t_plan, 1), "plans": len(plans),
-                "input_gb": round(in_buf.numel() / 1e9, 2), "output_gb": round(out_buf.numel() / 1e9, 2),
-                "l2": "inputs larger than L2 (%.1f GB)" % (in_buf.numel() / 1e9),
-                "modes": modes, "rel_l2_vs_fp64_worst": {k: float("%.3g" % v) for k, v in worst.items()},
-                "learned_planner": learned},
-            "e2e": {"value": round(step_flops / (e2e_ms * 1e-3) / 1e9, 1), "unit": "GFLOP/s",
-                    "h2d_bytes_per_step": int(in_buf.numel()), "d2h_bytes_per_step": int(out_buf.numel()),
+            "config": config,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_value, 1), "unit": "GFLOP/s",
+                    "h2d_bytes_per_step": int(in_offs[-1]), "d2h_bytes_per_step": int(out_offs[-1]),
                     "ms_per_step": round(e2e_ms, 3), "outputs_checked": bool(e2e_ok),
-                    "schedule": "one H2D copy of the input arena, the persistent group, one D2H copy"},
-            "gpu_launches": args.steps,
+                    "schedule": "plans split into %d chunks of about equal bytes, each a persistent group; "
+                                "per chunk: H2D from pinned host (stream 1), group (stream 2), D2H to pinned "
+                                "host (stream 3), ordered by events" % nc},
+            "gpu_launches": int(inf.kernels) * args.steps,
             "clocks": clk.summary(),
+            "detail": {"plans_seconds": round(t_plan, 1), "modes": modes, "by_kind": split,
+                       "rel_l2_vs_fp64_worst": {k: float("%.3g" % v) for k, v in worst.items()},
+                       "learned_planner": learned, **extra},
         }
         print(json.dumps(out))
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+def mixed_parts_breakdown(dev, reps=5):
+    """The mixed batch's six parts (forward C32/C64 at 42525, 10007, 2^18, batch
+    128) timed one plan at a time (CUDA events), for the default line's
+    breakdown."""
+    import torch
+    import fftj
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0xF17)
+    stream = torch.cuda.current_stream(dev)
+    parts = {}
+    for dt, n in PARTS:
+        T = np.float32 if dt == "c32" else np.float64
+        ct = torch.complex64 if dt == "c32" else torch.complex128
+        p = fftj.plan_fft(T, n, batch=BATCH)
+        x = torch.randn((BATCH, n), dtype=ct, device=dev, generator=gen)
+        y = torch.empty_like(x)
+        for _ in range(3):
+            p(y, x)
+        torch.cuda.synchronize(dev)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            p(y, x)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        pms = a.elapsed_time(b) / reps
+        ref = np.fft.fft(x[:2].cpu().numpy().astype(np.complex128), axis=-1)
+        got = y[:2].cpu().numpy().astype(np.complex128)
+        parts["%s_%d" % (dt, n)] = {
+            "ms": round(pms, 4), "gflops": round(flops(n, BATCH) / pms / 1e6, 1),
+            "alg_gbs": round(2.0 * x.numel() * x.element_size() / pms / 1e6, 1), "route": p.route,
+            "passes": [int(v) for v in p.info.pass_radix[:p.info.npasses]],
+            "rel_l2_vs_fp64": float("%.3g" % (np.linalg.norm(got - ref) / np.linalg.norm(ref)))}
+        del p, x, y
+    tot = sum(v["ms"] for v in parts.values())
+    return {"step_ms": round(tot, 4), "gflops": round(STEP_FLOPS / tot / 1e6, 1), "parts": parts}
+
+
+def precision_breakdown(dev, reps=10):
+    """The precision form against the plain form: C32 2^20 x64 and C32 4096 x 4096
+    (standard normal, 1% of entries x1e3), plain FP32 butterflies against the
+    FP16 hi+lo tensor-core radix-16 form; GFLOP/s and rel-L2 vs FP64."""
+    import torch
+    import fftj
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0xF17)
+    stream = torch.cuda.current_stream(dev)
+    out = {}
+    for label, dims, batch in (("c32_2^20_x64", (1 << 20,), 64), ("c32_4096x4096", (4096, 4096), 1)):
+        shape = (batch,) + tuple(reversed(dims)) if batch > 1 else tuple(reversed(dims))
+        x = torch.randn(shape, dtype=torch.complex64, device=dev, generator=gen)
+        flat = x.view(-1)
+        idx = torch.randperm(flat.numel(), generator=gen, device=dev)[: flat.numel() // 100]
+        flat[idx] *= 1e3
+        n = int(np.prod(dims))
+        fl = 5.0 * n * math.log2(n) * batch
+        xs = x.cpu().numpy()
+        if len(dims) == 1:
+            ref = np.fft.fft(xs[:2].astype(np.complex128), axis=-1)
+        else:
+            ref = np.fft.fftn(xs.astype(np.complex128))
+        row = {}
+        for form, prec in (("plain_fp32", 0), ("fp16_hilo_tensor_core", 1)):
+            p = fftj.Plan(np.float32, dims, kind="c2c", batch=batch, opts={"precision": prec})
+            y = torch.empty_like(x)
+            for _ in range(3):
+                p(y, x)
+            torch.cuda.synchronize(dev)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                p(y, x)
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            t = a.elapsed_time(b) / reps
+            got = y.cpu().numpy().astype(np.complex128)
+            got = got[:2] if len(dims) == 1 else got
+            row[form] = {"ms": round(t, 4), "gflops": round(fl / (t * 1e-3) / 1e9, 1),
+                         "tc_substages": int(p.info.tc_substages),
+                         "rel_l2_vs_fp64": float("%.3g" % (np.linalg.norm(got - ref) / np.linalg.norm(ref)))}
+            del p, y
+        row["chosen_over_plain"] = round(row["plain_fp32"]["ms"] / row["fp16_hilo_tensor_core"]["ms"], 3)
+        out[label] = row
+        del x
+        torch.cuda.empty_cache()
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -838,37 +1173,45 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed steps (default: 60 for the GPU workload, about 0.35 s timed so that the clock "
-                         "sampler sees it several times; 20 for the CPU reference arm)")
+                    help="timed steps (default 10 for the uneven workload, 60 for mixed, 20 for configs and "
+                         "for the CPU reference arm)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--only", default=None,
-                    help="run one part only, e.g. c32:262144 (profiling a single plan)")
-    ap.add_argument("--workload", default="mixed", choices=["mixed", "uneven", "configs"],
-                    help="mixed: the mixed-radix/prime batch (default); uneven: 10,000 uneven transforms "
-                         "as one group, plus the learned planner's regret")
+                    help="mixed workload: run one part only, e.g. c32:262144 (profiling a single plan)")
+    ap.add_argument("--workload", default="uneven", choices=["uneven", "mixed", "configs"],
+                    help="uneven: 10,000 uneven transforms + 256^3 rfft as one persistent group (default); "
+                         "mixed: the mixed-radix/prime batch; configs: the other configurations")
     ap.add_argument("--count", type=int, default=UNEVEN_COUNT, help="transforms of the uneven workload")
+    ap.add_argument("--e2e-chunks", type=int, default=6, help="uneven workload: chunks of the e2e pipeline")
+    ap.add_argument("--quick", action="store_true",
+                    help="uneven workload: the timed step, e2e and accuracy only (no other forms or breakdowns)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned planner report")
     ap.add_argument("--case", default=None, help="configs workload: only these cases (comma-separated labels)")
     ap.add_argument("--plain-loads", action="store_true",
                     help="configs workload: one-tile-per-CTA kernels only (no pipelined tensor-copy passes)")
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = 20 if args.impl == "reference" or args.workload != "mixed" else 60
+        args.steps = {"uneven": 10, "mixed": 60, "configs": 20}[args.workload]
+        if args.impl == "reference":
+            args.steps = 20 if args.workload != "uneven" else 10
     if args.only:
         dt, n = args.only.split(":")
         global PARTS, STEP_FLOPS
         PARTS = [(dt, int(n))]
         STEP_FLOPS = sum(flops(nn, BATCH) for _, nn in PARTS)
     if args.impl == "reference":
-        run_reference(args)
+        if args.workload == "mixed":
+            run_reference_mixed(args)
+        else:
+            run_reference_uneven(args)
     elif args.workload == "uneven":
         run_uneven(args)
     elif args.workload == "configs":
         run_configs(args)
     else:
-        run_ours(args)
+        run_mixed(args)
 
 
 if __name__ == "__main__":

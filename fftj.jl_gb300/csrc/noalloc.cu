@@ -1,10 +1,10 @@
 // Allocation-free transform entry point (no counterpart in the reference).
 //
 // Some callers cannot allocate device memory when they need a transform:
-// code recording a CUDA stream capture (cudaMalloc is not a capturable
-// operation), real-time pipelines that forbid allocation once running, and
-// hosts that own every byte of device memory through their own pool and have
-// no way to hand a plan its workspace. Plans (fftj_plan_c2c) allocate their
+// real-time pipelines that forbid allocation once running (an allocation can
+// block on the driver for an unbounded time), and hosts that own every byte
+// of device memory through their own pool and have no way to hand a plan its
+// workspace. Plans (fftj_plan_c2c) allocate their
 // twiddle tables and workspace when they are created; this entry point
 // allocates nothing. Its scratch -- the intermediate of a two-pass transform
 // and the twiddle tables, which it regenerates on the device on every call --
@@ -26,8 +26,9 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 // Device addresses of g_noalloc_scratch, one per device, looked up on the
-// first call made with that device current. (In host code the symbol's name
-// is a host-side stand-in, not a device address.)
+// first call made with that device current and kept for the life of the
+// process (a device reset after that first call is not supported). In host
+// code the symbol's name is a host-side stand-in, not a device address.
 static void* g_scratch_addr[kMaxDevices];
 static std::mutex g_scratch_mu;
 
@@ -100,6 +101,7 @@ static int run_noalloc(int64_t n, int64_t batch, int dir, double scale, const vo
     if (cursor > kNoAllocTableBytes) return nullptr;
     const int th = 256;
     k_fill_omega<T><<<(unsigned)((count + th - 1) / th), th, 0, st>>>(p, count, stride, modn, dir);
+    if (cudaGetLastError() != cudaSuccess) return nullptr;  // this launch's own error
     return p;
   };
 
@@ -123,22 +125,20 @@ static int run_noalloc(int64_t n, int64_t batch, int dir, double scale, const vo
       p.tw_hi = table((ncur + K - 1) / K, K, ncur);
       p.tw_lo = table(K, 1, ncur);
       if (!p.tw_hi || !p.tw_lo) {
-        set_error("fftj_execute_noalloc_c2c: twiddle tables exceed the table region");
+        set_error("fftj_execute_noalloc_c2c: twiddle tables exceed the table region, or their generation "
+                  "failed to launch");
         return FFTJ_ERR_UNSUPPORTED;
       }
     }
     if (!p.twR) {
-      set_error("fftj_execute_noalloc_c2c: twiddle tables exceed the table region");
+      set_error("fftj_execute_noalloc_c2c: twiddle tables exceed the table region, or their generation "
+                "failed to launch");
       return FFTJ_ERR_UNSUPPORTED;
     }
     p.scale = (i + 1 == npass) ? scale : 1.0;
     p.load_op = LOAD_PLAIN;
     s1 *= R;
     ncur /= R;
-  }
-  if (cudaGetLastError() != cudaSuccess) {
-    set_error("fftj_execute_noalloc_c2c: twiddle generation launch failed");
-    return FFTJ_ERR_CUDA;
   }
   const void* src = d_in;
   for (int i = 0; i < npass; ++i) {
@@ -168,6 +168,13 @@ extern "C" int fftj_execute_noalloc_c2c(int dtype, int64_t n, int64_t batch, int
   if (n < 1 || batch < 1 || (dir != -1 && dir != 1) || !d_in || !d_out) {
     set_error("fftj_execute_noalloc_c2c: bad length, batch, direction or pointer");
     return FFTJ_ERR_ARG;
+  }
+  // an error left pending by earlier work on this thread is reported as such
+  // (and left pending) rather than blamed on this call's launches
+  const cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess) {
+    set_error("fftj_execute_noalloc_c2c: a CUDA error from earlier work is pending on this thread");
+    return FFTJ_ERR_CUDA;
   }
   cudaStream_t st = (cudaStream_t)stream;
   return dtype == FFTJ_F32 ? run_noalloc<float>(n, batch, dir, scale, d_in, d_out, st)

@@ -18,7 +18,13 @@
 //
 // Every wait is bounded: a copy that has not landed after the plan's wait
 // limit sets a status word the host reads (fftj_plan_status), and the CTA
-// waits (again bounded) for its copies in flight and returns.
+// waits (again bounded) for its copies in flight and returns. The slot
+// barriers track only the real copies (the test hook's never-arriving bytes
+// sit on a barrier of their own), so that drain observes the copies
+// themselves: when it succeeds no copy into this CTA's shared memory is in
+// flight as it exits. Only when the copies themselves never land does the
+// CTA exit with them outstanding; the host then treats the whole stream's
+// results as lost (fftj_plan_status).
 #pragma once
 #include <cuda.h>
 
@@ -128,11 +134,18 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
     const Cx<T>* twG = reinterpret_cast<const Cx<T>*>(pp.twR);
     for (int t = tid; t < R; t += nthr) twS[t] = __ldg(twG + t);
   }
+  // bar[0], bar[1]: the two tile slots (real copies only); bar[2]: the test
+  // hook (fftj_plan_debug_stall) -- armed once with bytes that never arrive,
+  // and waited on after each slot's barrier, so every tile wait times out
+  // while the slot barriers still see their copies land
+  const uint32_t extra_tx = (uint32_t)pp.tma_extra_tx;
   if (tid == 0) {
     mbar_init(bar, 1);
     mbar_init(bar + 1, 1);
+    mbar_init(bar + 2, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (extra_tx) mbar_arrive_expect_tx(bar + 2, extra_tx);
   }
   __syncthreads();
   // one thread arms the slot's barrier with the tile's bytes and issues the
@@ -147,11 +160,11 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
       // the tile's batch entries that exist, each R contiguous elements
       const int64_t b0 = (int64_t)tb * NB;
       const int nv = (int)min((int64_t)NB, pp.nbatch - b0);
-      mbar_arrive_expect_tx(bar + slot, (uint32_t)(nv * R * sizeof(Cx<T>)) + (uint32_t)pp.tma_extra_tx);
+      mbar_arrive_expect_tx(bar + slot, (uint32_t)(nv * R * sizeof(Cx<T>)));
       for (int c = 0; c < nv; ++c)
         bulk_load(dst + c * R, in + (b0 + c) * pp.in_bstride, (uint32_t)(R * sizeof(Cx<T>)), bar + slot);
     } else {
-      mbar_arrive_expect_tx(bar + slot, kTx + (uint32_t)pp.tma_extra_tx);
+      mbar_arrive_expect_tx(bar + slot, kTx);
       for (int j0 = 0; j0 < R; j0 += rows) {
         if constexpr (MODE == 1)
           tma_load3(dst + j0 * NB, map, bar + slot, (int)(tp * (uint32_t)pp.P), j0, (int)tb);
@@ -172,12 +185,15 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       issue(nxt, slot ^ 1);
     }
-    const bool ok = mbar_wait(bar + slot, (it >> 1) & 1, limit);
+    const bool ok = mbar_wait(bar + slot, (it >> 1) & 1, limit) && (extra_tx == 0 || mbar_wait(bar + 2, 0, limit));
     if (__syncthreads_or(!ok)) {
+      // drain: wait (bounded) for this tile's copies and the next tile's,
+      // on the slot barriers that count only real copy bytes
       if (tid == 0) {
         atomicOr(status, 1u);
-        mbar_wait(bar + slot, (it >> 1) & 1, limit);
-        if (nxt < ntiles) mbar_wait(bar + (slot ^ 1), ((it + 1) >> 1) & 1, limit);
+        bool drained = mbar_wait(bar + slot, (it >> 1) & 1, limit);
+        if (nxt < ntiles) drained = mbar_wait(bar + (slot ^ 1), ((it + 1) >> 1) & 1, limit) && drained;
+        if (!drained) atomicOr(status, 2u);  // copies still in flight at exit
       }
       __syncthreads();
       return;

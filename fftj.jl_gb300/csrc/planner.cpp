@@ -1752,6 +1752,10 @@ int fftj_plan_status(fftj_plan plan, void* stream) {
     return fail(FFTJ_ERR_CUDA, "status read failed");
   if (st) {
     cudaMemset(plan->d_status, 0, sizeof(unsigned));
+    if (st & 2u)
+      return fail(FFTJ_ERR_TIMEOUT,
+                  "a pipelined pass gave up waiting for a tile's tensor copy and exited with copies in flight: "
+                  "treat every result produced on this stream since the previous status check as lost");
     return fail(FFTJ_ERR_TIMEOUT, "a pipelined pass gave up waiting for a tile's tensor copy; its output is incomplete");
   }
   g_err.clear();

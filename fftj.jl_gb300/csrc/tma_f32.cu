@@ -38,7 +38,7 @@ const RecipeEntry* tma_table(int dir, int* count) {
 
 size_t tma_smem_bytes(const PassParams& pp) {
   const int tw = pp.R <= 4096 ? pp.R : 0;  // tma_stages_twiddles
-  return (size_t)(2 * pp.tma_buf + tw) * sizeof(Cx<float>) + 2 * sizeof(uint64_t);
+  return (size_t)(2 * pp.tma_buf + tw) * sizeof(Cx<float>) + 3 * sizeof(uint64_t);  // 3 mbarriers
 }
 
 // Opts the kernel into the shared memory it needs and returns how many CTAs

@@ -244,8 +244,13 @@ int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info);
  * Pipelined passes (F32 power-of-two passes of multi-pass transforms) wait
  * for their tiles' tensor copies with a bounded wait. fftj_plan_status
  * synchronises `stream` and returns FFTJ_ERR_TIMEOUT if a wait of an earlier
- * execution gave up (the status is then cleared). No counterpart in the
- * reference (host code has no device waits).
+ * execution gave up (the status is then cleared). After such a timeout the
+ * CTA waits, again bounded, for the copies it issued before it exits; the
+ * plan's output is then incomplete. If even those copies never landed, the
+ * CTA exited with copies into shared memory in flight, which can disturb
+ * other work on the GPU: the error message says so, and the caller should
+ * treat every result produced on the stream since its previous status check
+ * as lost. No counterpart in the reference (host code has no device waits).
  */
 int fftj_plan_status(fftj_plan plan, void* stream);
 /* Bound of each such wait in nanoseconds (default 1e9). */
@@ -269,9 +274,10 @@ const char* fftj_version(void);
 /*
  * Allocation-free complex transform. No counterpart in the reference: it is
  * for callers that cannot allocate device memory when they transform, such
- * as code recording a CUDA stream capture (cudaMalloc cannot be captured),
- * real-time loops that forbid allocation after start-up, and hosts that own
- * all device memory through their own pool. It creates no plan and calls no
+ * as real-time loops that forbid allocation once they run (an allocation can
+ * block on the driver for an unbounded time), and hosts that own all device
+ * memory through their own pool and cannot hand a plan its workspace. It
+ * creates no plan and calls no
  * cudaMalloc, cudaFree or other allocating routine: its scratch is a
  * file-scope static device array of 64 MiB (1 MiB of twiddle tables,
  * regenerated on the device on every call, and 63 MiB for the intermediate
@@ -280,8 +286,11 @@ const char* fftj_version(void);
  * for two passes batch * n * sizeof(complex) <= 63 MiB; larger requests
  * return FFTJ_ERR_ARG / FFTJ_ERR_UNSUPPORTED with a message. d_in/d_out hold
  * batch dense transforms; in == out is allowed. The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) and should
- * come before any stream capture. All calls share the one array: calls that
+ * looks up the array's device address (cudaGetSymbolAddress) and keeps it,
+ * so it should come before any stream capture, and a device reset
+ * (cudaDeviceReset) after that first call is not supported: the kept address
+ * would be stale. A CUDA error already pending on the calling thread is
+ * reported as FFTJ_ERR_CUDA and left pending. All calls share the one array: calls that
  * overlap on the GPU (other streams, other threads) race and must be
  * serialised by the caller. Nothing in the array needs to start at zero.
  */

@@ -1,9 +1,9 @@
 """The allocation-free entry point, fftj_execute_noalloc_c2c.
 
 It serves callers that cannot allocate device memory at the moment they
-transform -- code recording a CUDA stream capture (cudaMalloc cannot be
-captured), real-time loops that forbid allocation after start-up, and hosts
-that own all device memory through their own pool. Instead of a plan's
+transform -- real-time loops that forbid allocation after start-up (an
+allocation can block on the driver for an unbounded time), and hosts that own
+all device memory through their own pool. Instead of a plan's
 workspace it uses one static device array inside the library, so this test
 checks, through the C ABI, that its outputs match the plan path
 (fftj_plan_c2c + fftj_execute) within the parity tolerance on two calls in a
