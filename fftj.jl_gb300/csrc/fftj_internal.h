@@ -75,6 +75,10 @@ struct PassParams {
   int smem_elems;          // padded elements per buffer
   int smem_tw_elems;       // extra shared elements (recipe kernels stage w_R^t there)
   int tc;                  // radix-16 sub-stages on tensor cores: 0 off, 1 FP16 hi+lo, 2 BF16 hi+lo (F32)
+  int fx;                  // 1: ComplexF64 data computed in block fixed point (fx64.cuh), twiddles Q61
+  int fx_cols;             // ints of shared memory for the column exponents (fx: NB, else 0)
+  int fx_b0;               // fx: headroom bits of the inputs (61 - ceil(log2 r0))
+  int fx_sht;              // fx: sum of the sub-stage boundary shifts (ceil(log2 r) of radices 2..)
   int threads;
   int Tf;                  // threads per tile column (threads = NB * Tf)
   int ept;                 // elements per thread per column (ceil(R / Tf))
@@ -141,6 +145,9 @@ struct CopyParams {
   double pre;          // mode 4: pair factor (1/2 irfft, 1 brfft)
 };
 
+// Block fixed-point compute type of the ComplexF64 passes (fx64.cuh).
+struct Fx;
+
 // A pass kernel specialised at compile time for one radix sequence.
 struct RecipeEntry {
   int f64, dir, load_op;
@@ -184,6 +191,7 @@ struct SchedOpts {
   int threads_max = 0;
   int precision = 0;
   int plain_loads = 0;
+  int f64_arith = 0;
   bool dry = false;
 };
 extern thread_local SchedOpts g_sched;

@@ -75,7 +75,7 @@ template <typename T, int DIR>
 __device__ __noinline__ void group_pass(const PassParams& pp, const void* src, void* dst, uint32_t t0, uint32_t t1,
                                         int tid) {
   for (uint32_t t = t0; t < t1; ++t) {
-    pass_tile<T, DIR, LOAD_RUNTIME, RuntimeRecipe, true>(pp, src, reinterpret_cast<Cx<T>*>(dst), t, tid,
+    pass_tile<T, DIR, LOAD_RUNTIME, RuntimeRecipe, true>(pp, src, reinterpret_cast<Cx<Hs<T>>*>(dst), t, tid,
                                                           pp.threads);
     __syncthreads();  // the next tile reuses the shared buffer
   }
@@ -141,9 +141,9 @@ __global__ void __launch_bounds__(kGroupThreads, 2)
     __syncthreads();
     if (!s_skip) {
       if (sop.kind == OP_PASS) {
-        if (sop.f64) {
-          if (sop.dir < 0) group_pass<double, -1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
-          else group_pass<double, 1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
+        if (sop.f64) {  // block fixed point (group creation rejects FP64-butterfly passes)
+          if (sop.dir < 0) group_pass<Fx, -1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
+          else group_pass<Fx, 1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
         } else {
           if (sop.dir < 0) group_pass<float, -1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
           else group_pass<float, 1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
@@ -256,8 +256,12 @@ int build_persistent(fftj_group_s* g) {
           return gfail(FFTJ_ERR_UNSUPPORTED,
                        "persistent group: a pass uses " + std::to_string(op.pp.threads) +
                            " threads per CTA; plan it with opts.threads_max = 256");
+        if (go.f64 && !op.pp.fx)
+          return gfail(FFTJ_ERR_UNSUPPORTED,
+                       "persistent group: ComplexF64 plans with FP64 butterflies (opts.f64_arith = 1) run "
+                       "outside persistent groups");
         const size_t esz = go.f64 ? 16 : 8;
-        g->smem = std::max(g->smem, (size_t)op.pp.smem_elems * esz);
+        g->smem = std::max(g->smem, (size_t)op.pp.smem_elems * esz + (size_t)op.pp.fx_cols * sizeof(int));
       }
       g->h_ops.push_back(go);
     }

@@ -19,7 +19,7 @@ namespace fftj {
 
 template <typename T, int DIR, int LOADOP>
 __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256, 2)
-    k_pass(const __grid_constant__ PassParams pp, const void* __restrict__ in, Cx<T>* __restrict__ out) {
+    k_pass(const __grid_constant__ PassParams pp, const void* __restrict__ in, Cx<Hs<T>>* __restrict__ out) {
   pass_body<T, DIR, LOADOP, RuntimeRecipe>(pp, in, out);
 }
 
@@ -47,7 +47,7 @@ __global__ void k_copy(const CopyParams cp, const void* __restrict__ in, void* _
 
 // ---------------------------------------------------------------------------
 template <typename T>
-using PassFn = void (*)(const PassParams, const void*, Cx<T>*);
+using PassFn = void (*)(const PassParams, const void*, Cx<Hs<T>>*);
 
 template <typename T>
 static PassFn<T> pass_fn(int dir, int load_op) {
@@ -69,6 +69,21 @@ static PassFn<T> pass_fn(int dir, int load_op) {
   }
 }
 
+// The generic kernel of a pass: ComplexF64 passes compute in block fixed
+// point unless the plan asked for FP64 butterflies.
+template <typename T>
+static const void* generic_pass(const PassParams& pp, int dir) {
+  if constexpr (sizeof(T) == 8) {
+    if (pp.fx) return (const void*)pass_fn<Fx>(dir, pp.load_op);
+  }
+  return (const void*)pass_fn<T>(dir, pp.load_op);
+}
+// dynamic shared memory of a pass: the tile, staged twiddles and (block
+// fixed point) the column exponents
+static size_t pass_smem(const PassParams& pp, size_t esz) {
+  return (size_t)(pp.smem_elems + pp.smem_tw_elems) * esz + (size_t)pp.fx_cols * sizeof(int);
+}
+
 // Opt a pass kernel into the device's largest dynamic shared memory. The
 // attribute belongs to the kernel function (shared by every plan), so it is
 // never set below the maximum any plan may need.
@@ -79,14 +94,14 @@ cudaError_t prepare_pass(const PassParams& pp, int dir, const void* fn) {
   if (e != cudaSuccess) return e;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const void* f = fn ? fn : (const void*)pass_fn<T>(dir, pp.load_op);
+  const void* f = fn ? fn : generic_pass<T>(pp, dir);
   // the dynamic limit is what the device allows per block minus the
   // kernel's own static shared memory
   cudaFuncAttributes fa;
   e = cudaFuncGetAttributes(&fa, f);
   if (e != cudaSuccess) return e;
   const int maxdyn = optin - (int)fa.sharedSizeBytes;
-  const size_t need = (size_t)(pp.smem_elems + pp.smem_tw_elems) * sizeof(Cx<T>);
+  const size_t need = pass_smem(pp, sizeof(Cx<T>));
   if (maxdyn <= 0 || need > (size_t)maxdyn) return cudaErrorInvalidValue;
   return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn);
 }
@@ -94,9 +109,9 @@ cudaError_t prepare_pass(const PassParams& pp, int dir, const void* fn) {
 template <typename T>
 cudaError_t launch_pass(const PassParams& pp, int dir, const void* fn, const void* in, void* out,
                         cudaStream_t st) {
-  const size_t smem = (size_t)(pp.smem_elems + pp.smem_tw_elems) * sizeof(Cx<T>);
+  const size_t smem = pass_smem(pp, sizeof(Cx<T>));
   const uint32_t grid = pp.tiles_q * pp.tiles_p * pp.tiles_b;
-  const void* f = fn ? fn : (const void*)pass_fn<T>(dir, pp.load_op);
+  const void* f = fn ? fn : generic_pass<T>(pp, dir);
   void* args[3] = {const_cast<PassParams*>(&pp), const_cast<void**>(&in), &out};
   return cudaLaunchKernel(f, dim3(grid), dim3(pp.threads), args, smem, st);
 }

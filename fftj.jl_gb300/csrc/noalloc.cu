@@ -16,6 +16,7 @@
 
 #include "../../include/fftj.h"
 #include "fftj_internal.h"
+#include "fx64.cuh"
 
 namespace fftj {
 
@@ -40,14 +41,23 @@ template <>
 struct Cplx<double> { using t = double2; };
 
 // dst[i] = exp(dir * 2 pi i (i*stride mod n) / n), generated in FP64 with an
-// exact integer reduction of the exponent.
+// exact integer reduction of the exponent; as Q61 integers (the twiddles of
+// block fixed-point ComplexF64 passes) when q61 is set.
 template <typename T>
-__global__ void k_fill_omega(typename Cplx<T>::t* dst, int64_t count, int64_t stride, int64_t n, int dir) {
+__global__ void k_fill_omega(typename Cplx<T>::t* dst, int64_t count, int64_t stride, int64_t n, int dir,
+                             int q61) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const int64_t r = (i * stride) % n;
   double s, c;
   sincospi(2.0 * (double)r / (double)n, &s, &c);
+  if (sizeof(T) == 8 && q61) {
+    longlong2 q;
+    q.x = fx_q61(c);
+    q.y = fx_q61(dir * s);
+    reinterpret_cast<longlong2*>(dst)[i] = q;
+    return;
+  }
   typename Cplx<T>::t w;
   w.x = (T)c;
   w.y = (T)(dir * s);
@@ -95,12 +105,12 @@ static int run_noalloc(int64_t n, int64_t batch, int dir, double scale, const vo
   unsigned char* tab = static_cast<unsigned char*>(base);
   unsigned char* data = tab + kNoAllocTableBytes;
   size_t cursor = 0;
-  auto table = [&](int64_t count, int64_t stride, int64_t modn) -> C* {
+  auto table = [&](int64_t count, int64_t stride, int64_t modn, int q61) -> C* {
     C* p = reinterpret_cast<C*>(tab + cursor);
     cursor += ((size_t)count * sizeof(C) + 255) / 256 * 256;
     if (cursor > kNoAllocTableBytes) return nullptr;
     const int th = 256;
-    k_fill_omega<T><<<(unsigned)((count + th - 1) / th), th, 0, st>>>(p, count, stride, modn, dir);
+    k_fill_omega<T><<<(unsigned)((count + th - 1) / th), th, 0, st>>>(p, count, stride, modn, dir, q61);
     if (cudaGetLastError() != cudaSuccess) return nullptr;  // this launch's own error
     return p;
   };
@@ -114,7 +124,7 @@ static int run_noalloc(int64_t n, int64_t batch, int dir, double scale, const vo
     const int64_t m = ncur / R;
     int rc = pass_geometry(p, f64, R, m, s1, ncur, batch, n, n);
     if (rc) return rc;
-    p.twR = table(R, 1, R);
+    p.twR = table(R, 1, R, p.fx);
     if (m > 1) {
       // two-level outer twiddles: O(sqrt(n)) entries fit the table region
       int sh = 0;
@@ -122,8 +132,8 @@ static int run_noalloc(int64_t n, int64_t batch, int dir, double scale, const vo
       const int64_t K = (int64_t)1 << sh;
       p.tw_mode = 2;
       p.tw_shift = sh;
-      p.tw_hi = table((ncur + K - 1) / K, K, ncur);
-      p.tw_lo = table(K, 1, ncur);
+      p.tw_hi = table((ncur + K - 1) / K, K, ncur, p.fx);
+      p.tw_lo = table(K, 1, ncur, p.fx);
       if (!p.tw_hi || !p.tw_lo) {
         set_error("fftj_execute_noalloc_c2c: twiddle tables exceed the table region, or their generation "
                   "failed to launch");

@@ -5,8 +5,11 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "bfly_consts.h"
 #include "fftj_internal.h"
+#include "fx64.cuh"
 
 namespace fftj {
 
@@ -16,10 +19,144 @@ template <>
 struct CT<float> { using t = float2; };
 template <>
 struct CT<double> { using t = double2; };
+template <>
+struct CT<Fx> { using t = Fx2; };
 
 template <typename T>
 using Cx = typename CT<T>::t;
 
+// Element type of the data in HBM for a pass that computes in T: the
+// ComplexF64 passes compute in block fixed point (Fx, fx64.cuh) on FP64 data.
+template <typename T>
+struct HbmT { using t = T; };
+template <>
+struct HbmT<Fx> { using t = double; };
+template <typename T>
+using Hs = typename HbmT<T>::t;
+template <typename T>
+constexpr bool kFx = std::is_same<T, Fx>::value;
+
+// read-only load of a table entry (twiddles: Q61 int64 pairs for Fx)
+template <typename T>
+__device__ __forceinline__ Cx<T> ldt(const Cx<T>* p) {
+  if constexpr (kFx<T>) {
+    const longlong2 v = __ldg(reinterpret_cast<const longlong2*>(p));
+    Fx2 r;
+    r.x = Fx::raw(v.x);
+    r.y = Fx::raw(v.y);
+    return r;
+  } else {
+    return __ldg(p);
+  }
+}
+
+// ---- per-column conversion of Fx passes (no-ops for float and double).
+// hexpo: the exponent field maximum of an element; to_c: HBM element ->
+// compute element given cin = 53 - B + E of its column.
+template <typename T>
+__device__ __forceinline__ int hexpo(const Cx<Hs<T>>& h) {
+  if constexpr (kFx<T>) {
+    const int a = fx_expo(h.x), b = fx_expo(h.y);
+    return a > b ? a : b;
+  } else {
+    return 0;
+  }
+}
+template <typename T>
+__device__ __forceinline__ Cx<T> to_c(const Cx<Hs<T>>& h, int cin) {
+  if constexpr (kFx<T>) {
+    Fx2 r;
+    r.x = fx_in(h.x, cin);
+    r.y = fx_in(h.y, cin);
+    return r;
+  } else {
+    (void)cin;
+    return h;
+  }
+}
+// outputs of a sub-stage scaled down by 2^s for the next one (Fx only)
+template <typename T>
+__device__ __forceinline__ Cx<T> shr_c(Cx<T> v, int s) {
+  if constexpr (kFx<T>) {
+    v.x = fx_shr(v.x, s);
+    v.y = fx_shr(v.y, s);
+  }
+  return v;
+}
+// growth bound in bits of the sub-stage after the first of Rs (0: none)
+template <int r, int... rest>
+__host__ __device__ constexpr int next_shift() {
+  if constexpr (sizeof...(rest) > 0) {
+    constexpr int a[] = {rest...};
+    return fx_l(a[0]);
+  } else {
+    return 0;
+  }
+}
+
+// largest exponent field of each tile column, combined across the lanes of
+// a warp that share a column (one shared-memory atomic per column and warp)
+__device__ __forceinline__ void col_expo_max(int* colE, int c, int e) {
+  const unsigned act = __activemask();
+  const unsigned grp = __match_any_sync(act, c);
+  const int m = (int)__reduce_max_sync(grp, (unsigned)e);
+  if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(colE + c, m);
+}
+// The store conversion and scaling of a pass: float/double multiply by the
+// plan's scale when it is not 1; Fx converts back from the column's units,
+// folding a power-of-two scale into the exponent shift.
+template <typename T>
+struct OutConv {
+  bool scaled;
+  T sc;
+  __device__ __forceinline__ explicit OutConv(const PassParams& pp) {
+    scaled = __double_as_longlong(pp.scale) != 0x3FF0000000000000ll;
+    sc = (T)pp.scale;
+  }
+  __device__ __forceinline__ Cx<T> operator()(Cx<T> x, int /*E*/) const {
+    if (scaled) { x.x *= sc; x.y *= sc; }
+    return x;
+  }
+};
+template <>
+struct OutConv<Fx> {
+  int B, se;   // headroom bits of the inputs; power-of-two part of the scale minus the stage shifts
+  bool mul;    // the scale is not a positive power of two: multiply by its significand
+  Fx sm;       // the significand as Q61, |sm| in [1/2, 1) (0 for a zero scale)
+  __device__ __forceinline__ explicit OutConv(const PassParams& pp) {
+    const long long b = __double_as_longlong(pp.scale);
+    const long long frac = b & 0x000fffffffffffffll;
+    const int field = (int)((b >> 52) & 0x7ff);
+    B = pp.fx_b0;
+    if (field == 0) {  // zero (or subnormal) scale: every output is 0
+      mul = true;
+      sm = Fx::raw(0);
+      se = 0;
+    } else if (frac == 0 && b > 0) {  // 2^(field - 1023): folded into the exponent
+      mul = false;
+      sm = Fx::raw(0);
+      se = field - 1023;
+    } else {  // +-(1 + frac/2^52)/2 * 2^(field - 1022)
+      mul = true;
+      const long long q = ((1ll << 52) | frac) << 8;
+      sm = Fx::raw(b < 0 ? -q : q);
+      se = field - 1022;
+    }
+    se += pp.fx_sht;  // values were divided by 2^fx_sht between sub-stages
+  }
+  __device__ __forceinline__ double2 operator()(Fx2 x, int E) const {
+    int K = fx_k(B, E);
+    if (K != kFxNaN) K -= se;  // se includes the sub-stage shifts
+    if (mul) {
+      x.x = sm * x.x;
+      x.y = sm * x.y;
+    }
+    double2 r;
+    r.x = fx_out(x.x, K);
+    r.y = fx_out(x.y, K);
+    return r;
+  }
+};
 template <typename T>
 __device__ __forceinline__ Cx<T> mk(T x, T y) { Cx<T> c; c.x = x; c.y = y; return c; }
 template <typename C>
@@ -209,7 +346,7 @@ struct Dft<T, DIR, 13> { __device__ __forceinline__ static void run(Cx<T>* v) { 
 template <typename T, int DIR, int r>
 __device__ __noinline__ void substage(Cx<T>* __restrict__ buf, const int b, const int kg, const int Tf,
                                          const int NB, const int Rr, const int S, const FastDiv fS,
-                                         const Cx<T>* __restrict__ twR) {
+                                         const Cx<T>* __restrict__ twR, const int sh = 0) {
   constexpr int IPT = (16 / r) > 0 ? (16 / r) : 1;
   const int jstride_in = Rr * NB;
   const int jstride_out = S * NB;
@@ -232,16 +369,16 @@ __device__ __noinline__ void substage(Cx<T>* __restrict__ buf, const int b, cons
       const int q = k - p * S;
       Dft<T, DIR, r>::run(v[i]);
       const int a = (r * S * p + q) * NB + b;
-      buf[pidx<T>(a)] = v[i][0];
+      buf[pidx<T>(a)] = shr_c<T>(v[i][0], sh);
       if (p == 0) {
 #pragma unroll
-        for (int j = 1; j < r; ++j) buf[pidx<T>(a + j * jstride_out)] = v[i][j];
+        for (int j = 1; j < r; ++j) buf[pidx<T>(a + j * jstride_out)] = shr_c<T>(v[i][j], sh);
       } else {
         const int tstep = p * S;
 #pragma unroll
         for (int j = 1; j < r; ++j) {
-          const Cx<T> w = __ldg(&twR[j * tstep]);
-          buf[pidx<T>(a + j * jstride_out)] = cmul(v[i][j], w);
+          const Cx<T> w = ldt<T>(&twR[j * tstep]);
+          buf[pidx<T>(a + j * jstride_out)] = shr_c<T>(cmul(v[i][j], w), sh);
         }
       }
     }
@@ -339,10 +476,17 @@ __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in,
 
 template <typename T>
 __device__ __forceinline__ Cx<T> outer_tw(const PassParams& pp, int64_t e) {
-  if (pp.tw_mode == 1) return __ldg(reinterpret_cast<const Cx<T>*>(pp.tw_full) + e);
-  const Cx<T> hi = __ldg(reinterpret_cast<const Cx<T>*>(pp.tw_hi) + (e >> pp.tw_shift));
-  const Cx<T> lo = __ldg(reinterpret_cast<const Cx<T>*>(pp.tw_lo) + (e & ((1ll << pp.tw_shift) - 1)));
-  return cmul(hi, lo);
+  if (pp.tw_mode == 1) return ldt<T>(reinterpret_cast<const Cx<T>*>(pp.tw_full) + e);
+  const Cx<T> hi = ldt<T>(reinterpret_cast<const Cx<T>*>(pp.tw_hi) + (e >> pp.tw_shift));
+  const Cx<T> lo = ldt<T>(reinterpret_cast<const Cx<T>*>(pp.tw_lo) + (e & ((1ll << pp.tw_shift) - 1)));
+  Cx<T> w = cmul(hi, lo);
+  if constexpr (kFx<T>) {
+    // the rounded product of two Q61 twiddles can land a few units beyond
+    // +-(2^61 - 1) (at angles near multiples of pi/2): clamp to the Q61 range
+    w.x = fx_clamp_q61(w.x);
+    w.y = fx_clamp_q61(w.y);
+  }
+  return w;
 }
 
 // ---------------------------------------------------------------------------
@@ -408,7 +552,7 @@ struct Lay {
 template <typename T, int NBC>
 using LayC = Lay<T, NBC == 0 ? 1 : NBC>;
 
-template <typename T, int DIR, int r, int S, int Rr, int TF, int NBC = 0>
+template <typename T, int DIR, int r, int S, int Rr, int TF, int NBC = 0, int SH = 0>
 __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b, const int kg, const int NB,
                                             const Cx<T>* __restrict__ twR) {
   constexpr int IPT = (Rr + TF - 1) / TF;
@@ -455,18 +599,18 @@ __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b
 #define FFTJ_OUT_AT(j)                                                               \
   (kLay ? base + LayC<T, NBC>::step((j) * S)                           \
         : (S % PP == 0) ? base + (j) * step : pidx<T>(a + (j) * jstride_out))
-      buf[base] = v[i][0];
+      buf[base] = shr_c<T>(v[i][0], SH);
       if (Rr == S) {
         // last sub-stage of the pass (L = r): no twiddle
 #pragma unroll
-        for (int j = 1; j < r; ++j) buf[FFTJ_OUT_AT(j)] = v[i][j];
+        for (int j = 1; j < r; ++j) buf[FFTJ_OUT_AT(j)] = shr_c<T>(v[i][j], SH);
       } else {
         const int tstep = p * S;
 #pragma unroll
         for (int j = 1; j < r; ++j) {
           Cx<T> w = v[i][j];
           if (p != 0) w = cmul(w, twR[j * tstep]);
-          buf[FFTJ_OUT_AT(j)] = w;
+          buf[FFTJ_OUT_AT(j)] = shr_c<T>(w, SH);
         }
       }
 #undef FFTJ_OUT_AT
@@ -478,7 +622,7 @@ __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b
 template <typename T, int DIR, int TF, int R, int S, int NBC, int r, int... rest>
 __device__ __forceinline__ void run_subs_ct(Cx<T>* buf, const int b, const int kg, const int NB,
                                             const Cx<T>* twR) {
-  substage_ct<T, DIR, r, S, R / r, TF, NBC>(buf, b, kg, NB, twR);
+  substage_ct<T, DIR, r, S, R / r, TF, NBC, next_shift<r, rest...>()>(buf, b, kg, NB, twR);
   if constexpr (sizeof...(rest) > 0) run_subs_ct<T, DIR, TF, R, S * r, NBC, rest...>(buf, b, kg, NB, twR);
 }
 template <typename T, int DIR, int... Rs>
@@ -679,10 +823,12 @@ __device__ __noinline__ void substage_tc16(float2* __restrict__ buf, const int t
 // L2-coherent.
 template <typename T, int DIR, int LOADOP, class Rec, bool GROUP>
 __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __restrict__ in,
-                                          Cx<T>* __restrict__ out, const uint32_t tile, const int tid,
+                                          Cx<Hs<T>>* __restrict__ out, const uint32_t tile, const int tid,
                                           const int nthr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* buf = reinterpret_cast<Cx<T>*>(smem_raw);
+  // Fx passes: exponent maximum of each tile column, after the tile
+  int* const colE = reinterpret_cast<int*>(buf + pp.smem_elems);
   constexpr int EPT = Rec::kConst ? (Rec::R + Rec::Tf - 1) / Rec::Tf : 16;
   const bool active = !GROUP || tid < nthr;
   const uint32_t t1 = pp.ftq.div(tile);
@@ -709,8 +855,15 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
 
   // ---- load: HBM -> shared. All of a thread's loads are issued before its
   // first shared store; indices are recomputed rather than kept in registers.
+  // Fx: the column's exponent maximum is taken between loads and stores.
+  using H = Hs<T>;
+  if constexpr (kFx<T>) {
+    if (tid < NB) colE[tid] = 1;
+    __syncthreads();
+  }
+  const int B = pp.fx_b0;
   {
-    Cx<T> v[EPT];
+    Cx<H> v[EPT];
     if (pp.load_rows) {
       // transforms contiguous along j (one pass over whole transforms)
 #pragma unroll
@@ -719,15 +872,24 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
         if (e < E) {
           const int c = Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e);
           const int64_t bb = b0 + c;
-          v[i] = bb < pp.nbatch ? load_elem<T, LOADOP, GROUP>(pp, in, bb, e - c * R) : mk<T>(0, 0);
+          v[i] = bb < pp.nbatch ? load_elem<H, LOADOP, GROUP>(pp, in, bb, e - c * R) : mk<H>(0, 0);
         }
+      }
+      if constexpr (kFx<T>) {
+#pragma unroll
+        for (int i = 0; i < EPT; ++i) {
+          const int e = tid + i * nthr;
+          if (e < E) col_expo_max(colE, Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e), hexpo<T>(v[i]));
+        }
+        __syncthreads();
       }
 #pragma unroll
       for (int i = 0; i < EPT; ++i) {
         const int e = tid + i * nthr;
         if (e < E) {
           const int c = Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e);
-          buf[pidx<T>((e - c * R) * NB + c)] = v[i];
+          const int cin = kFx<T> ? 53 - B + colE[c] : 0;
+          buf[pidx<T>((e - c * R) * NB + c)] = to_c<T>(v[i], cin);
         }
       }
     } else {
@@ -737,12 +899,24 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
 #pragma unroll
       for (int i = 0; i < EPT; ++i) {
         const int j = kg + i * Tf;
-        if (j < R) v[i] = ok ? load_elem<T, LOADOP, GROUP>(pp, in, batch, gcol + (int64_t)j * ms) : mk<T>(0, 0);
+        if (j < R) v[i] = ok ? load_elem<H, LOADOP, GROUP>(pp, in, batch, gcol + (int64_t)j * ms) : mk<H>(0, 0);
+      }
+      int cin = 0;
+      if constexpr (kFx<T>) {
+        int em = 1;
+#pragma unroll
+        for (int i = 0; i < EPT; ++i) {
+          const int j = kg + i * Tf;
+          if (j < R) em = max(em, hexpo<T>(v[i]));
+        }
+        if (active) atomicMax(colE + b, em);
+        __syncthreads();
+        cin = 53 - B + colE[b];
       }
 #pragma unroll
       for (int i = 0; i < EPT; ++i) {
         const int j = kg + i * Tf;
-        if (j < R) buf[pidx<T>(j * NB + b)] = v[i];
+        if (j < R) buf[pidx<T>(j * NB + b)] = to_c<T>(v[i], cin);
       }
     }
   }
@@ -756,15 +930,16 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
 #pragma unroll 1
     for (int si = 0; si < pp.nsub; ++si) {
       const SubStage& ss = pp.sub[si];
+      const int sh = kFx<T> && si + 1 < pp.nsub ? fx_l(pp.sub[si + 1].r) : 0;
       switch (ss.r) {
-        case 2: substage<T, DIR, 2>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
-        case 3: substage<T, DIR, 3>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
-        case 4: substage<T, DIR, 4>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
-        case 5: substage<T, DIR, 5>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
-        case 7: substage<T, DIR, 7>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
-        case 8: substage<T, DIR, 8>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
-        case 11: substage<T, DIR, 11>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
-        case 13: substage<T, DIR, 13>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR); break;
+        case 2: substage<T, DIR, 2>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
+        case 3: substage<T, DIR, 3>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
+        case 4: substage<T, DIR, 4>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
+        case 5: substage<T, DIR, 5>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
+        case 7: substage<T, DIR, 7>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
+        case 8: substage<T, DIR, 8>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
+        case 11: substage<T, DIR, 11>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
+        case 13: substage<T, DIR, 13>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
         case 16:
           if constexpr (sizeof(T) == 4) {
             if (pp.tc && tc16_fits(nthr, NB, ss.Rr)) {
@@ -775,7 +950,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
               break;
             }
           }
-          substage<T, DIR, 16>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR);
+          substage<T, DIR, 16>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh);
           break;
         default: break;
       }
@@ -784,8 +959,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
 
   // ---- store: shared -> HBM with the outer twiddle w_ncur^(p*j) and scale.
   // The twiddle loads of all of a thread's elements are issued first.
-  const bool scaled = not_one(pp.scale);
-  const T sc = (T)pp.scale;
+  const OutConv<T> oc(pp);
   const bool tw = pp.tw_mode != 0;
   Cx<T> w[EPT];
   if (pp.store_rows) {
@@ -813,8 +987,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
         if (bb < pp.nbatch) {
           Cx<T> v = buf[pidx<T>(j * NB + c)];
           if (tw) v = cmul(v, w[i]);
-          if (scaled) { v.x *= sc; v.y *= sc; }
-          out[bb * pp.out_bstride + (int64_t)R * (p0 + (c - cbt2 * P)) + j] = v;
+          out[bb * pp.out_bstride + (int64_t)R * (p0 + (c - cbt2 * P)) + j] = oc(v, kFx<T> ? colE[c] : 0);
         }
       }
     }
@@ -827,15 +1000,15 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
       if (j < R && tw && pcol * j != 0) w[i] = outer_tw<T>(pp, pcol * (int64_t)j);
     }
     if (ok) {
-      Cx<T>* ob = out + batch * pp.out_bstride + (int64_t)R * pp.s * pcol + q0 + ql;
+      Cx<H>* ob = out + batch * pp.out_bstride + (int64_t)R * pp.s * pcol + q0 + ql;
+      const int Eb = kFx<T> ? colE[b] : 0;
 #pragma unroll
       for (int i = 0; i < EPT; ++i) {
         const int j = kg + i * Tf;
         if (j < R) {
           Cx<T> v = buf[pidx<T>(j * NB + b)];
           if (tw) v = cmul(v, w[i]);
-          if (scaled) { v.x *= sc; v.y *= sc; }
-          ob[(int64_t)j * pp.s] = v;
+          ob[(int64_t)j * pp.s] = oc(v, Eb);
         }
       }
     }
@@ -844,7 +1017,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
 
 template <typename T, int DIR, int LOADOP, class Rec>
 __device__ __forceinline__ void pass_body(const PassParams& pp, const void* __restrict__ in,
-                                          Cx<T>* __restrict__ out) {
+                                          Cx<Hs<T>>* __restrict__ out) {
   pass_tile<T, DIR, LOADOP, Rec, false>(pp, in, out, blockIdx.x, threadIdx.x, blockDim.x);
 }
 
@@ -907,7 +1080,7 @@ __device__ __forceinline__ void run_mid_skip(Cx<T>* buf, const int b, const int 
     if constexpr (sizeof...(rest) == 0) {
       substage_ct<T, DIR, r, S, R / r, TF, NBC>(buf, b, kg, NB, twR);
     } else {
-      substage_ct<T, DIR, r, S, R / r, TF, NBC>(buf, b, kg, NB, twR);
+      substage_ct<T, DIR, r, S, R / r, TF, NBC, next_shift<r, rest...>()>(buf, b, kg, NB, twR);
       run_mid_skip<T, DIR, TF, R, S * r, DROP, NBC, rest...>(buf, b, kg, NB, twR);
     }
   }
@@ -923,18 +1096,18 @@ __device__ __forceinline__ void run_mid_ct(Cx<T>* buf, const int b, const int kg
 // (s == 1), MODE 2 the strided store of a later pass. Shared by the one-tile-per-CTA recipe
 // kernels and the pipelined tensor-copy kernel (pass_tma.cuh).
 template <typename T, int DIR, int MODE, int NBC, int... Rs>
-__device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restrict__ out,
+__device__ __forceinline__ void store_last(const PassParams& pp, Cx<Hs<T>>* __restrict__ out,
                                            const Cx<T>* __restrict__ buf, const int tid, const int nthr,
                                            const int kg, const int b, const int64_t b0, const int64_t p0,
                                            const int64_t q0, const int ql, const int64_t batch,
-                                           const int64_t pcol, const bool colok) {
+                                           const int64_t pcol, const bool colok, const int* colE = nullptr) {
   using Rec = Recipe<Rs...>;
   constexpr int R = Rec::R, TF = Rec::Tf, NS = Rec::n;
   constexpr int rad[] = {Rs...};
   constexpr int rL = rad[NS - 1];
   const int NB = NBC > 0 ? NBC : pp.NB;
-  const bool scaled = not_one(pp.scale);
-  const T sc = (T)pp.scale;
+  const OutConv<T> oc(pp);
+  using H = Hs<T>;
   const bool tw = pp.tw_mode != 0;
   if constexpr (MODE == 0) {
     // ---- fused last sub-stage (radix rL) + row store: butterfly u = c S + k
@@ -958,13 +1131,10 @@ __device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restri
         for (int j = 0; j < rL; ++j) v[j] = buf[pidx<T>((k + j * S) * NB + c)];
       }
       Dft<T, DIR, rL>::run(v);
-      Cx<T>* o = out + (b0 + c) * pp.out_bstride + k;
+      Cx<H>* o = out + (b0 + c) * pp.out_bstride + k;
+      const int Ec = kFx<T> ? colE[c] : 0;
 #pragma unroll
-      for (int j = 0; j < rL; ++j) {
-        Cx<T> x = v[j];
-        if (scaled) { x.x *= sc; x.y *= sc; }
-        o[j * S] = x;
-      }
+      for (int j = 0; j < rL; ++j) o[j * S] = oc(v[j], Ec);
     }
   } else if constexpr (MODE == 1) {
     // ---- fused last sub-stage (radix rL) + row store (s == 1). Butterfly
@@ -979,7 +1149,7 @@ __device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restri
     constexpr bool kRecur = sizeof(T) == 4;
     const int nbf = NB * S;
     if (b0 < pp.nbatch) {
-      Cx<T>* orow = out + b0 * pp.out_bstride + (int64_t)R * p0;
+      Cx<H>* orow = out + b0 * pp.out_bstride + (int64_t)R * p0;
       for (int u = tid; u < nbf; u += nthr) {
         const int c = u / S;
         const int k = u - c * S;
@@ -1001,7 +1171,8 @@ __device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restri
           if (e != 0) w = outer_tw<T>(pp, e);
           if (estep != 0) wstep = outer_tw<T>(pp, estep);
         }
-        Cx<T>* o = orow + (int64_t)R * c + k;
+        Cx<H>* o = orow + (int64_t)R * c + k;
+        const int Ec = kFx<T> ? colE[c] : 0;
 #pragma unroll
         for (int j = 0; j < rL; ++j) {
           Cx<T> x = v[j];
@@ -1013,8 +1184,7 @@ __device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restri
           } else if (tw && e != 0) {
             x = cmul(x, outer_tw<T>(pp, e));
           }
-          if (scaled) { x.x *= sc; x.y *= sc; }
-          o[j * S] = x;
+          o[j * S] = oc(x, Ec);
           e += estep;
         }
       }
@@ -1040,7 +1210,8 @@ __device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restri
       }
     }
     if (colok) {
-      Cx<T>* ob = out + batch * pp.out_bstride + (int64_t)R * pp.s * pcol + q0 + ql;
+      Cx<H>* ob = out + batch * pp.out_bstride + (int64_t)R * pp.s * pcol + q0 + ql;
+      const int Eb = kFx<T> ? colE[b] : 0;
       const int64_t jstep = (int64_t)S * pp.s;
       const uint32_t estep = (uint32_t)pcol * (uint32_t)S;
       // F32: along a butterfly's outputs the outer twiddle w^(pcol (k + j S))
@@ -1054,7 +1225,7 @@ __device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restri
         const int k = kg + i * TF;
         if ((i + 1) * TF <= S || k < S) {
           Dft<T, DIR, rL>::run(v[i]);
-          Cx<T>* o = ob + (int64_t)k * pp.s;
+          Cx<H>* o = ob + (int64_t)k * pp.s;
           uint32_t e = (uint32_t)pcol * (uint32_t)k;
           Cx<T> w = (kRecur && tw && e != 0) ? outer_tw<T>(pp, e) : mk<T>(1, 0);
 #pragma unroll
@@ -1068,8 +1239,7 @@ __device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restri
             } else if (tw && e != 0) {
               x = cmul(x, outer_tw<T>(pp, e));
             }
-            if (scaled) { x.x *= sc; x.y *= sc; }
-            *o = x;
+            *o = oc(x, Eb);
             o += jstep;
             e += estep;
           }
@@ -1089,7 +1259,8 @@ __device__ __forceinline__ void store_last(const PassParams& pp, Cx<T>* __restri
 // row) counters advance by additions.
 template <typename T, int DIR, int LOADOP, int MODE, int NBC, int... Rs>
 __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __restrict__ in,
-                                           Cx<T>* __restrict__ out) {
+                                           Cx<Hs<T>>* __restrict__ out) {
+  using H = Hs<T>;
   using Rec = Recipe<Rs...>;
   constexpr int R = Rec::R, TF = Rec::Tf, NS = Rec::n;
   constexpr int rad[] = {Rs...};
@@ -1136,8 +1307,16 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
   if (pp.smem_tw_elems >= R) {
     Cx<T>* twS = buf + pp.smem_elems;
     const Cx<T>* twG = twR + tid;
-    for (int t = tid; t < R; t += nthr, twG += nthr) twS[t] = __ldg(twG);
+    for (int t = tid; t < R; t += nthr, twG += nthr) twS[t] = ldt<T>(twG);
     twR = twS;
+  }
+  // Fx: exponent maximum of each tile column (after the tile and the staged
+  // twiddles); made visible by the first barrier below
+  int* const colE = reinterpret_cast<int*>(buf + pp.smem_elems + pp.smem_tw_elems);
+  const int B = pp.fx_b0;
+  constexpr int SH1 = next_shift<Rs...>();  // shift after the first sub-stage
+  if constexpr (kFx<T>) {
+    if (tid < NB) colE[tid] = 1;
   }
 
   if constexpr (MODE == 0 && NS >= 2) {
@@ -1149,26 +1328,43 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
     const int nbf = NB * Rr;
     const int64_t bstr = LOADOP == LOAD_PLAIN ? pp.in_bstride : pp.ld_stride;
     __syncthreads();  // staged twiddles visible
+    if constexpr (kFx<T>) {
+      // column exponents first (the loop below loads the same elements
+      // again, from L1/L2)
+      for (int u = tid; u < nbf; u += nthr) {
+        const int c = u / Rr;
+        const int k = u - c * Rr;
+        const int64_t bb = b0 + c;
+        int em = 1;
+        if (bb < pp.nbatch) {
+#pragma unroll
+          for (int j = 0; j < r0; ++j) em = max(em, hexpo<T>(load_elem_off<H, LOADOP>(pp, in, bb * bstr, k + j * Rr)));
+        }
+        col_expo_max(colE, c, em);
+      }
+      __syncthreads();
+    }
     for (int u = tid; u < nbf; u += nthr) {
       const int c = u / Rr;
       const int k = u - c * Rr;
       const int64_t bb = b0 + c;
+      const int cin = kFx<T> ? 53 - B + colE[c] : 0;
       Cx<T> v[r0];
       if (bb < pp.nbatch) {
 #pragma unroll
-        for (int j = 0; j < r0; ++j) v[j] = load_elem_off<T, LOADOP>(pp, in, bb * bstr, k + j * Rr);
+        for (int j = 0; j < r0; ++j) v[j] = to_c<T>(load_elem_off<H, LOADOP>(pp, in, bb * bstr, k + j * Rr), cin);
       } else {
 #pragma unroll
         for (int j = 0; j < r0; ++j) v[j] = mk<T>(0, 0);
       }
       Dft<T, DIR, r0>::run(v);
       const int a = r0 * k * NB + c;
-      buf[pidx<T>(a)] = v[0];
+      buf[pidx<T>(a)] = shr_c<T>(v[0], SH1);
 #pragma unroll
       for (int j = 1; j < r0; ++j) {
         Cx<T> w = v[j];
         if (k != 0) w = cmul(w, twR[j * k]);
-        buf[pidx<T>(a + j * NB)] = w;
+        buf[pidx<T>(a + j * NB)] = shr_c<T>(w, SH1);
       }
     }
     __syncthreads();
@@ -1178,7 +1374,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
     }
   } else if constexpr (MODE == 0) {
     // ---- row load (lanes walk j): e = tid + i*nthr -> (c, j), c = column
-    Cx<T> v[EPT];
+    Cx<H> v[EPT];
     const int dc = nthr / R, dj = nthr - (nthr / R) * R;
     {
       int c = tid / R, j = tid - (tid / R) * R;
@@ -1188,17 +1384,28 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
 #pragma unroll
       for (int i = 0; i < EPT; ++i) {
         if (tid + i * nthr < E) {
-          v[i] = b0 + c < pp.nbatch ? load_elem_off<T, LOADOP>(pp, in, boff, j) : mk<T>(0, 0);
+          v[i] = b0 + c < pp.nbatch ? load_elem_off<H, LOADOP>(pp, in, boff, j) : mk<H>(0, 0);
         }
         j += dj; c += dc; boff += dstep;
         if (j >= R) { j -= R; c++; boff += bstr; }
       }
     }
+    if constexpr (kFx<T>) {
+      __syncthreads();  // column exponent initialisation visible
+      int c = tid / R, j = tid - (tid / R) * R;
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        if (tid + i * nthr < E) col_expo_max(colE, c, hexpo<T>(v[i]));
+        j += dj; c += dc;
+        if (j >= R) { j -= R; c++; }
+      }
+      __syncthreads();
+    }
     {
       int c = tid / R, j = tid - (tid / R) * R;
 #pragma unroll
       for (int i = 0; i < EPT; ++i) {
-        if (tid + i * nthr < E) buf[pidx<T>(j * NB + c)] = v[i];
+        if (tid + i * nthr < E) buf[pidx<T>(j * NB + c)] = to_c<T>(v[i], kFx<T> ? 53 - B + colE[c] : 0);
         j += dj; c += dc;
         if (j >= R) { j -= R; c++; }
       }
@@ -1214,7 +1421,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
     const int64_t bstr = LOADOP == LOAD_PLAIN ? pp.in_bstride : pp.ld_stride;
     const int64_t boff = batch * bstr;
     const int64_t gcol = pp.s * pcol + q0 + ql;
-    Cx<T> v[IPT][r0];
+    Cx<H> h[IPT][r0];
 #pragma unroll
     for (int i = 0; i < IPT; ++i) {
       const int k = kg + i * TF;
@@ -1223,28 +1430,46 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
         const int64_t gstep = (int64_t)Rr * ms;
 #pragma unroll
         for (int j = 0; j < r0; ++j) {
-          v[i][j] = colok ? load_elem_off<T, LOADOP>(pp, in, boff, g) : mk<T>(0, 0);
+          h[i][j] = colok ? load_elem_off<H, LOADOP>(pp, in, boff, g) : mk<H>(0, 0);
           g += gstep;
         }
       }
     }
     __syncthreads();  // staged twiddles visible (the loads above stay in flight)
+    int cin = 0;
+    if constexpr (kFx<T>) {
+      int em = 1;
+#pragma unroll
+      for (int i = 0; i < IPT; ++i) {
+        const int k = kg + i * TF;
+        if ((i + 1) * TF <= Rr || k < Rr) {
+#pragma unroll
+          for (int j = 0; j < r0; ++j) em = max(em, hexpo<T>(h[i][j]));
+        }
+      }
+      atomicMax(colE + b, em);
+      __syncthreads();
+      cin = 53 - B + colE[b];
+    }
 #pragma unroll
     for (int i = 0; i < IPT; ++i) {
       const int k = kg + i * TF;
       if ((i + 1) * TF <= Rr || k < Rr) {
-        Dft<T, DIR, r0>::run(v[i]);
+        Cx<T> v[r0];
+#pragma unroll
+        for (int j = 0; j < r0; ++j) v[j] = to_c<T>(h[i][j], cin);
+        Dft<T, DIR, r0>::run(v);
         const int a = r0 * k * NB + b;
         // compile-time columns: output rows r0 k + j are constant offsets
         // from row r0 k (a multiple of the rows per padding period)
         constexpr bool kLay = NBC > 0 && LayC<T, NBC>::exact(r0);
         const int base = kLay ? LayC<T, NBC>::row(r0 * k) + LayC<T, NBC>::col(b) : pidx<T>(a);
-        buf[base] = v[i][0];
+        buf[base] = shr_c<T>(v[0], SH1);
 #pragma unroll
         for (int j = 1; j < r0; ++j) {
-          Cx<T> w = v[i][j];
+          Cx<T> w = v[j];
           if (NS > 1 && k != 0) w = cmul(w, twR[j * k]);
-          buf[kLay ? base + LayC<T, NBC>::step(j) : pidx<T>(a + j * NB)] = w;
+          buf[kLay ? base + LayC<T, NBC>::step(j) : pidx<T>(a + j * NB)] = shr_c<T>(w, SH1);
         }
       }
     }
@@ -1256,14 +1481,13 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
   }
 
   if constexpr (MODE == 1 || MODE == 2) {
-    store_last<T, DIR, MODE, NBC, Rs...>(pp, out, buf, tid, nthr, kg, b, b0, p0, q0, ql, batch, pcol, colok);
+    store_last<T, DIR, MODE, NBC, Rs...>(pp, out, buf, tid, nthr, kg, b, b0, p0, q0, ql, batch, pcol, colok, colE);
     return;
   }
-  const bool scaled = not_one(pp.scale);
-  const T sc = (T)pp.scale;
+  const OutConv<T> oc(pp);
   const bool tw = pp.tw_mode != 0;
   if constexpr (MODE == 0 && NS >= 2) {
-    store_last<T, DIR, MODE, NBC, Rs...>(pp, out, buf, tid, nthr, kg, b, b0, p0, q0, ql, batch, pcol, colok);
+    store_last<T, DIR, MODE, NBC, Rs...>(pp, out, buf, tid, nthr, kg, b, b0, p0, q0, ql, batch, pcol, colok, colE);
   } else if constexpr (MODE == 0) {
     // ---- row store (lanes walk j): outputs contiguous along j (s == 1)
     const int dc = nthr / R, dj = nthr - (nthr / R) * R;
@@ -1280,7 +1504,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
       if (j >= R) { j -= R; c++; }
     }
     c = tid / R; j = tid - (tid / R) * R;
-    Cx<T>* op = out + b0 * pp.out_bstride + (int64_t)R * p0 + tid;
+    Cx<H>* op = out + b0 * pp.out_bstride + (int64_t)R * p0 + tid;
 #pragma unroll
     for (int i = 0; i < EPT; ++i) {
       const int e = tid + i * nthr;
@@ -1288,8 +1512,7 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
       if (e < E && b0 + c < pp.nbatch) {
         Cx<T> v = buf[pidx<T>(j * NB + c)];
         if (tw) v = cmul(v, w[i]);
-        if (scaled) { v.x *= sc; v.y *= sc; }
-        *op = v;
+        *op = oc(v, kFx<T> ? colE[c] : 0);
       }
       op += nthr;
       j += dj; c += dc;
@@ -1302,7 +1525,7 @@ template <typename T, int DIR, int LOADOP, int MODE, int NBC, class Rec>
 struct FusedLaunch;
 template <typename T, int DIR, int LOADOP, int MODE, int NBC, int... Rs>
 struct FusedLaunch<T, DIR, LOADOP, MODE, NBC, Recipe<Rs...>> {
-  __device__ __forceinline__ static void run(const PassParams& pp, const void* in, Cx<T>* out) {
+  __device__ __forceinline__ static void run(const PassParams& pp, const void* in, Cx<Hs<T>>* out) {
     pass_fused<T, DIR, LOADOP, MODE, NBC, Rs...>(pp, in, out);
   }
 };

@@ -615,6 +615,16 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
       return fail(FFTJ_ERR_UNSUPPORTED, "tile exceeds 16 elements per thread");
     const int padsh = f64 ? 3 : 4;
     pp.smem_elems = (int)(E + (E >> padsh) + 2);
+    // ComplexF64: block fixed point unless the plan asks for FP64 butterflies
+    pp.fx = (f64 && !g_sched.f64_arith) ? 1 : 0;
+    pp.fx_cols = pp.fx ? pp.NB : 0;
+    pp.fx_b0 = 0;
+    pp.fx_sht = 0;
+    if (pp.fx && pp.nsub > 0) {
+      auto lg = [](int r) { int l = 0; while ((1 << l) < r) ++l; return l; };
+      pp.fx_b0 = std::min(61 - lg(pp.sub[0].r), 60);
+      for (int i = 1; i < pp.nsub; ++i) pp.fx_sht += lg(pp.sub[i].r);
+    }
   return FFTJ_OK;
 }
 
@@ -665,7 +675,10 @@ const void* pick_pass_kernel_t(int dir, const PassParams& pp) {
   return nullptr;
 }
 const void* pick_pass_kernel(bool f64, int dir, const PassParams& pp) {
-  return f64 ? pick_pass_kernel_t<double>(dir, pp) : pick_pass_kernel_t<float>(dir, pp);
+  // ComplexF64 recipe kernels compute in block fixed point; FP64-butterfly
+  // passes run the generic kernel
+  if (f64) return pp.fx ? pick_pass_kernel_t<Fx>(dir, pp) : nullptr;
+  return pick_pass_kernel_t<float>(dir, pp);
 }
 
 // Sub-stage i of a pass runs on the tensor cores in the precision form (the
@@ -745,9 +758,24 @@ const void* upload_raw(fftj_plan_s* P, const void* data, size_t bytes) {
   return b.p;
 }
 
-// the complex table w_n^e for e in [0, count), sign dir
+// round(c * 2^61) clamped to [-2^61, 2^61 - 1]: the Q61 twiddles of block
+// fixed-point passes (fx64.cuh)
+int64_t q61(double c) {
+  if (c >= 1.0) return ((int64_t)1 << 61) - 1;
+  if (c <= -1.0) return -((int64_t)1 << 61);
+  return (int64_t)std::llround(c * 2305843009213693952.0);
+}
+const void* upload_q61(fftj_plan_s* P, const std::vector<double>& ri) {
+  if (g_sched.dry) return kDryTable;
+  std::vector<int64_t> h(ri.size());
+  for (size_t i = 0; i < ri.size(); ++i) h[i] = q61(ri[i]);
+  return upload_raw(P, h.data(), h.size() * sizeof(int64_t));
+}
+
+// the complex table w_n^e for e in [0, count), sign dir (as T, or as Q61
+// integers when as_q61 is set)
 template <typename T>
-const void* omega_table(fftj_plan_s* P, i64 n, i64 count, i64 stride, int dir) {
+const void* omega_table(fftj_plan_s* P, i64 n, i64 count, i64 stride, int dir, bool as_q61 = false) {
   if (g_sched.dry) return kDryTable;
   std::vector<double> ri(2 * count);
   if (g_tables.omega && g_tables.N % n == 0) {
@@ -761,7 +789,7 @@ const void* omega_table(fftj_plan_s* P, i64 n, i64 count, i64 stride, int dir) {
   } else {
     for (i64 e = 0; e < count; ++e) omega(e * stride, n, dir, &ri[2 * e], &ri[2 * e + 1]);
   }
-  return upload_cplx<T>(P, ri);
+  return as_q61 ? upload_q61(P, ri) : upload_cplx<T>(P, ri);
 }
 
 // Build the passes of a length-n transform along an axis with inner stride
@@ -792,18 +820,19 @@ int build_axis_passes(fftj_plan_s* P, i64 n, i64 Bi, i64 nbatch, i64 ibs, i64 ob
       int grc = pass_geometry(pp, f64, R, m, s, ncur, nbatch, ibs, obs);
       if (grc) return grc;
     }
-    // inner twiddles w_R^t
-    pp.twR = omega_table<T>(P, R, R, 1, dir);
+    // inner twiddles w_R^t (Q61 integers for block fixed-point passes)
+    const bool q = pp.fx != 0;
+    pp.twR = omega_table<T>(P, R, R, 1, dir, q);
     if (!pp.twR) return fail(FFTJ_ERR_CUDA, "table upload failed");
     // outer twiddles w_ncur^(p*j), p*j < ncur
     outer_twiddle_layout(pp, f64);
     if (pp.tw_mode == 1) {
-      pp.tw_full = omega_table<T>(P, ncur, ncur, 1, dir);
+      pp.tw_full = omega_table<T>(P, ncur, ncur, 1, dir, q);
       if (!pp.tw_full) return fail(FFTJ_ERR_CUDA, "table upload failed");
     } else if (pp.tw_mode == 2) {
       const i64 K = (i64)1 << pp.tw_shift;
-      pp.tw_hi = omega_table<T>(P, ncur, (ncur + K - 1) / K, K, dir);
-      pp.tw_lo = omega_table<T>(P, ncur, K, 1, dir);
+      pp.tw_hi = omega_table<T>(P, ncur, (ncur + K - 1) / K, K, dir, q);
+      pp.tw_lo = omega_table<T>(P, ncur, K, 1, dir, q);
       if (!pp.tw_hi || !pp.tw_lo) return fail(FFTJ_ERR_CUDA, "table upload failed");
     }
     pp.scale = (pi + 1 == Rs.size()) ? scale : 1.0;
@@ -1542,6 +1571,7 @@ struct SchedScope {
     g_sched.dry = o->dry != 0;
     g_sched.precision = (o->precision >= 0 && o->precision <= 2) ? o->precision : 0;
     g_sched.plain_loads = o->plain_loads != 0 ? 1 : 0;
+    g_sched.f64_arith = o->f64_arith != 0 ? 1 : 0;
   }
   ~SchedScope() { g_sched = SchedOpts(); }
 };
@@ -1843,6 +1873,7 @@ int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info) {
     if (op.kind == OP_PASS) {
       const PassParams& pp = op.pp;
       if (op.kfn) info->specialized_passes++;
+      info->fx_passes += pp.fx ? 1 : 0;
       if (pp.tc)
         for (int i = 0; i < pp.nsub; ++i) info->tc_substages += tc16_substage_fits(pp, i) ? 1 : 0;
       if (pi < 8) {
@@ -1853,6 +1884,7 @@ int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info) {
       pi++;
       for (int64_t v : {(int64_t)pp.R, (int64_t)pp.P, (int64_t)pp.Q, (int64_t)pp.NBt, (int64_t)pp.Tf,
                         (int64_t)pp.threads, (int64_t)pp.nsub, (int64_t)pp.tw_mode, (int64_t)pp.load_op, (int64_t)pp.tc,
+                        (int64_t)pp.fx,
                         (int64_t)(uintptr_t)op.kfn, (int64_t)(uintptr_t)op.kfn_tma})
         mix(v);
       for (int i = 0; i < pp.nsub; ++i) mix(pp.sub[i].r);

@@ -1,3 +1,3 @@
-#define FFTJ_T double
+#define FFTJ_T Fx  // ComplexF64 data, block fixed-point compute (fx64.cuh)
 #define FFTJ_DIR -1
 #include "recipes.inc"

@@ -53,6 +53,7 @@ class PlanInfo(ctypes.Structure):
         ("schedule_hash", ctypes.c_uint64), ("pass_tile", ctypes.c_int * 8),
         ("pass_threads", ctypes.c_int * 8), ("pass_ctas", ctypes.c_int64 * 8), ("nops", ctypes.c_int),
         ("dry", ctypes.c_int), ("tc_substages", ctypes.c_int), ("tma_passes", ctypes.c_int),
+        ("fx_passes", ctypes.c_int),
     ]
 
 
@@ -60,7 +61,7 @@ class PlanOpts(ctypes.Structure):
     """fftj_plan_opts_t: schedule options (all zero = the planner's default)."""
     _fields_ = [(k, ctypes.c_int32) for k in
                 ("tile", "extra_passes", "order", "tf_mult", "route", "threads_max", "dry", "precision",
-                 "plain_loads")]
+                 "plain_loads", "f64_arith")]
 
 
 class TuneQuery(ctypes.Structure):

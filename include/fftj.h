@@ -74,6 +74,7 @@ typedef struct {
   int dry;                /* 1: planned without tables or workspace (cannot execute) */
   int tc_substages;       /* radix-16 sub-stages run on tensor cores (opts.precision != 0) */
   int tma_passes;         /* passes with a pipelined tensor-copy kernel (used when the input is 16-byte aligned) */
+  int fx_passes;          /* ComplexF64 passes computed in block fixed point (integer pipes) */
 } fftj_plan_info_t;
 
 /*
@@ -95,6 +96,8 @@ typedef struct {
   int32_t precision;     /* F32 radix-16 sub-stages: 0 FP32 butterflies, 1 FP16 hi+lo tensor-core GEMM,
                             2 BF16 hi+lo tensor-core GEMM (FP32 accumulation, FP32 twiddles) */
   int32_t plain_loads;   /* 1: one-tile-per-CTA kernels only (no pipelined tensor-copy passes) */
+  int32_t f64_arith;     /* ComplexF64 passes: 0 block fixed point on the integer pipes (default), 1 FP64
+                            butterflies on the FP64 pipe (run-time-radix kernel) */
 } fftj_plan_opts_t;
 
 int fftj_plan_c2c_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch,
