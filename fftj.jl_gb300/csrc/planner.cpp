@@ -618,7 +618,7 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
     // ComplexF64: block fixed point unless the plan asks for FP64 butterflies
     pp.fx = (f64 && !g_sched.f64_arith) ? 1 : 0;
     pp.fx_cols = pp.fx ? pp.NB : 0;
-    pp.fx_b0 = 0;
+    pp.fx_b0 = 53;  // a pass without sub-stages (R = 1) copies: inputs stay exact
     pp.fx_sht = 0;
     if (pp.fx && pp.nsub > 0) {
       auto lg = [](int r) { int l = 0; while ((1 << l) < r) ++l; return l; };
