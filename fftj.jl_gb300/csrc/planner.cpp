@@ -227,6 +227,15 @@ i64 hvdh_t(i64 n) {
       while (((i64)o << k) < N) k++;
       t = std::min<i64>(t, (i64)o << k);
     }
+  } else {
+    // even n: the smallest odd 7-smooth length coprime to n
+    auto smooth7 = [](i64 m) {
+      for (int p : {3, 5, 7})
+        while (m % p == 0) m /= p;
+      return m == 1;
+    };
+    for (i64 m = N | 1; m <= 2 * n - 1; m += 2)
+      if (smooth7(m) && gcd_(m, n) == 1) { t = m; break; }
   }
   return (t != INT64_MAX && t - n < n) ? t : 0;
 }
@@ -1009,7 +1018,18 @@ template <typename T>
 int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir, double scale,
                  std::vector<Op>* ops, int* route) {
   std::vector<int> primes;
-  if (smooth13(n, &primes)) {
+  const bool smooth = smooth13(n, &primes);
+  // opts.route = 2 asks for Gaussian resampling: at full length (as
+  // FFTJ._hvdh, src/hvdh.jl:153-209, smooth lengths included) unless the
+  // length is even, non-smooth and taken by the split route. FFTJ throws
+  // ArgumentError when no smooth t is coprime to n (src/hvdh.jl:160-161).
+  if (g_sched.route == 2 && !g_tables.rs && n >= 2 &&
+      (smooth || n % 2 == 1 || !use_split(sizeof(T) == 8, n))) {
+    Hvdh hv = hvdh_parts(n, sizeof(T) == 8, scale, batch);
+    if (!hv.t) return fail(FFTJ_ERR_ARG, "no coprime smooth t for n = " + std::to_string(n));
+    if (hv.ok) return build_c2c_hvdh<T>(P, hv, batch, idist, odist, dir, ops, route);
+  }
+  if (smooth) {
     // intermediate passes use dense strides n
     std::vector<Op> tmp;
     int rc = build_axis_passes<T>(P, n, 1, batch, n, n, dir, scale, &tmp);

@@ -22,6 +22,7 @@
 #include <memory>
 #include <mutex>
 #include <stdexcept>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -942,17 +943,10 @@ struct ResamplePlan : PlanBase {
   }
 };
 
-// _anyplan routing (src/plan.jl:192-206). Composite/split are not restated;
-// HvdH-routed lengths fall back to the resampling restatement.
+// _anyplan routing (src/plan.jl:192-206), defined after the plans for
+// non-smooth lengths below
 template <typename T>
-static PlanBase* anyplan(i64 n, int D, T scale, int nthreads) {
-  if (n < 1) throw std::runtime_error("transform length must be positive");
-  if (!factor_radices(n).ok) return new ResamplePlan<T>(n, D, scale);
-  if (use_ragged<T>(n, nthreads > 1)) return new FourStepPlan<T>(n, D, scale, nthreads);
-  if (slow_smooth<T>(n)) return new ResamplePlan<T>(n, D, scale);
-  if (use_fourstep<T>(n, nthreads > 1 && n >= 2 * FS_TASK_MIN)) return new FourStepPlan<T>(n, D, scale, nthreads);
-  return new FFTPlan<T>(n, D, scale, nthreads);
-}
+static PlanBase* anyplan(i64 n, int D, T scale, int nthreads);
 
 // ---- real transforms (src/real.jl) ----------------------------------------
 template <typename T>
@@ -1091,6 +1085,457 @@ struct RsPass {
     }
   }
 };
+
+// ---- Gaussian resampling: HvdhPlan (src/hvdh.jl) ----------------------------
+// Restated from the reference's mathematics and parameters; the reference's
+// SIMD code advances the Gaussian entries and spread weights by
+// multiplicative recurrences with exact re-seeds (src/hvdh.jl:472-510,
+// 397-418), which this restatement evaluates directly with exp() -- the same
+// values up to rounding.
+static i64 gcd_i(i64 a, i64 b) {
+  a = a < 0 ? -a : a; b = b < 0 ? -b : b;
+  while (b) { i64 t = a % b; a = b; b = t; }
+  return a;
+}
+static i64 invmod_i(i64 a, i64 m) {  // a^{-1} mod m, gcd(a, m) = 1
+  i64 g = m, x = 0, x1 = 1, aa = ((a % m) + m) % m;
+  while (aa) {
+    i64 q = g / aa, t = g - q * aa;
+    g = aa; aa = t;
+    t = x - q * x1; x = x1; x1 = t;
+  }
+  return ((x % m) + m) % m;
+}
+static i64 fld_i(i64 a, i64 b) { i64 q = a / b; if ((a % b != 0) && ((a < 0) != (b < 0))) q--; return q; }
+static i64 cld_i(i64 a, i64 b) { return -fld_i(-a, b); }
+static i64 mod_i(i64 a, i64 m) { i64 r = a % m; return r < 0 ? r + m : r; }
+
+static const double HVDH_THETA_MIN = 1.0 / 128;  // src/hvdh.jl:67
+static const i64 HVDH_LTARGET = 256;             // src/hvdh.jl:68
+static const i64 HVDH_TABLE_MAX = 8 << 20;       // src/hvdh.jl:75
+
+// _hvdh_t (src/hvdh.jl:78-92): t coprime to n; 0 when there is none
+static i64 hvdh_t(i64 n) {
+  const i64 N = (i64)std::ceil(n * (1 + HVDH_THETA_MIN));
+  i64 t = INT64_MAX;
+  if (n % 2 == 1) {
+    for (int o : SMOOTH_ODD)
+      if (gcd_i(o, n) == 1) t = std::min<i64>(t, (i64)o << top_set_bit((N + o - 1) / o - 1));
+  } else {
+    for (i64 m = N | 1; m <= 2 * n - 1; m += 2)
+      if (factor_smooth(m) && gcd_i(m, n) == 1) { t = m; break; }
+  }
+  return (t != INT64_MAX && t - n < n) ? t : 0;
+}
+template <typename T>
+static bool use_hvdh(i64 n) { return n % 2 == 1 && n >= (sizeof(T) >= 8 ? 1000 : 16384); }  // src/hvdh.jl:97
+
+// Dense solve A x = b with partial pivoting (Julia's `\` on a square matrix).
+static void dense_solve(std::vector<double>& A, std::vector<double>& b, i64 m) {
+  for (i64 k = 0; k < m; ++k) {
+    i64 p = k;
+    for (i64 i = k + 1; i < m; ++i)
+      if (std::fabs(A[i * m + k]) > std::fabs(A[p * m + k])) p = i;
+    if (p != k) {
+      for (i64 j = 0; j < m; ++j) std::swap(A[k * m + j], A[p * m + j]);
+      std::swap(b[k], b[p]);
+    }
+    const double piv = A[k * m + k];
+    for (i64 i = k + 1; i < m; ++i) {
+      const double f = A[i * m + k] / piv;
+      if (f == 0) continue;
+      for (i64 j = k; j < m; ++j) A[i * m + j] -= f * A[k * m + j];
+      b[i] -= f * b[k];
+    }
+  }
+  for (i64 k = m - 1; k >= 0; --k) {
+    double s = b[k];
+    for (i64 j = k + 1; j < m; ++j) s -= A[k * m + j] * b[j];
+    b[k] = s / A[k * m + k];
+  }
+}
+
+// _hvdh_halo (src/hvdh.jl:117-145): halo rows from a few dense probes of the
+// l-indexed system's inverse
+static i64 hvdh_halo(i64 n, i64 t, double a, i64 B, double tol) {
+  const double rho = (double)t / n;
+  const i64 c = invmod_i(t - n, n);
+  std::vector<i64> probes;
+  const i64 L = std::min<i64>(n, 16);
+  for (i64 k = 0; k < L; ++k)
+    probes.push_back(L == 1 ? 0 : (i64)std::nearbyint((double)k * (double)(n - 1) / (double)(L - 1)));
+  for (i64 h : {n / 2, n / 2 + 1}) probes.push_back(mod_i(h * c, n));
+  i64 P = 64;
+  for (;;) {
+    i64 H = 0;
+    const i64 m = 2 * P + 1;
+    for (i64 l0 : probes) {
+      // transpose(M) r = e, built transposed: A[j][i] = M[i][j]
+      std::vector<double> A(m * m, 0.0), r(m, 0.0);
+      for (i64 i = 0; i < m; ++i)
+        for (i64 j = std::max<i64>(0, i - B - 1); j <= std::min<i64>(m - 1, i + B + 1); ++j) {
+          const i64 li = l0 - P + i, lj = l0 - P + j;
+          const double d = rho * lj - (double)fld_i(2 * t * li + n, 2 * n);
+          A[j * m + i] = std::exp(-a * d * d);
+        }
+      r[P] = 1;
+      dense_solve(A, r, m);
+      double mx = 0;
+      for (i64 j = 0; j < m; ++j) mx = std::max(mx, std::fabs(r[j]));
+      for (i64 j = 0; j < m; ++j)
+        if (std::fabs(r[j]) > tol * mx) H = std::max<i64>(H, std::llabs(j - P));
+    }
+    if (H < P - 2 * B) return (i64)std::ceil(rho * H) + B;
+    P *= 2;
+    if (P > 8192) throw std::runtime_error("HvdH halo did not converge");
+  }
+}
+
+// 2 t l' - 2 n q + n and l' for the first unknown l' with rho l' >= q - 1/2
+// (_hvdh_e, src/hvdh.jl:147-151)
+static void hvdh_e(i64 n, i64 t, i64 q, i64* e, i64* l) {
+  *l = cld_i(2 * n * q - n, 2 * t);
+  *e = 2 * t * (*l) - 2 * n * q + n;
+}
+
+// HvdhPlan (src/hvdh.jl:30-58, 153-230): scatter, Gaussian spread onto the
+// t-grid, length-t transform, banded solve by chunks (K chunks per group,
+// L core rows + H halo rows per side), scale n/t.
+template <typename T>
+struct HvdhPlan : PlanBase {
+  int D;
+  T scale;
+  i64 t, Delta, c, h, w, B, H, K, G, L, R;
+  double alpha, a, b;
+  std::vector<i64> se, sx, so;
+  std::unique_ptr<PlanBase> pt;
+  bool tab;  // factors precomputed (:table) or rebuilt per call (:fly)
+  // per chunk: multipliers f[i][k] (k = 1..B), 1/U_ii, U_{i,i+1..i+B}, output index
+  std::vector<T> lt, ut;
+  std::vector<i64> ot;
+  // factors: 0 :auto, 1 :table, 2 :fly (src/hvdh.jl:187-191)
+  HvdhPlan(i64 n_, int D_, T scale_, int factors) : D(D_), scale(scale_) {
+    n = n_;
+    route = ORC_HVDH;
+    t = hvdh_t(n);
+    if (!t) throw std::invalid_argument("no coprime smooth t");
+    Delta = t - n;
+    c = invmod_i(Delta, n);
+    alpha = sizeof(T) >= 8 ? 1.45 : 1.0;  // _hvdh_alpha (src/hvdh.jl:64)
+    a = M_PI * alpha * alpha;
+    b = M_PI / (alpha * alpha);
+    const double tol = (sizeof(T) >= 8 ? 2.220446049250313e-16 : 1.1920928955078125e-07) / 4;
+    h = (i64)std::ceil(alpha * std::sqrt(std::log(1 / tol) / M_PI));
+    w = 2 * h;
+    B = (i64)std::floor(std::sqrt(std::log(1 / tol) / a) + 0.5);
+    if (2 * B + 1 > 8) throw std::invalid_argument("band too wide");
+    H = hvdh_halo(n, t, a, B, tol);
+    K = pick_width<T>();
+    G = std::max<i64>(1, cld_i(t, K * HVDH_LTARGET));
+    L = cld_i(t, K * G);
+    R = L + 2 * H;
+    se.resize(G * K); sx.resize(G * K); so.resize(G * K);
+    for (i64 ch = 0; ch < G * K; ++ch) {
+      const i64 q0 = mod_i(ch * L - H, t);
+      i64 e, l;
+      hvdh_e(n, t, q0 - B, &e, &l);
+      se[ch] = e;
+      sx[ch] = q0;
+      hvdh_e(n, t, q0, &e, &l);
+      so[ch] = mod_i((i64)((__int128)Delta * l % n), n);
+    }
+    pt.reset(anyplan<T>(t, D, (T)1, 1));
+    const i64 ufl = (R + B) * (B + 1) * K;
+    const i64 tbytes = G * (R * B * K * (i64)sizeof(T) + ufl * (i64)sizeof(T) + R * K * 8);
+    tab = factors == 1 || (factors == 0 && tbytes <= HVDH_TABLE_MAX);
+    if (tab) {
+      lt.resize(G * K * R * B); ut.resize(G * K * R * (B + 1)); ot.resize(G * K * R);
+      for (i64 ch = 0; ch < G * K; ++ch)
+        factor(ch, &lt[ch * R * B], &ut[ch * R * (B + 1)], &ot[ch * R]);
+    }
+  }
+  // the band of chunk ch, eliminated row by row without pivoting
+  // (_hvdh_prime!, _hvdh_row!, _hvdh_factor!: src/hvdh.jl:500-540, 617-633)
+  void factor(i64 ch, T* lf, T* uf, i64* ob) const {
+    // column j (relative to the chunk's first row, j in [-B, R + B)):
+    // beta' = (e - n) / 2n, an unknown sits there when e < 2n
+    const i64 nc = R + 2 * B;
+    std::vector<double> beta(nc);
+    std::vector<char> hit(nc);
+    i64 e = se[ch];
+    for (i64 j = 0; j < nc; ++j) {
+      hit[j] = e < 2 * n;
+      beta[j] = (double)(e - n) / (2.0 * n);
+      e = hit[j] ? e + 2 * Delta : e - 2 * n;
+    }
+    i64 on = so[ch];
+    // rows -B .. -1: identity pads
+    std::vector<T> U((R + B) * (B + 1), (T)0);
+    for (i64 i = 0; i < B; ++i) U[i * (B + 1)] = (T)1;
+    for (i64 i = 0; i < R; ++i) {
+      const i64 ci = i + B;  // column index of row i
+      std::vector<T> r(2 * B + 1, (T)0);
+      if (hit[ci]) {
+        for (i64 m = -B; m <= B; ++m) {
+          const i64 cj = ci + m;
+          if (!hit[cj]) continue;
+          const double d = (double)m + beta[cj];
+          r[m + B] = (T)std::exp(-a * d * d);
+        }
+      } else {
+        r[B] = (T)1;
+      }
+      for (i64 k = B; k >= 1; --k) {
+        const T* ur = &U[(i - k + B) * (B + 1)];
+        const T fk = r[B - k] * ur[0];
+        lf[i * B + (k - 1)] = fk;
+        for (i64 j = 1; j <= B; ++j) r[B - k + j] = std::fma(-fk, ur[j], r[B - k + j]);
+      }
+      T* ur = &U[(i + B) * (B + 1)];
+      ur[0] = (T)1 / r[B];
+      for (i64 j = 1; j <= B; ++j) ur[j] = r[B + j];
+      for (i64 j = 0; j <= B; ++j) uf[i * (B + 1) + j] = ur[j];
+      ob[i] = hit[ci] ? on : -1;
+      if (hit[ci]) { on += Delta; if (on >= n) on -= n; }
+    }
+  }
+  void exec(const void* xv, void* yv) override {
+    const T* x = (const T*)xv;
+    T* y = (T*)yv;
+    // _hvdh_scatter! (src/hvdh.jl:246-294): ys[l Delta mod n] = u_l
+    std::vector<T> ys(2 * n);
+    for (i64 l = 0; l < n; ++l) {
+      const i64 m = (i64)((__int128)l * Delta % n);
+      ys[2 * m] = x[2 * l]; ys[2 * m + 1] = x[2 * l + 1];
+    }
+    // _hvdh_spread! (src/hvdh.jl:337-470): v[q] = sum over taps o of
+    // exp(-b (delta_q - o)^2) / alpha * ys[(q + (o - 1) Delta) mod n],
+    // delta_q = (t - q) / t, o = 1 - w/2 .. w/2
+    std::vector<T> v(2 * t), Y(2 * t);
+    const i64 hw = w / 2;
+    for (i64 q = 0; q < t; ++q) {
+      const double dq = (double)(t - q) / (double)t;
+      T re = 0, im = 0;
+      for (i64 o = 1 - hw; o <= hw; ++o) {
+        const double d = dq - (double)o;
+        const T wt = (T)(std::exp(-b * d * d) / alpha);
+        const i64 m = mod_i(q + (o - 1) * Delta, n);
+        re = std::fma(wt, ys[2 * m], re);
+        im = std::fma(wt, ys[2 * m + 1], im);
+      }
+      v[2 * q] = re; v[2 * q + 1] = im;
+    }
+    pt->exec(v.data(), Y.data());
+    // _hvdh_groups! -> _hvdh_subst! / _hvdh_group!, _hvdh_back!
+    // (src/hvdh.jl:232-240, 560-686)
+    std::vector<T> lf, uf;
+    std::vector<i64> ob;
+    if (!tab) { lf.resize(R * B); uf.resize(R * (B + 1)); ob.resize(R); }
+    std::vector<T> zr(R + 2 * B), zi(R + 2 * B);
+    const T sc = scale * (T)n / (T)t;
+    for (i64 ch = 0; ch < G * K; ++ch) {
+      const T* L_ = tab ? &lt[ch * R * B] : lf.data();
+      const T* U_ = tab ? &ut[ch * R * (B + 1)] : uf.data();
+      const i64* O_ = tab ? &ot[ch * R] : ob.data();
+      if (!tab) factor(ch, lf.data(), uf.data(), ob.data());
+      std::fill(zr.begin(), zr.end(), (T)0);
+      std::fill(zi.begin(), zi.end(), (T)0);
+      i64 idx = sx[ch];
+      for (i64 i = 0; i < R; ++i) {
+        T ar = 0, ai = 0;
+        if (O_[i] >= 0) { ar = Y[2 * idx]; ai = Y[2 * idx + 1]; }
+        for (i64 k = B; k >= 1; --k) {
+          const T f = L_[i * B + (k - 1)];
+          ar = std::fma(-f, zr[i - k + B], ar);
+          ai = std::fma(-f, zi[i - k + B], ai);
+        }
+        zr[i + B] = ar; zi[i + B] = ai;
+        if (++idx >= t) idx -= t;
+      }
+      for (i64 i = R - 1; i >= H; --i) {
+        const T* ur = U_ + i * (B + 1);
+        T xr = zr[i + B], xi = zi[i + B];
+        for (i64 j = 1; j <= B; ++j) {
+          xr = std::fma(-ur[j], zr[i + B + j], xr);
+          xi = std::fma(-ur[j], zi[i + B + j], xi);
+        }
+        xr *= ur[0]; xi *= ur[0];
+        zr[i + B] = xr; zi[i + B] = xi;
+        if (i < H + L && O_[i] >= 0) { y[2 * O_[i]] = xr * sc; y[2 * O_[i] + 1] = xi * sc; }
+      }
+    }
+  }
+  void info(std::vector<i64>& vv) override {
+    vv.push_back(route); vv.push_back(n); vv.push_back(t); vv.push_back(w); vv.push_back(B); vv.push_back(H);
+    vv.push_back(L); vv.push_back(G * K); vv.push_back(tab ? 1 : 2);
+  }
+};
+
+// smooth part s (2, 3, 5, 7) of n (_smooth_part, src/composite.jl:43-51)
+static i64 smooth_part(i64 n) {
+  i64 s = 1;
+  for (int f : {2, 3, 5, 7})
+    while (n % (s * f) == 0) s *= f;
+  return s;
+}
+static const i64 COMPOSITE_MIN_S = 16;    // src/composite.jl:37
+static const i64 COMPOSITE_HV_MINP = 500;  // src/composite.jl:42
+template <typename T>
+static bool use_composite(i64 n) {  // src/composite.jl:53-54
+  return n >= (sizeof(T) >= 8 ? 4096 : 32768) && smooth_part(n) >= COMPOSITE_MIN_S;
+}
+template <typename T>
+static bool use_split(i64 n) {  // src/composite.jl:131-135
+  const i64 s = smooth_part(n);
+  return n % 2 == 0 && s < COMPOSITE_MIN_S && use_hvdh<T>(n / s) && n >= (sizeof(T) >= 8 ? 16384 : 65536);
+}
+
+// w_n^e (sign D) as the reference's two-level product hi[e / K] lo[e % K]
+// (_tw2, src/composite.jl:275-279; tables src/composite.jl:61-73)
+template <typename T>
+struct TwoLevel {
+  i64 n, K;
+  std::vector<T> hir, hii, lor, loi;
+  TwoLevel(i64 n_, int D) : n(n_) {
+    K = isqrt_(n - 1) + 1;
+    const i64 nh = (n + K - 1) / K;
+    hir.resize(nh); hii.resize(nh); lor.resize(K); loi.resize(K);
+    for (i64 i = 0; i < nh; ++i) {
+      double s, co;
+      sincospi((double)(2 * D * i * K) / (double)n, &s, &co);
+      hir[i] = (T)co; hii[i] = (T)s;
+    }
+    for (i64 i = 0; i < K; ++i) {
+      double s, co;
+      sincospi((double)(2 * D * i) / (double)n, &s, &co);
+      lor[i] = (T)co; loi[i] = (T)s;
+    }
+  }
+  void at(i64 e, T* wr, T* wi) const {
+    const i64 hi = e / K, lo = e % K;
+    *wr = hir[hi] * lor[lo] - hii[hi] * loi[lo];
+    *wi = hir[hi] * loi[lo] + hii[hi] * lor[lo];
+  }
+};
+
+// CompositePlan (src/composite.jl:10-101): n = p s, j = j1 + p j2,
+// k = k2 + s k1: length-s transforms over j2 (batch p), twiddles
+// w_n^(j1 k2), then the length-p transforms over j1 for each k2 by
+// resampling -- batched HvdH (HvPass) for p >= 500, else batched
+// oversampled resampling (RsPass). The restatement runs each lane's
+// length-p transform with the single-transform HvdH plan (the batched pass
+// shares its weights and factors one cyclic band; same mathematics).
+template <typename T>
+struct CompositePlan : PlanBase {
+  int D;
+  T scale;
+  i64 p, s;
+  std::vector<Stage<T>> stages;
+  std::unique_ptr<HvdhPlan<T>> hv;
+  std::unique_ptr<RsPass<T>> rs;
+  TwoLevel<T> tw;
+  CompositePlan(i64 n_, int D_, T scale_) : D(D_), scale(scale_), tw(n_, D_) {
+    n = n_;
+    route = ORC_COMPOSITE;
+    s = smooth_part(n);
+    p = n / s;
+    stages = build_stages<T>(s, D, false);
+    if (p >= COMPOSITE_HV_MINP) hv.reset(new HvdhPlan<T>(p, D, (T)1, 0));
+    else rs.reset(new RsPass<T>(p, D, s));
+  }
+  void exec(const void* xv, void* yv) override {
+    const T* x = (const T*)xv;
+    T* y = (T*)yv;
+    std::vector<T> are(n), aim(n), bre(n), bim(n);
+    for (i64 i = 0; i < n; ++i) { are[i] = x[2 * i]; aim[i] = x[2 * i + 1]; }
+    const bool sw = run_chain(are.data(), aim.data(), bre.data(), bim.data(), stages, 0, stages.size(), s, 1, p, D, 1);
+    const T* cre = sw ? bre.data() : are.data();
+    const T* cim = sw ? bim.data() : aim.data();
+    // c[j1 + p k2] -> o[k2 + s j1] with the twiddle w_n^(j1 k2)
+    std::vector<T> ore(n), oim(n);
+    for (i64 k2 = 0; k2 < s; ++k2)
+      for (i64 j1 = 0; j1 < p; ++j1) {
+        T wr, wi;
+        tw.at(j1 * k2, &wr, &wi);
+        const T zr = cre[j1 + p * k2], zi = cim[j1 + p * k2];
+        ore[k2 + s * j1] = zr * wr - zi * wi;
+        oim[k2 + s * j1] = zr * wi + zi * wr;
+      }
+    if (rs) {
+      rs->run(ore.data(), oim.data(), 0, D);  // rows j1 of s lanes k2, in place: rows k1
+      for (i64 i = 0; i < n; ++i) { y[2 * i] = ore[i] * scale; y[2 * i + 1] = oim[i] * scale; }
+    } else {
+      std::vector<T> lin(2 * p), lout(2 * p);
+      for (i64 k2 = 0; k2 < s; ++k2) {
+        for (i64 j1 = 0; j1 < p; ++j1) { lin[2 * j1] = ore[k2 + s * j1]; lin[2 * j1 + 1] = oim[k2 + s * j1]; }
+        hv->exec(lin.data(), lout.data());
+        for (i64 k1 = 0; k1 < p; ++k1) {
+          y[2 * (k2 + s * k1)] = lout[2 * k1] * scale;
+          y[2 * (k2 + s * k1) + 1] = lout[2 * k1 + 1] * scale;
+        }
+      }
+    }
+  }
+  void info(std::vector<i64>& v) override { v.push_back(route); v.push_back(n); v.push_back(p); v.push_back(s); }
+};
+
+// SplitPlan (src/composite.jl:103-280): decimation in time, x_r[j] =
+// x[r + s j]; s length-p HvdH transforms (unnormalized); planes
+// p r + k1 <- w_n^(r k1) Y_r[k1]; the length-s chain over r (batch p)
+// writes X[k1 + p k2] in natural order.
+template <typename T>
+struct SplitPlan : PlanBase {
+  int D;
+  T scale;
+  i64 p, s;
+  std::unique_ptr<HvdhPlan<T>> hv;
+  std::vector<Stage<T>> stages;
+  TwoLevel<T> tw;
+  SplitPlan(i64 n_, int D_, T scale_) : D(D_), scale(scale_), tw(n_, D_) {
+    n = n_;
+    route = ORC_SPLIT;
+    s = smooth_part(n);
+    p = n / s;
+    hv.reset(new HvdhPlan<T>(p, D, (T)1, 0));
+    stages = build_stages<T>(s, D, false);
+  }
+  void exec(const void* xv, void* yv) override {
+    const T* x = (const T*)xv;
+    T* y = (T*)yv;
+    std::vector<T> xs(2 * p), ys(2 * p), are(n), aim(n), bre(n), bim(n);
+    for (i64 r = 0; r < s; ++r) {
+      for (i64 j = 0; j < p; ++j) { xs[2 * j] = x[2 * (s * j + r)]; xs[2 * j + 1] = x[2 * (s * j + r) + 1]; }
+      hv->exec(xs.data(), ys.data());
+      for (i64 k1 = 0; k1 < p; ++k1) {  // _split_twiddle! (src/composite.jl:240-272)
+        T wr, wi;
+        tw.at(r * k1, &wr, &wi);
+        are[p * r + k1] = ys[2 * k1] * wr - ys[2 * k1 + 1] * wi;
+        aim[p * r + k1] = ys[2 * k1] * wi + ys[2 * k1 + 1] * wr;
+      }
+    }
+    const bool sw = run_chain(are.data(), aim.data(), bre.data(), bim.data(), stages, 0, stages.size(), s, 1, p, D, 1);
+    const T* cre = sw ? bre.data() : are.data();
+    const T* cim = sw ? bim.data() : aim.data();
+    for (i64 i = 0; i < n; ++i) { y[2 * i] = cre[i] * scale; y[2 * i + 1] = cim[i] * scale; }
+  }
+  void info(std::vector<i64>& v) override { v.push_back(route); v.push_back(n); v.push_back(p); v.push_back(s); }
+};
+
+// _anyplan routing (src/plan.jl:192-206)
+template <typename T>
+static PlanBase* anyplan(i64 n, int D, T scale, int nthreads) {
+  if (n < 1) throw std::runtime_error("transform length must be positive");
+  if (!factor_radices(n).ok) {
+    if (use_composite<T>(n)) return new CompositePlan<T>(n, D, scale);
+    if (use_hvdh<T>(n)) return new HvdhPlan<T>(n, D, scale, 0);
+    if (use_split<T>(n)) return new SplitPlan<T>(n, D, scale);
+    return new ResamplePlan<T>(n, D, scale);
+  }
+  if (use_ragged<T>(n, nthreads > 1)) return new FourStepPlan<T>(n, D, scale, nthreads);
+  if (slow_smooth<T>(n)) return new ResamplePlan<T>(n, D, scale);
+  if (use_fourstep<T>(n, nthreads > 1 && n >= 2 * FS_TASK_MIN)) return new FourStepPlan<T>(n, D, scale, nthreads);
+  return new FFTPlan<T>(n, D, scale, nthreads);
+}
 
 template <typename T>
 struct DimPass {
@@ -1275,6 +1720,24 @@ struct Handle {
 };
 }  // namespace
 
+static std::string g_orc_err;
+template <template <typename> class PT, typename... A>
+static void* plan_direct(int dtype, int64_t n, int D, int scale_mode, A... args) {
+  try {
+    Handle* h = new Handle();
+    h->dtype = dtype; h->kind = 0; h->n = n; h->nin = 2 * n; h->nout = 2 * n;
+    try {
+      if (dtype == 0) h->p32.reset(new PT<float>(n, D, scale_mode ? 1.0f : default_scale<float>(n, D), args...));
+      else h->p64.reset(new PT<double>(n, D, scale_mode ? 1.0 : default_scale<double>(n, D), args...));
+    } catch (const std::exception& e) {
+      g_orc_err = e.what();
+      delete h;
+      return nullptr;
+    }
+    g_orc_err.clear();
+    return h;
+  } catch (...) { return nullptr; }
+}
 extern "C" {
 
 void orc_set_vector_bits(int bits) { g_vector_bits = bits; }
@@ -1289,6 +1752,16 @@ void* orc_plan_c2c(int dtype, int64_t n, int D, int scale_mode, int nthreads) {
     else h->p64.reset(anyplan<double>(n, D, scale_mode ? 1.0 : default_scale<double>(n, D), nthreads));
     return h;
   } catch (...) { return nullptr; }
+}
+const char* orc_last_error(void) { return g_orc_err.c_str(); }
+void* orc_plan_hvdh(int dtype, int64_t n, int D, int scale_mode, int factors) {
+  return plan_direct<HvdhPlan>(dtype, n, D, scale_mode, factors);
+}
+void* orc_plan_composite(int dtype, int64_t n, int D, int scale_mode) {
+  return plan_direct<CompositePlan>(dtype, n, D, scale_mode);
+}
+void* orc_plan_split(int dtype, int64_t n, int D, int scale_mode) {
+  return plan_direct<SplitPlan>(dtype, n, D, scale_mode);
 }
 int orc_plan_route(void* p) {
   Handle* h = (Handle*)p;

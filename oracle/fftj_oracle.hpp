@@ -22,6 +22,8 @@ enum orc_route {
   ORC_FOURSTEP = 1,   // four-step (src/fourstep.jl:130-156)
   ORC_RESAMPLE = 2,   // oversampled resampling (src/resample.jl:175-182)
   ORC_HVDH = 3,       // Gaussian resampling (src/hvdh.jl:30-58)
+  ORC_COMPOSITE = 5,  // smooth part first, then batched resampling (src/composite.jl:10-101)
+  ORC_SPLIT = 6,      // decimation in time into HvdH sub-transforms (src/composite.jl:103-280)
 };
 
 // Host SIMD width FFTJ would see (src/kernels.jl:11-22). 128 = NEON (the GPU
@@ -55,6 +57,15 @@ void* orc_plan_rfft_nd(int dtype, int rank, const int64_t* dims, int nthreads);
 void* orc_plan_irfft_nd(int dtype, int rank, const int64_t* dims, int normalized, int nthreads);
 int orc_execute_rfft_nd(void* plan, const void* x, void* y);
 int orc_execute_irfft_nd(void* plan, const void* x, void* y);
+
+// Plans of a given type, built directly as the reference's tests build them
+// (FFTJ._hvdh, FFTJ._composite, FFTJ._split). factors: 0 :auto, 1 :table
+// (factors tabulated at plan time), 2 :fly (rebuilt every call). NULL when
+// the reference throws ArgumentError (orc_last_error gives the message).
+void* orc_plan_hvdh(int dtype, int64_t n, int D, int scale_mode, int factors);
+void* orc_plan_composite(int dtype, int64_t n, int D, int scale_mode);
+void* orc_plan_split(int dtype, int64_t n, int D, int scale_mode);
+const char* orc_last_error(void);
 
 // FP64 direct DFT, exact integer angle reduction, double-double accumulation.
 // sign = -1 forward (no scaling), +1 backward (no scaling).

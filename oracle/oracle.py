@@ -14,7 +14,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "liboracle_fftj.so")
 _lib = None
 
-ROUTES = {0: "FFTPlan", 1: "FourStepPlan", 2: "ResamplePlan", 3: "HvdhPlan"}
+ROUTES = {0: "FFTPlan", 1: "FourStepPlan", 2: "ResamplePlan", 3: "HvdhPlan", 5: "CompositePlan",
+          6: "SplitPlan"}
 
 
 def build(quiet=True):
@@ -56,6 +57,13 @@ def lib():
         L.orc_execute_rfft_nd.argtypes = [vp, vp, vp]
         L.orc_execute_irfft_nd.argtypes = [vp, vp, vp]
         L.orc_dft_f64.argtypes = [i64, vp, vp, i32]
+        L.orc_plan_hvdh.restype = vp
+        L.orc_plan_hvdh.argtypes = [i32, i64, i32, i32, i32]
+        L.orc_plan_composite.restype = vp
+        L.orc_plan_composite.argtypes = [i32, i64, i32, i32]
+        L.orc_plan_split.restype = vp
+        L.orc_plan_split.argtypes = [i32, i64, i32, i32]
+        L.orc_last_error.restype = ctypes.c_char_p
         L.orc_set_vector_bits.argtypes = [i32]
         L.orc_max_threads.restype = i32
         L.orc_nextsmooth.restype = i64
@@ -110,6 +118,32 @@ class Plan1D:
         if getattr(self, "h", None):
             lib().orc_destroy(self.h)
             self.h = None
+
+
+class PlanDirect(Plan1D):
+    """A 1-D complex plan of a given type, built directly as the reference's
+    tests build them: kind 'hvdh' (FFTJ._hvdh; factors 'auto' | 'table' |
+    'fly'), 'composite' (FFTJ._composite) or 'split' (FFTJ._split). direction
+    'fft' | 'ifft' | 'bfft'. Raises ValueError where the reference throws
+    ArgumentError (e.g. HvdH at n = 390: no coprime smooth t)."""
+
+    def __init__(self, dtype, n, kind, direction="fft", factors="auto"):
+        self.dt = _dt(dtype)
+        self.n = int(n)
+        D = -1 if direction == "fft" else 1
+        sm = 1 if direction == "bfft" else 0
+        if kind == "hvdh":
+            f = {"auto": 0, "table": 1, "fly": 2}[factors]
+            self.h = lib().orc_plan_hvdh(self.dt, self.n, D, sm, f)
+        elif kind == "composite":
+            self.h = lib().orc_plan_composite(self.dt, self.n, D, sm)
+        elif kind == "split":
+            self.h = lib().orc_plan_split(self.dt, self.n, D, sm)
+        else:
+            raise ValueError("kind must be hvdh, composite or split")
+        if not self.h:
+            raise ValueError("oracle %s plan failed for n=%d: %s" % (kind, n, lib().orc_last_error().decode()))
+        self.ctype = np.complex64 if self.dt == 0 else np.complex128
 
 
 class PlanReal:

@@ -26,7 +26,8 @@ MIXED = [3, 5, 6, 7, 9, 10, 12, 14, 15, 20, 21, 24, 25, 27, 35, 45, 48, 49, 60,
          15 * 2 ** 7, 105 * 2 ** 4, 11, 13, 22, 26, 429, 352, 416, 1001,
          11 ** 2 * 2 ** 4, 13 ** 2 * 2 ** 4]                             # :39-45
 NONSMOOTH = [17, 19, 23, 34, 38, 51, 97, 101, 289, 331, 361, 997, 1026, 1234, 2050]  # :61-63
-HVDH = [46, 202, 3107]                                                  # :114-115 subset
+HVDH = [11, 13, 17, 19, 22, 23, 26, 34, 38, 46, 97, 101, 202, 331, 997, 1001, 3107, 10007,
+        20011]                                                          # :114-115 (65537 at test time)
 RAGGED = [3 ** 8, 5 ** 5, 2835, 1000]                                    # :212 subset
 REAL = [1, 2, 3, 4, 5, 6, 8, 11, 16, 22, 34, 64, 100, 255, 256, 257, 1024, 768, 1000, 4096]  # :235-236
 ND = [(64, 48), (33, 17), (16, 11), (11, 16), (8, 1), (1, 8), (128, 3, 5), (16, 16, 16),

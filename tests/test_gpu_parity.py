@@ -193,8 +193,9 @@ def _dft_bins(x, ks, sign=-1):
 
 @pytest.mark.parametrize("T,logn", [(np.float32, 26), (np.float64, 24)])
 def test_config_large_single(fftj, T, logn):
-    """Single ComplexF32 2^26 / ComplexF64 2^24 (U[-1,1)): sampled FP64 bins,
-    Parseval, inverse round trip."""
+    """Single ComplexF32 2^26 / ComplexF64 2^24 (U[-1,1)): the whole output
+    vector against FP64 numpy, exact FP64 DFT bins, Parseval, inverse round
+    trip."""
     n = 1 << logn
     rng = np.random.default_rng(logn)
     x = (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)).astype(np.complex64 if T == np.float32 else np.complex128)
@@ -210,6 +211,10 @@ def test_config_large_single(fftj, T, logn):
     px = np.sum(np.abs(x.astype(np.complex128)) ** 2) * n
     py = np.sum(np.abs(yh.astype(np.complex128)) ** 2)
     assert abs(py - px) / px <= parity_tol(T, n)
+    # full vector vs FP64 (numpy pocketfft in complex128)
+    full = np.fft.fft(x.astype(np.complex128))
+    assert rel_l2(yh, full) <= parity_tol(T, n), rel_l2(yh, full) / EPS[T]
+    del full
     xi = host(fftj.plan_ifft(T, n)(y))
     assert rel_l2(xi, x) <= 2 * parity_tol(T, n)
 
@@ -398,7 +403,9 @@ def test_hvdh_route_and_parity(fftj, orc, T, n):
     tol = parity_tol(T, n)
     ref = np.fft.fft(x, axis=-1)
     assert rel_l2(host(y), ref) <= tol, (n, rel_l2(host(y), ref) / EPS[T])
-    assert rel_l2(host(y)[:1], orc.Plan1D(T, n, "fft")(x[:1])) <= tol
+    po = orc.Plan1D(T, n, "fft")
+    assert po.route == "HvdhPlan"  # the oracle's HvdH restatement (src/hvdh.jl)
+    assert rel_l2(host(y)[:1], po(x[:1])) <= tol
     xi = host(fftj.plan_ifft(T, n, batch=B)(y))
     assert rel_l2(xi, x) <= 2 * tol
     xb = host(fftj.plan_bfft(T, n, batch=B)(dev(ref, T)))
@@ -433,7 +440,7 @@ def test_odd_radix_lengths_that_need_two_passes(fftj, orc, T, n):
 @pytest.mark.parametrize("T,n,B", [(np.float64, 2 * 10007, 2), (np.float64, 6 * 3001, 3), (np.float64, 16 * 509, 4),
                                    (np.float64, 30 * 4099, 1), (np.float64, 1024 * 1009, 1),
                                    (np.float32, 4 * 32771, 2), (np.float32, 64 * 1031, 1)])
-def test_split_route(fftj, T, n, B):
+def test_split_route(fftj, orc, T, n, B):
     """Even non-smooth lengths n = s p (s 7-smooth, p odd and Gaussian-
     resampled): decimation, s HvdH sub-transforms with the w_n^(r k1)
     twiddles in their banded solve, length-s passes along r (FFTJ
@@ -446,5 +453,41 @@ def test_split_route(fftj, T, n, B):
     y = p(dev(x, T))
     tol = parity_tol(T, n)
     assert rel_l2(host(y), np.fft.fft(x, axis=-1)) <= tol
+    # the FFTJ CPU plan FFTJ routes this length to: CompositePlan (s >= 16)
+    # or SplitPlan (s < 16), restated in the oracle (src/composite.jl)
+    po = orc.Plan1D(T, n, "fft")
+    assert po.route in ("CompositePlan", "SplitPlan"), po.route
+    assert rel_l2(host(y)[:1], po(x[:1])) <= tol
     xi = host(fftj.plan_ifft(T, n, batch=B)(y))
     assert rel_l2(xi, x) <= 2 * tol
+
+
+# FFTJ's HvdH test sizes (test/runtests.jl:110-137), the route forced to
+# Gaussian resampling (opts.route = 2, as the reference's tests build
+# FFTJ._hvdh directly): tiny and even lengths, halos wider than t.
+HVDH_FORCED = [11, 13, 17, 19, 22, 23, 26, 34, 38, 46, 97, 101, 202, 331, 997, 1001]
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_hvdh_forced_reference_sizes(fftj, orc, T):
+    for n in HVDH_FORCED:
+        rng = np.random.default_rng([0x4D4, n])
+        x = cn(rng, (2, n))
+        p = fftj.Plan(T, (n,), kind="c2c", batch=2, opts={"route": 2})
+        assert p.route == "HvdhPlan", (n, p.route)
+        y = host(p(dev(x, T)))
+        tol = 50 * EPS[T]  # runtests.jl:121
+        assert rel_l2(y, np.fft.fft(x, axis=-1)) <= tol, (n, rel_l2(y, np.fft.fft(x, axis=-1)) / EPS[T])
+        yo = orc.PlanDirect(T, n, "hvdh")(x[0])
+        assert rel_l2(y[0], yo) <= tol, (n, rel_l2(y[0], yo) / EPS[T])
+        pinv = fftj.Plan(T, (n,), kind="c2c", batch=2, direction=1, scale=1.0 / n, opts={"route": 2})
+        xi = host(pinv(dev(y, T)))
+        assert rel_l2(xi, x) <= tol, (n, rel_l2(xi, x) / EPS[T])
+
+
+def test_hvdh_no_coprime_t(fftj):
+    """runtests.jl:139: HvdH at n = 390 (an even multiple of 30) has no smooth
+    t coprime to n: ArgumentError, as FFTJ._hvdh throws."""
+    for T in T_LIST:
+        with pytest.raises(fftj.ArgumentError, match="no coprime smooth t"):
+            fftj.Plan(T, (390,), kind="c2c", opts={"route": 2})

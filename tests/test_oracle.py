@@ -142,3 +142,135 @@ def test_threaded_bitwise_serial(orc, T):
             if orc.Plan1D(T, n, "fft", nthreads=1).info()[2:4] == info[2:4]:
                 assert np.array_equal(y1, y4), n
         assert rel_l2(y4, np.fft.fft(x)) <= 50 * EPS[T]
+
+
+# ---------------------------------------------------------------------------
+# Gaussian resampling (HvdhPlan), CompositePlan and SplitPlan restatements,
+# at the reference's own test sizes and tolerance classes.
+
+# test/runtests.jl:114-115
+HVDH_SIZES = [11, 13, 17, 19, 22, 23, 26, 34, 38, 46, 97, 101, 202, 331, 997, 1001, 3107, 10007,
+              20011, 65537]
+# test/runtests.jl:148-150 (filtered by _use_composite per dtype)
+COMPOSITE_SIZES = [17 * 1024, 101 * 64, 1009 * 16, 19 * 3072, 17 * 2 ** 13, 101 * 1024, 1009 * 64,
+                   10007 * 32, 17 * 19 * 512, 3 ** 4 * 5 * 7 * 101]
+# test/runtests.jl:88-89
+SPLIT_SIZES = [2 * 1009, 6 * 1009, 14 * 1009, 2 * 10007, 4 * 10007, 12 * 2003, 2 * 32771, 8 * 16411,
+               2 * 65537]
+
+
+def _smooth_part(n):  # src/composite.jl:43-51
+    s = 1
+    for f in (2, 3, 5, 7):
+        while n % (s * f) == 0:
+            s *= f
+    return s
+
+
+def _use_hvdh(T, n):  # src/hvdh.jl:97
+    return n % 2 == 1 and n >= (1000 if T == np.float64 else 16384)
+
+
+def _use_composite(T, n):  # src/composite.jl:53-54
+    return n >= (4096 if T == np.float64 else 32768) and _smooth_part(n) >= 16
+
+
+def _use_split(T, n):  # src/composite.jl:131-135
+    s = _smooth_part(n)
+    return n % 2 == 0 and s < 16 and _use_hvdh(T, n // s) and n >= (16384 if T == np.float64 else 65536)
+
+
+def _smooth13(n):
+    for p in (2, 3, 5, 7, 11, 13):
+        while n % p == 0:
+            n //= p
+    return n == 1
+
+
+def _input(golden, n, seed):
+    key = "c2c_x_%d" % n
+    if key in golden.files:
+        return golden[key], golden["c2c_y_%d" % n]
+    rng = np.random.default_rng([seed, n])
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)
+    return x, np.fft.fft(x)
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_hvdh_reference_sizes(golden, orc, T):
+    """runtests.jl:110-137: FFTJ._hvdh at every size within 50 eps of FFTW
+    (here: the golden FP64 outputs / numpy), :fly factors equal to the
+    tabulated ones, the inverse round trip within 50 eps, and plan_fft's route
+    for non-smooth lengths."""
+    ct = np.complex64 if T == np.float32 else np.complex128
+    for n in HVDH_SIZES:
+        x, ref = _input(golden, n, 0x4D4)
+        x = x.astype(ct)
+        p = orc.PlanDirect(T, n, "hvdh", factors="table")
+        y = p(x)
+        assert rel_l2(y, ref) <= 50 * EPS[T], (n, rel_l2(y, ref) / EPS[T])
+        yf = orc.PlanDirect(T, n, "hvdh", factors="fly")(x)
+        assert np.array_equal(y, yf), n
+        pinv = orc.PlanDirect(T, n, "hvdh", direction="ifft")
+        assert rel_l2(pinv(y), x) <= 50 * EPS[T], n
+        if not _smooth13(n):
+            route = orc.Plan1D(T, n, "fft").route
+            if _use_hvdh(T, n) and not _use_composite(T, n):
+                assert route == "HvdhPlan", (n, route)
+            else:
+                assert route in ("ResamplePlan", "CompositePlan", "SplitPlan"), (n, route)
+
+
+def test_hvdh_no_coprime_t():
+    """runtests.jl:139: even multiples of 30 have no coprime smooth t."""
+    from oracle import oracle as O
+    for T in T_LIST:
+        with pytest.raises(ValueError, match="no coprime smooth t"):
+            O.PlanDirect(T, 390, "hvdh")
+
+
+def test_hvdh_bfft_20011(orc):
+    """runtests.jl:140-143: plan_bfft routes 20011 to HvdH, and bfft(fft(x))
+    = n x within 50 eps."""
+    for T in T_LIST:
+        ct = np.complex64 if T == np.float32 else np.complex128
+        rng = np.random.default_rng(0x4D4)
+        x = (rng.standard_normal(20011) + 1j * rng.standard_normal(20011)).astype(ct)
+        pb = orc.Plan1D(T, 20011, "bfft")
+        assert pb.route == "HvdhPlan"
+        assert rel_l2(pb(orc.Plan1D(T, 20011, "fft")(x)), 20011 * x.astype(np.complex128)) <= 50 * EPS[T]
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_composite_reference_sizes(orc, T):
+    """runtests.jl:146-170: plan_fft routes these to CompositePlan; within
+    100 eps of FFTW; ifft round trip and bfft = n x."""
+    ct = np.complex64 if T == np.float32 else np.complex128
+    ns = [n for n in COMPOSITE_SIZES if _use_composite(T, n)]
+    assert len(ns) >= 4
+    for n in ns:
+        rng = np.random.default_rng([0xC0B, n])
+        x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(ct)
+        ref = np.fft.fft(x.astype(np.complex128))
+        p = orc.Plan1D(T, n, "fft")
+        assert p.route == "CompositePlan", (n, p.route)
+        y = p(x)
+        assert rel_l2(y, ref) <= 100 * EPS[T], (n, rel_l2(y, ref) / EPS[T])
+        assert rel_l2(orc.Plan1D(T, n, "ifft")(y), x) <= 100 * EPS[T], n
+        assert rel_l2(orc.Plan1D(T, n, "bfft")(y), n * x.astype(np.complex128)) <= 100 * EPS[T], n
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_split_reference_sizes(orc, T):
+    """runtests.jl:84-107: FFTJ._split within 100 eps of FFTW; plan_fft takes
+    SplitPlan where _use_split holds; the inverse round trip."""
+    ct = np.complex64 if T == np.float32 else np.complex128
+    for n in SPLIT_SIZES:
+        rng = np.random.default_rng([0x5B1, n])
+        x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(ct)
+        ref = np.fft.fft(x.astype(np.complex128))
+        y = orc.PlanDirect(T, n, "split")(x)
+        assert rel_l2(y, ref) <= 100 * EPS[T], (n, rel_l2(y, ref) / EPS[T])
+        if _use_split(T, n):
+            assert orc.Plan1D(T, n, "fft").route == "SplitPlan", n
+        assert rel_l2(orc.PlanDirect(T, n, "split", direction="ifft")(y), x) <= 100 * EPS[T], n
