@@ -1019,12 +1019,10 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
                  std::vector<Op>* ops, int* route) {
   std::vector<int> primes;
   const bool smooth = smooth13(n, &primes);
-  // opts.route = 2 asks for Gaussian resampling: at full length (as
-  // FFTJ._hvdh, src/hvdh.jl:153-209, smooth lengths included) unless the
-  // length is even, non-smooth and taken by the split route. FFTJ throws
-  // ArgumentError when no smooth t is coprime to n (src/hvdh.jl:160-161).
-  if (g_sched.route == 2 && !g_tables.rs && n >= 2 &&
-      (smooth || n % 2 == 1 || !use_split(sizeof(T) == 8, n))) {
+  // opts.route = 3: Gaussian resampling at full length for any length, as
+  // FFTJ._hvdh (src/hvdh.jl:153-209) is built directly; FFTJ throws
+  // ArgumentError when no smooth t is coprime to n (src/hvdh.jl:160-161)
+  if (g_sched.route == 3 && !g_tables.rs && n >= 2) {
     Hvdh hv = hvdh_parts(n, sizeof(T) == 8, scale, batch);
     if (!hv.t) return fail(FFTJ_ERR_ARG, "no coprime smooth t for n = " + std::to_string(n));
     if (hv.ok) return build_c2c_hvdh<T>(P, hv, batch, idist, odist, dir, ops, route);

@@ -90,9 +90,9 @@ typedef struct {
   int32_t extra_passes;  /* HBM passes beyond the fewest that fit (0, 1, 2) */
   int32_t order;         /* k-th lexicographic permutation of the pass radices (0 = largest first) */
   int32_t tf_mult;       /* threads per transform column = the minimum x tf_mult (0/1 = minimum) */
-  int32_t route;         /* 0 planner; 1 oversampled resampling (non-smooth lengths); 2 Gaussian (HvdH)
-                            resampling, for any length as FFTJ._hvdh (even non-smooth lengths the split
-                            route takes excepted): FFTJ_ERR_ARG when no smooth t is coprime to n */
+  int32_t route;         /* non-smooth lengths: 0 planner, 1 resampling, 2 Gaussian (HvdH; even lengths
+                            by the split route); any length: 3 Gaussian resampling at full length, as
+                            FFTJ._hvdh (FFTJ_ERR_ARG when no smooth t is coprime to n) */
   int32_t threads_max;   /* cap on threads per CTA (0 = 512 F32 / 256 F64) */
   int32_t dry;           /* 1: plan the schedule only (no tables, no workspace, cannot execute) */
   int32_t precision;     /* F32 radix-16 sub-stages: 0 FP32 butterflies, 1 FP16 hi+lo tensor-core GEMM,

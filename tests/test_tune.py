@@ -48,8 +48,9 @@ def test_options_shape_the_schedule(T):
     assert info(T, "c2c", np.float64, 10007, route=1).route == 2   # forced resampling
     assert info(T, "c2c", np.float32, 10007).route == 2            # resampling by default (F32)
     assert info(T, "c2c", np.float32, 10007, route=2).route == 3   # forced HvdH
-    assert info(T, "c2c", np.float32, 10240, route=2).route == 3       # forced HvdH (as FFTJ._hvdh)
-    assert info(T, "c2c", np.float32, 10240, route=1).route in (0, 1)  # smooth: resampling knob ignored
+    assert info(T, "c2c", np.float32, 10240, route=2).route in (0, 1)  # smooth: knob ignored
+    assert info(T, "c2c", np.float32, 10240, route=3).route == 3       # full-length HvdH, as FFTJ._hvdh
+    assert info(T, "c2c", np.float64, 2 * 10007, route=3).route == 3
 
 
 def test_candidates_are_distinct_and_start_with_default(T):
