@@ -261,7 +261,9 @@ int build_persistent(fftj_group_s* g) {
                        "persistent group: ComplexF64 plans with FP64 butterflies (opts.f64_arith = 1) run "
                        "outside persistent groups");
         const size_t esz = go.f64 ? 16 : 8;
-        g->smem = std::max(g->smem, (size_t)op.pp.smem_elems * esz + (size_t)op.pp.fx_cols * sizeof(int));
+        // passes run the run-time-radix body, which ping-pongs between two
+        // tile buffers
+        g->smem = std::max(g->smem, 2 * (size_t)op.pp.smem_elems * esz + (size_t)op.pp.fx_cols * sizeof(int));
       }
       g->h_ops.push_back(go);
     }

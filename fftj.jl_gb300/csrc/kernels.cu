@@ -78,10 +78,11 @@ static const void* generic_pass(const PassParams& pp, int dir) {
   }
   return (const void*)pass_fn<T>(dir, pp.load_op);
 }
-// dynamic shared memory of a pass: the tile, staged twiddles and (block
+// dynamic shared memory of a pass: the tile (two tile buffers for the
+// generic kernel, which ping-pongs between them), staged twiddles and (block
 // fixed point) the column exponents
-static size_t pass_smem(const PassParams& pp, size_t esz) {
-  return (size_t)(pp.smem_elems + pp.smem_tw_elems) * esz + (size_t)pp.fx_cols * sizeof(int);
+static size_t pass_smem(const PassParams& pp, size_t esz, bool generic) {
+  return (size_t)((generic ? 2 : 1) * pp.smem_elems + pp.smem_tw_elems) * esz + (size_t)pp.fx_cols * sizeof(int);
 }
 
 // Opt a pass kernel into the device's largest dynamic shared memory. The
@@ -101,7 +102,7 @@ cudaError_t prepare_pass(const PassParams& pp, int dir, const void* fn) {
   e = cudaFuncGetAttributes(&fa, f);
   if (e != cudaSuccess) return e;
   const int maxdyn = optin - (int)fa.sharedSizeBytes;
-  const size_t need = pass_smem(pp, sizeof(Cx<T>));
+  const size_t need = pass_smem(pp, sizeof(Cx<T>), fn == nullptr);
   if (maxdyn <= 0 || need > (size_t)maxdyn) return cudaErrorInvalidValue;
   return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn);
 }
@@ -109,7 +110,7 @@ cudaError_t prepare_pass(const PassParams& pp, int dir, const void* fn) {
 template <typename T>
 cudaError_t launch_pass(const PassParams& pp, int dir, const void* fn, const void* in, void* out,
                         cudaStream_t st) {
-  const size_t smem = pass_smem(pp, sizeof(Cx<T>));
+  const size_t smem = pass_smem(pp, sizeof(Cx<T>), fn == nullptr);
   const uint32_t grid = pp.tiles_q * pp.tiles_p * pp.tiles_b;
   const void* f = fn ? fn : generic_pass<T>(pp, dir);
   void* args[3] = {const_cast<PassParams*>(&pp), const_cast<void**>(&in), &out};

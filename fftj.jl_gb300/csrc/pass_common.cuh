@@ -337,53 +337,46 @@ template <typename T, int DIR>
 struct Dft<T, DIR, 13> { __device__ __forceinline__ static void run(Cx<T>* v) { DftPrime<T, DIR, 13>::run(v); } };
 
 // ---------------------------------------------------------------------------
-// One radix-r Stockham sub-stage on all NB columns of the tile, in place.
-// Element j of sub-butterfly k (= p*S + q) is read at position k + j*R/r and
-// written at r*S*p + j*S + q, twiddled by w_L^(p*j) = w_R^(p*j*S). Thread
-// (b, kg) owns column b and butterflies k = kg + i*Tf; it loads all of them
-// into registers before the barrier, so one shared buffer suffices. The host
-// sizes Tf so that no thread holds more than max(1, 16/r) butterflies.
+// One radix-r sub-stage of the run-time-radix pass between two shared
+// buffers: the maps of substage<> (butterfly k = p S + q of column b reads
+// k + j Rr, writes r S p + j S + q, twiddled by w_R^(p j S)), from src to
+// dst. With the input and output apart, a thread runs its butterflies one
+// at a time in a loop that is not unrolled: registers for r elements, and a
+// small body per radix (no calls, no spills).
 template <typename T, int DIR, int r>
-__device__ __noinline__ void substage(Cx<T>* __restrict__ buf, const int b, const int kg, const int Tf,
-                                         const int NB, const int Rr, const int S, const FastDiv fS,
-                                         const Cx<T>* __restrict__ twR, const int sh = 0) {
-  constexpr int IPT = (16 / r) > 0 ? (16 / r) : 1;
+__device__ __forceinline__ void substage_pp(const Cx<T>* __restrict__ src, Cx<T>* __restrict__ dst, const int b,
+                                            const int kg, const int Tf, const int NB, const int Rr, const int S,
+                                            const FastDiv fS, const Cx<T>* __restrict__ twR, const int sh,
+                                            const bool raw = false, const int cin = 0) {
   const int jstride_in = Rr * NB;
   const int jstride_out = S * NB;
-  Cx<T> v[IPT][r];
+#pragma unroll 1
+  for (int k = kg; k < Rr; k += Tf) {
+    Cx<T> v[r];
+    const int a = k * NB + b;
+    if (kFx<T> && raw) {
+      // first sub-stage of an Fx pass: the buffer holds the raw FP64 inputs
+      // of column b, converted here with the column's scale
+      const Cx<Hs<T>>* rs = reinterpret_cast<const Cx<Hs<T>>*>(src);
 #pragma unroll
-  for (int i = 0; i < IPT; ++i) {
-    const int k = kg + i * Tf;
-    if (k < Rr) {
-      const int a = k * NB + b;
+      for (int j = 0; j < r; ++j) v[j] = to_c<T>(rs[pidx<T>(a + j * jstride_in)], cin);
+    } else {
 #pragma unroll
-      for (int j = 0; j < r; ++j) v[i][j] = buf[pidx<T>(a + j * jstride_in)];
+      for (int j = 0; j < r; ++j) v[j] = src[pidx<T>(a + j * jstride_in)];
+    }
+    const int p = (int)fS.div((uint32_t)k);
+    const int q = k - p * S;
+    Dft<T, DIR, r>::run(v);
+    const int ao = (r * S * p + q) * NB + b;
+    dst[pidx<T>(ao)] = shr_c<T>(v[0], sh);
+    const int tstep = p * S;
+#pragma unroll
+    for (int j = 1; j < r; ++j) {
+      Cx<T> w = v[j];
+      if (p != 0) w = cmul(w, ldt<T>(&twR[j * tstep]));
+      dst[pidx<T>(ao + j * jstride_out)] = shr_c<T>(w, sh);
     }
   }
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < IPT; ++i) {
-    const int k = kg + i * Tf;
-    if (k < Rr) {
-      const int p = (int)fS.div((uint32_t)k);
-      const int q = k - p * S;
-      Dft<T, DIR, r>::run(v[i]);
-      const int a = (r * S * p + q) * NB + b;
-      buf[pidx<T>(a)] = shr_c<T>(v[i][0], sh);
-      if (p == 0) {
-#pragma unroll
-        for (int j = 1; j < r; ++j) buf[pidx<T>(a + j * jstride_out)] = shr_c<T>(v[i][j], sh);
-      } else {
-        const int tstep = p * S;
-#pragma unroll
-        for (int j = 1; j < r; ++j) {
-          const Cx<T> w = ldt<T>(&twR[j * tstep]);
-          buf[pidx<T>(a + j * jstride_out)] = shr_c<T>(cmul(v[i][j], w), sh);
-        }
-      }
-    }
-  }
-  __syncthreads();
 }
 
 // LOADOP = LOAD_RUNTIME reads the load op from pp (one code path for all;
@@ -813,9 +806,18 @@ __device__ __noinline__ void substage_tc16(float2* __restrict__ buf, const int t
 }
 
 // ---------------------------------------------------------------------------
-// One Stockham pass over one tile (the kernel comment in kernels.cu gives
-// the maps). Rec is RuntimeRecipe (radix sequence read from pp.sub) or a
-// Recipe<r...> fixed at compile time.
+// One Stockham pass over one tile with the radix sequence read at run time
+// from pp.sub: the generic kernel (k_pass) and the persistent group kernel.
+// Compile-time recipes run pass_fused. The maps are those of the kernel
+// comment in kernels.cu.
+//
+// The tile ping-pongs between two shared buffers. Loads stream into the
+// first buffer -- for Fx passes the raw FP64 values, converted when the
+// first sub-stage reads them, once every column's exponent maximum is
+// known; every sub-stage reads one buffer and writes the other, one
+// butterfly at a time; the store streams the result out with the outer
+// twiddle and the scale. No phase keeps more than a few elements per thread
+// in registers.
 //
 // pass_tile runs tile `tile` with threads [0, nthr) of the CTA doing the
 // work. GROUP (the persistent group kernel): the CTA may have more threads
@@ -825,23 +827,23 @@ template <typename T, int DIR, int LOADOP, class Rec, bool GROUP>
 __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __restrict__ in,
                                           Cx<Hs<T>>* __restrict__ out, const uint32_t tile, const int tid,
                                           const int nthr) {
+  static_assert(!Rec::kConst, "compile-time recipes run pass_fused");
+  using H = Hs<T>;
+  static_assert(sizeof(Cx<H>) == sizeof(Cx<T>), "raw and compute elements share the tile layout");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  Cx<T>* buf = reinterpret_cast<Cx<T>*>(smem_raw);
-  // Fx passes: exponent maximum of each tile column, after the tile
-  int* const colE = reinterpret_cast<int*>(buf + pp.smem_elems);
-  constexpr int EPT = Rec::kConst ? (Rec::R + Rec::Tf - 1) / Rec::Tf : 16;
+  Cx<T>* const bufA = reinterpret_cast<Cx<T>*>(smem_raw);
+  Cx<T>* const bufB = bufA + pp.smem_elems;
+  int* const colE = reinterpret_cast<int*>(bufA + 2 * pp.smem_elems);
   const bool active = !GROUP || tid < nthr;
   const uint32_t t1 = pp.ftq.div(tile);
   const uint32_t tq = tile - t1 * pp.tiles_q;
   const uint32_t tb = pp.ftp.div(t1);
   const uint32_t tp = t1 - tb * pp.tiles_p;
   const int64_t q0 = (int64_t)tq * pp.Q, p0 = (int64_t)tp * pp.P, b0 = (int64_t)tb * pp.NBt;
-  const int R = Rec::kConst ? Rec::R : pp.R;
-  const int Tf = Rec::kConst ? Rec::Tf : pp.Tf;
+  const int R = pp.R, Tf = pp.Tf;
   const int P = pp.P, Q = pp.Q, NB = pp.NB;
   const int E = active ? NB * R : 0;  // idle threads own no elements
   const int64_t ms = pp.m * pp.s;
-
   // this thread's column b = (bt, pl, ql) and first butterfly row kg (idle
   // threads get a row beyond every sub-stage, so they own no butterflies)
   const int kg = active ? (int)pp.fNB.div((uint32_t)tid) : (1 << 29);
@@ -852,164 +854,124 @@ __device__ __forceinline__ void pass_tile(const PassParams& pp, const void* __re
   const int pl = cq - cbt * P;
   const int64_t batch = b0 + cbt;
   const int64_t pcol = p0 + pl;
+  const int B = pp.fx_b0;
+  Cx<H>* const rawA = reinterpret_cast<Cx<H>*>(bufA);
 
-  // ---- load: HBM -> shared. All of a thread's loads are issued before its
-  // first shared store; indices are recomputed rather than kept in registers.
-  // Fx: the column's exponent maximum is taken between loads and stores.
-  using H = Hs<T>;
+  // ---- load: HBM -> first buffer, element by element
   if constexpr (kFx<T>) {
     if (tid < NB) colE[tid] = 1;
     __syncthreads();
   }
-  const int B = pp.fx_b0;
-  {
-    Cx<H> v[EPT];
-    if (pp.load_rows) {
-      // transforms contiguous along j (one pass over whole transforms)
-#pragma unroll
-      for (int i = 0; i < EPT; ++i) {
-        const int e = tid + i * nthr;
-        if (e < E) {
-          const int c = Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e);
-          const int64_t bb = b0 + c;
-          v[i] = bb < pp.nbatch ? load_elem<H, LOADOP, GROUP>(pp, in, bb, e - c * R) : mk<H>(0, 0);
-        }
-      }
-      if constexpr (kFx<T>) {
-#pragma unroll
-        for (int i = 0; i < EPT; ++i) {
-          const int e = tid + i * nthr;
-          if (e < E) col_expo_max(colE, Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e), hexpo<T>(v[i]));
-        }
-        __syncthreads();
-      }
-#pragma unroll
-      for (int i = 0; i < EPT; ++i) {
-        const int e = tid + i * nthr;
-        if (e < E) {
-          const int c = Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e);
-          const int cin = kFx<T> ? 53 - B + colE[c] : 0;
-          buf[pidx<T>((e - c * R) * NB + c)] = to_c<T>(v[i], cin);
-        }
-      }
-    } else {
-      // lanes walk the tile's columns (contiguous p or q runs)
-      const int64_t gcol = pp.s * pcol + q0 + ql;
-      const bool ok = batch < pp.nbatch && q0 + ql < pp.s;  // ragged lane tiles
-#pragma unroll
-      for (int i = 0; i < EPT; ++i) {
-        const int j = kg + i * Tf;
-        if (j < R) v[i] = ok ? load_elem<H, LOADOP, GROUP>(pp, in, batch, gcol + (int64_t)j * ms) : mk<H>(0, 0);
-      }
-      int cin = 0;
-      if constexpr (kFx<T>) {
-        int em = 1;
-#pragma unroll
-        for (int i = 0; i < EPT; ++i) {
-          const int j = kg + i * Tf;
-          if (j < R) em = max(em, hexpo<T>(v[i]));
-        }
-        if (active) atomicMax(colE + b, em);
-        __syncthreads();
-        cin = 53 - B + colE[b];
-      }
-#pragma unroll
-      for (int i = 0; i < EPT; ++i) {
-        const int j = kg + i * Tf;
-        if (j < R) buf[pidx<T>(j * NB + b)] = to_c<T>(v[i], cin);
-      }
+  if (pp.load_rows) {
+    // transforms contiguous along j (one pass over whole transforms)
+#pragma unroll 4
+    for (int e = tid; e < E; e += nthr) {
+      const int c = (int)pp.fR.div((uint32_t)e);
+      const int j = e - c * R;
+      const int64_t bb = b0 + c;
+      const Cx<H> v = bb < pp.nbatch ? load_elem<H, LOADOP, GROUP>(pp, in, bb, j) : mk<H>(0, 0);
+      if constexpr (kFx<T>) col_expo_max(colE, c, hexpo<T>(v));
+      rawA[pidx<T>(j * NB + c)] = v;
+    }
+  } else {
+    // lanes walk the tile's columns (contiguous p or q runs)
+    const int64_t gcol = pp.s * pcol + q0 + ql;
+    const bool ok = batch < pp.nbatch && q0 + ql < pp.s;  // ragged lane tiles
+    int em = 1;
+#pragma unroll 4
+    for (int j = kg; j < R; j += Tf) {
+      const Cx<H> v = ok ? load_elem<H, LOADOP, GROUP>(pp, in, batch, gcol + (int64_t)j * ms) : mk<H>(0, 0);
+      if constexpr (kFx<T>) em = max(em, hexpo<T>(v));
+      rawA[pidx<T>(j * NB + b)] = v;
+    }
+    if constexpr (kFx<T>) {
+      if (active) atomicMax(colE + b, em);
     }
   }
   __syncthreads();
 
-  // ---- the pass's R-point DFTs: radix sub-stages in shared memory
+  // ---- the pass's R-point DFTs: radix sub-stages between the buffers
   const Cx<T>* twR = reinterpret_cast<const Cx<T>*>(pp.twR);
-  if constexpr (Rec::kConst) {
-    run_recipe<T, DIR>((Rec*)nullptr, buf, b, kg, NB, twR);
-  } else {
+  const int cinb = kFx<T> ? 53 - B + colE[b] : 0;  // this thread's column, first sub-stage
+  Cx<T>* cur = bufA;
+  Cx<T>* nxt = bufB;
+  bool raw = kFx<T>;  // cur holds unconverted FP64 values
 #pragma unroll 1
-    for (int si = 0; si < pp.nsub; ++si) {
-      const SubStage& ss = pp.sub[si];
-      const int sh = kFx<T> && si + 1 < pp.nsub ? fx_l(pp.sub[si + 1].r) : 0;
-      switch (ss.r) {
-        case 2: substage<T, DIR, 2>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
-        case 3: substage<T, DIR, 3>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
-        case 4: substage<T, DIR, 4>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
-        case 5: substage<T, DIR, 5>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
-        case 7: substage<T, DIR, 7>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
-        case 8: substage<T, DIR, 8>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
-        case 11: substage<T, DIR, 11>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
-        case 13: substage<T, DIR, 13>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh); break;
-        case 16:
-          if constexpr (sizeof(T) == 4) {
-            if (pp.tc && tc16_fits(nthr, NB, ss.Rr)) {
-              if (pp.tc == 1)
-                substage_tc16<DIR, 1>(buf, tid, nthr, NB, ss.Rr, ss.S, ss.fS, pp.fNB, twR);
-              else
-                substage_tc16<DIR, 2>(buf, tid, nthr, NB, ss.Rr, ss.S, ss.fS, pp.fNB, twR);
-              break;
-            }
+  for (int si = 0; si < pp.nsub; ++si) {
+    const SubStage& ss = pp.sub[si];
+    const int sh = kFx<T> && si + 1 < pp.nsub ? fx_l(pp.sub[si + 1].r) : 0;
+    bool moved = true;
+    switch (ss.r) {
+      case 2: substage_pp<T, DIR, 2>(cur, nxt, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh, raw, cinb); break;
+      case 3: substage_pp<T, DIR, 3>(cur, nxt, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh, raw, cinb); break;
+      case 4: substage_pp<T, DIR, 4>(cur, nxt, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh, raw, cinb); break;
+      case 5: substage_pp<T, DIR, 5>(cur, nxt, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh, raw, cinb); break;
+      case 7: substage_pp<T, DIR, 7>(cur, nxt, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh, raw, cinb); break;
+      case 8: substage_pp<T, DIR, 8>(cur, nxt, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh, raw, cinb); break;
+      case 11: substage_pp<T, DIR, 11>(cur, nxt, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh, raw, cinb); break;
+      case 13: substage_pp<T, DIR, 13>(cur, nxt, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh, raw, cinb); break;
+      case 16:
+        if constexpr (sizeof(T) == 4) {
+          if (pp.tc && tc16_fits(nthr, NB, ss.Rr)) {
+            // tensor-core sub-stage: in place on the current buffer
+            if (pp.tc == 1)
+              substage_tc16<DIR, 1>(cur, tid, nthr, NB, ss.Rr, ss.S, ss.fS, pp.fNB, twR);
+            else
+              substage_tc16<DIR, 2>(cur, tid, nthr, NB, ss.Rr, ss.S, ss.fS, pp.fNB, twR);
+            moved = false;
+            break;
           }
-          substage<T, DIR, 16>(buf, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh);
-          break;
-        default: break;
-      }
+        }
+        substage_pp<T, DIR, 16>(cur, nxt, b, kg, Tf, NB, ss.Rr, ss.S, ss.fS, twR, sh, raw, cinb);
+        break;
+      default: break;
+    }
+    __syncthreads();
+    raw = false;
+    if (moved) {
+      Cx<T>* t = cur;
+      cur = nxt;
+      nxt = t;
     }
   }
 
-  // ---- store: shared -> HBM with the outer twiddle w_ncur^(p*j) and scale.
-  // The twiddle loads of all of a thread's elements are issued first.
+  // ---- store: shared -> HBM with the outer twiddle w_ncur^(p*j) and scale
   const OutConv<T> oc(pp);
   const bool tw = pp.tw_mode != 0;
-  Cx<T> w[EPT];
+  const Cx<H>* const rawc = reinterpret_cast<const Cx<H>*>(cur);
+  // element at a padded position of column col (a pass without sub-stages
+  // still holds the raw Fx inputs)
+  auto elem = [&](int idx, int col) -> Cx<T> {
+    if constexpr (kFx<T>) {
+      if (raw) return to_c<T>(rawc[idx], 53 - B + colE[col]);
+    }
+    return cur[idx];
+  };
   if (pp.store_rows) {
     // outputs contiguous along j (s == 1): lanes walk j
-#pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      const int e = tid + i * nthr;
-      w[i] = mk<T>(1, 0);
-      if (e < E && tw) {
-        const int c = Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e);
-        const int j = e - c * R;
-        const int cbt2 = (int)pp.fP.div((uint32_t)c);
+#pragma unroll 4
+    for (int e = tid; e < E; e += nthr) {
+      const int c = (int)pp.fR.div((uint32_t)e);
+      const int j = e - c * R;
+      const int cbt2 = (int)pp.fP.div((uint32_t)c);
+      const int64_t bb = b0 + cbt2;
+      if (bb < pp.nbatch) {
         const int64_t p = p0 + (c - cbt2 * P);
-        if (p * j != 0) w[i] = outer_tw<T>(pp, p * (int64_t)j);
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      const int e = tid + i * nthr;
-      if (e < E) {
-        const int c = Rec::kConst ? e / Rec::R : (int)pp.fR.div((uint32_t)e);
-        const int j = e - c * R;
-        const int cbt2 = (int)pp.fP.div((uint32_t)c);
-        const int64_t bb = b0 + cbt2;
-        if (bb < pp.nbatch) {
-          Cx<T> v = buf[pidx<T>(j * NB + c)];
-          if (tw) v = cmul(v, w[i]);
-          out[bb * pp.out_bstride + (int64_t)R * (p0 + (c - cbt2 * P)) + j] = oc(v, kFx<T> ? colE[c] : 0);
-        }
+        Cx<T> v = elem(pidx<T>(j * NB + c), c);
+        if (tw && p * j != 0) v = cmul(v, outer_tw<T>(pp, p * (int64_t)j));
+        out[bb * pp.out_bstride + (int64_t)R * p + j] = oc(v, kFx<T> ? colE[c] : 0);
       }
     }
   } else {
     const bool ok = batch < pp.nbatch && q0 + ql < pp.s;
-#pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      const int j = kg + i * Tf;
-      w[i] = mk<T>(1, 0);
-      if (j < R && tw && pcol * j != 0) w[i] = outer_tw<T>(pp, pcol * (int64_t)j);
-    }
     if (ok) {
       Cx<H>* ob = out + batch * pp.out_bstride + (int64_t)R * pp.s * pcol + q0 + ql;
       const int Eb = kFx<T> ? colE[b] : 0;
-#pragma unroll
-      for (int i = 0; i < EPT; ++i) {
-        const int j = kg + i * Tf;
-        if (j < R) {
-          Cx<T> v = buf[pidx<T>(j * NB + b)];
-          if (tw) v = cmul(v, w[i]);
-          ob[(int64_t)j * pp.s] = oc(v, Eb);
-        }
+#pragma unroll 4
+      for (int j = kg; j < R; j += Tf) {
+        Cx<T> v = elem(pidx<T>(j * NB + b), b);
+        if (tw && pcol * j != 0) v = cmul(v, outer_tw<T>(pp, pcol * (int64_t)j));
+        ob[(int64_t)j * pp.s] = oc(v, Eb);
       }
     }
   }

@@ -440,8 +440,12 @@ thread_local SchedOpts g_sched;
 
 DtypeCfg dtype_cfg(bool f64) {
   // F32: 4096-element tiles (35 KB) give 4 CTAs of 256 threads per SM,
-  // measured faster than 8192-element tiles at 2 CTAs per SM
-  DtypeCfg c = f64 ? DtypeCfg{16, env_int("FFTJ_TILE_F64", 4096), 4096, 256, 1024, 4}
+  // measured faster than 8192-element tiles at 2 CTAs per SM. F64: tiles of
+  // at most 2048 elements (37 KB) and multi-pass radices of at most 512
+  // (>= 4 columns, 64-byte runs, per tile), so that the run-time-radix body's
+  // two tile buffers leave two CTAs per SM, in the persistent group kernel
+  // too
+  DtypeCfg c = f64 ? DtypeCfg{16, env_int("FFTJ_TILE_F64", 2048), 2048, 256, 512, 4}
                    : DtypeCfg{8, env_int("FFTJ_TILE_F32", 4096), 8192, 512, 1024, env_int("FFTJ_MIN_RUN_F32", 8)};
   if (g_sched.tile > 0) c.tile_max = std::min(std::max(g_sched.tile, 256), c.tile_cap);
   if (g_sched.threads_max > 0) c.threads_max = std::min(c.threads_max, std::max(g_sched.threads_max, 64));
