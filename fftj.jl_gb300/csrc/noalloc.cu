@@ -88,7 +88,7 @@ static int run_noalloc(int64_t n, int64_t batch, int dir, double scale, const vo
   int64_t Rs[2];
   const int npass = pass_radices(n, f64, false, Rs, 2);
   if (npass < 1 || npass > 2) {
-    set_error("fftj_execute_noalloc_c2c: n must be 13-smooth and run in one or two passes (n <= 2^20)");
+    set_error("fftj_execute_noalloc_c2c: n must be 13-smooth and run in one or two passes (n <= 2^20 F32, 2^18 F64)");
     return FFTJ_ERR_UNSUPPORTED;
   }
   const size_t data_bytes = (size_t)n * (size_t)batch * sizeof(C);

@@ -1550,6 +1550,19 @@ int finalize_passes(fftj_plan_s* P) {
     // kernel; passes without a radix-16 sub-stage keep their recipe kernel
     if (op.pp.tc && !has_tc16_substage(op.pp)) op.pp.tc = 0;
     op.kfn = op.pp.tc ? nullptr : pick_pass_kernel(sizeof(T) == 8, op.dir, op.pp);
+    if (!op.kfn && !op.pp.tc) {
+      // the run-time-radix body loops over a column's butterflies and
+      // elements with any number of threads per column: fill the CTA up to
+      // the thread cap (no idle warps in the persistent group's 256-thread
+      // CTAs, more warps in the pass's own launch)
+      const int tmax = dtype_cfg(sizeof(T) == 8).threads_max;
+      const int tf = std::min(std::max(op.pp.Tf, tmax / std::max(op.pp.NB, 1)), op.pp.R);
+      if (tf > op.pp.Tf) {
+        op.pp.Tf = tf;
+        op.pp.threads = op.pp.NB * tf;
+        op.pp.ept = (op.pp.R + tf - 1) / tf;
+      }
+    }
     op.pp.smem_tw_elems = stage_inner_twiddles(op.pp, op.kfn != nullptr) ? op.pp.R : 0;
     if (sizeof(T) == 4 && op.kfn && !op.pp.tc && !P->plain_loads) pick_tma(op, P->dry);
     any_tma = any_tma || op.kfn_tma != nullptr;

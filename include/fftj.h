@@ -287,7 +287,7 @@ const char* fftj_version(void);
  * file-scope static device array of 64 MiB (1 MiB of twiddle tables,
  * regenerated on the device on every call, and 63 MiB for the intermediate
  * of a two-pass transform) that every GPU loading the library holds until
- * exit. Limits: n 13-smooth and done in one or two passes (n <= 2^20), and
+ * exit. Limits: n 13-smooth and done in one or two passes (n <= 2^20 F32, 2^18 F64), and
  * for two passes batch * n * sizeof(complex) <= 63 MiB; larger requests
  * return FFTJ_ERR_ARG / FFTJ_ERR_UNSUPPORTED with a message. d_in/d_out hold
  * batch dense transforms; in == out is allowed. The first call on a device
