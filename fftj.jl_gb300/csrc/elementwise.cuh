@@ -42,6 +42,130 @@ __device__ __forceinline__ void interp_at(const InterpParams& ip, const Cx<T>* _
 // .. q0+R-1 of the length-t transform, cyclic), keeping z in a strided
 // scratch, then back substitution, writing the core rows' unknowns to their
 // permuted outputs, scaled by scale * n / t.
+// HvdH banded solve with its factors rebuilt per call (FFTJ factors = :fly,
+// src/hvdh.jl:500-602): thread (b, c) walks its chunk's R rows; column j's
+// state e_j = 2 t l' - 2 n q_j + n (an unknown sits at row q_j when
+// e_j < 2n, offset beta' = (e_j - n)/2n; the next column's state is e + 2
+// Delta on an unknown, e - 2n off one) gives row i's band entries
+// exp(-a (k + beta'_{i+k})^2), |k| <= B, columns outside [0, R) dropped as
+// in the tabulated factors; rows are eliminated without pivoting as they are
+// built, their U rows and output indices kept in per-thread scratch for the
+// back pass. Same mathematics as the tabulated solve (solve_at), FP64 exp
+// per column instead of a table read per row: on GB300 (slow FP64, fast
+// HBM) the tables are faster, so they are the default up to a size cap.
+template <typename T, int B, bool CG>
+__device__ __forceinline__ void solve_fly_at(const SolveParams& sp, const Cx<T>* __restrict__ g,
+                                             Cx<T>* __restrict__ y, const int64_t tid) {
+  const int64_t nt = sp.nbatch * sp.nchunk;
+  if (tid >= nt) return;
+  const int64_t b = tid / sp.nchunk, ch = tid - b * sp.nchunk;
+  const int R = (int)sp.R, H = (int)sp.H, L = (int)sp.L;
+  const int t = (int)sp.t;
+  const int64_t n = sp.n, d2 = 2 * sp.delta, n2 = 2 * n;
+  const double a = sp.a, inv2n = 1.0 / (double)n2;
+  constexpr int W = 2 * B + 1;
+  // column window: columns i - B .. i + B of row i (relative to the chunk)
+  int64_t e = sp.se[ch];
+  double beta[W];
+  bool hit[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    hit[w] = e < n2;
+    beta[w] = (double)(e - n) * inv2n;
+    e = hit[w] ? e + d2 : e - n2;
+  }
+  int64_t on = sp.so[ch];
+  Cx<T>* zwp = reinterpret_cast<Cx<T>*>(sp.zw) + tid;
+  T* uwp = reinterpret_cast<T*>(sp.uw) + tid;
+  int32_t* owp = sp.ow + tid;
+  const Cx<T>* gb = g + b * sp.g_bstride;
+  int q = (int)((((int64_t)ch * L - H) % t + t) % t);
+  T up[B][B + 1];  // U rows i-1 .. i-B: 1/U_jj, U_{j,j+1..j+B}
+#pragma unroll
+  for (int k = 0; k < B; ++k) {
+    up[k][0] = (T)1;
+#pragma unroll
+    for (int j = 1; j <= B; ++j) up[k][j] = (T)0;
+  }
+  Cx<T> zp[B];
+#pragma unroll
+  for (int k = 0; k < B; ++k) zp[k] = mk<T>(0, 0);
+  for (int i = 0; i < R; ++i) {
+    // row i's band: r[k + B] = entry at column i + k
+    T r[W];
+    const bool hi = hit[B];
+#pragma unroll
+    for (int k = -B; k <= B; ++k) {
+      const int j = i + k;
+      const double dd = (double)k + beta[k + B];
+      r[k + B] = (hi && hit[k + B] && j >= 0 && j < R) ? (T)exp(-a * dd * dd) : (T)0;
+    }
+    if (!hi) r[B] = (T)1;  // identity row
+    // eliminate columns i-B .. i-1 against the previous U rows
+    Cx<T> z = mk<T>(0, 0);
+    if (hi) z = ldd<CG>(gb + q);
+#pragma unroll
+    for (int k = B; k >= 1; --k) {
+      const T f = r[B - k] * up[k - 1][0];
+#pragma unroll
+      for (int j = 1; j <= B; ++j) r[B - k + j] = fma(-f, up[k - 1][j], r[B - k + j]);
+      z.x = fma(-f, zp[k - 1].x, z.x);
+      z.y = fma(-f, zp[k - 1].y, z.y);
+    }
+#pragma unroll
+    for (int k = B - 1; k > 0; --k) {
+      zp[k] = zp[k - 1];
+#pragma unroll
+      for (int j = 0; j <= B; ++j) up[k][j] = up[k - 1][j];
+    }
+    zp[0] = z;
+    up[0][0] = (T)1 / r[B];
+#pragma unroll
+    for (int j = 1; j <= B; ++j) up[0][j] = r[B + j];
+    zwp[(int64_t)i * nt] = z;
+#pragma unroll
+    for (int j = 0; j <= B; ++j) uwp[((int64_t)i * (B + 1) + j) * nt] = up[0][j];
+    owp[(int64_t)i * nt] = hi ? (int32_t)on : -1;
+    if (hi) { on += sp.delta; if (on >= n) on -= n; }
+    // slide the column window by one
+#pragma unroll
+    for (int w = 0; w < W - 1; ++w) { hit[w] = hit[w + 1]; beta[w] = beta[w + 1]; }
+    hit[W - 1] = e < n2;
+    beta[W - 1] = (double)(e - n) * inv2n;
+    e = hit[W - 1] ? e + d2 : e - n2;
+    if (++q >= t) q -= t;
+  }
+  // back substitution from row R-1 down to H
+  Cx<T> xp[B];
+#pragma unroll
+  for (int k = 0; k < B; ++k) xp[k] = mk<T>(0, 0);
+  const T sc = (T)sp.sc;
+  Cx<T>* yb = y + b * sp.y_bstride;
+  const Cx<T>* twb = sp.tw ? reinterpret_cast<const Cx<T>*>(sp.tw) : nullptr;
+  const int64_t twr = sp.tw ? (b % sp.tw_s) : 0;
+  for (int i = R - 1; i >= H; --i) {
+    Cx<T> x = zwp[(int64_t)i * nt];
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const T u = uwp[((int64_t)i * (B + 1) + 1 + j) * nt];
+      x.x = fma(-u, xp[j].x, x.x);
+      x.y = fma(-u, xp[j].y, x.y);
+    }
+    const T iu = uwp[(int64_t)i * (B + 1) * nt];
+    x.x *= iu;
+    x.y *= iu;
+#pragma unroll
+    for (int k = B - 1; k > 0; --k) xp[k] = xp[k - 1];
+    xp[0] = x;
+    const int32_t o = owp[(int64_t)i * nt];
+    if (i < H + L && o >= 0) {
+      Cx<T> v = mk<T>(x.x * sc, x.y * sc);
+      if (twb) v = cmul(v, __ldg(twb + twr * o));
+      yb[o] = v;
+    }
+  }
+}
+
 template <typename T, int B, bool CG>
 __device__ __forceinline__ void solve_at(const SolveParams& sp, const Cx<T>* __restrict__ g,
                                          Cx<T>* __restrict__ y, const int64_t tid) {

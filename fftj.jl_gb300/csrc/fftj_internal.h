@@ -114,6 +114,16 @@ struct SolveParams {
   void* zw;                  // R * nbatch * nchunk forward-substitution scratch
   const void* tw;            // split route: w_(tw_s * n)^(r * o) applied to output o of sub-transform b,
   int64_t tw_s;              //   r = b mod tw_s (nullptr: none)
+  // factors rebuilt in the solve (FFTJ factors = :fly) instead of read from
+  // lf/uf/oi: per chunk the column state e = 2 t l' - 2 n q + n at its first
+  // column (q = q0 - B) and the output index Delta l' mod n of its first row
+  int fly;
+  double a;                  // Gaussian exponent a = pi alpha^2
+  int64_t delta;             // t - n
+  const int64_t* se;         // nchunk: column state at column -B
+  const int64_t* so;         // nchunk: output index of the first unknown at or after row 0
+  void* uw;                  // R * (B + 1) * nbatch * nchunk: U rows of each thread's chunk
+  int32_t* ow;               // R * nbatch * nchunk: output index of each row (-1: identity row)
 };
 
 // Resampling interpolation: y[b*ody + k] = sum_i wt[k*w+i] g[b*m + (l0[k]+i) mod m]
@@ -192,6 +202,7 @@ struct SchedOpts {
   int precision = 0;
   int plain_loads = 0;
   int f64_arith = 0;
+  int hvdh_factors = 0;
   bool dry = false;
 };
 extern thread_local SchedOpts g_sched;

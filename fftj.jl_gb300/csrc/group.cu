@@ -92,7 +92,11 @@ __device__ __noinline__ void group_elementwise(const GroupOp& op, uint32_t t0, u
       case OP_RPOST: real_post_at<T, true>(op.rp, src, dst, idx); break;
       case OP_COPY: copy_at<T, true>(op.cp, op.src, op.dst, idx); break;
       case OP_SOLVE:
-        if (op.B == 1) solve_at<T, 1, true>(op.sv, src, dst, idx);
+        if (op.sv.fly) {
+          if (op.B == 1) solve_fly_at<T, 1, true>(op.sv, src, dst, idx);
+          else if (op.B == 2) solve_fly_at<T, 2, true>(op.sv, src, dst, idx);
+          else solve_fly_at<T, 3, true>(op.sv, src, dst, idx);
+        } else if (op.B == 1) solve_at<T, 1, true>(op.sv, src, dst, idx);
         else if (op.B == 2) solve_at<T, 2, true>(op.sv, src, dst, idx);
         else solve_at<T, 3, true>(op.sv, src, dst, idx);
         break;

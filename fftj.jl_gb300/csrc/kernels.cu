@@ -32,7 +32,8 @@ __global__ void k_interp(const __grid_constant__ InterpParams ip, const Cx<T>* _
 template <typename T, int B>
 __global__ void k_hvdh_solve(const __grid_constant__ SolveParams sp, const Cx<T>* __restrict__ g,
                              Cx<T>* __restrict__ y) {
-  solve_at<T, B, false>(sp, g, y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  if (sp.fly) solve_fly_at<T, B, false>(sp, g, y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  else solve_at<T, B, false>(sp, g, y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <typename T>

@@ -300,6 +300,8 @@ i64 hvdh_halo(i64 n, i64 t, double a, int B, double tol) {
   return -1;
 }
 
+constexpr i64 kHvdhTableMax = i64(64) << 20;
+
 struct Hvdh {
   i64 n, t, delta, c, w, h, H, L, R, nchunk;
   int B;
@@ -311,6 +313,10 @@ struct Hvdh {
   std::vector<double> lf;    // R*nchunk*B forward multipliers (rows i-1 .. i-B)
   std::vector<double> uf;    // R*nchunk*(B+1): 1/U_ii, U_{i,i+1..i+B}
   std::vector<int32_t> oi;   // R*nchunk: output index of the row's unknown (-1: identity row)
+  // factors rebuilt in the solve instead (FFTJ factors = :fly): per chunk the
+  // column state at its column -B and the output index of its first unknown
+  bool fly = false;
+  std::vector<int64_t> se, so;
   bool ok = false;
 };
 
@@ -353,6 +359,15 @@ Hvdh hvdh_parts(i64 n, bool f64, double scale, i64 nbatch) {
   P.R = L + 2 * P.H;
   P.nchunk = t / L;
   P.sc = scale * (double)n / (double)t;
+  // factor tables (8 + 8 B per band entry, 4 B per row) unless they would
+  // exceed kHvdhTableMax or the plan asks for factors rebuilt per call.
+  // FFTJ caps its tables at 8 MiB (_HVDH_TABLE_MAX, src/hvdh.jl:75) for the
+  // CPU's caches; on GB300 the table stream is cheaper than rebuilding
+  // (FP64 runs at 1/64 of FP32), so the cap only bounds device memory.
+  {
+    const double tbytes = (double)P.nchunk * P.R * ((2 * P.B + 1) * 8.0 + 4.0);
+    P.fly = g_sched.hvdh_factors == 2 || (g_sched.hvdh_factors == 0 && tbytes > (double)kHvdhTableMax);
+  }
   if (g_sched.dry) {  // a dry plan needs the sizes, not the tables
     P.ok = true;
     return P;
@@ -368,6 +383,24 @@ Hvdh hvdh_parts(i64 n, bool f64, double scale, i64 nbatch) {
       P.wt[q * w + op] = std::exp(-P.b * (delta - o) * (delta - o)) / P.alpha;
     }
     P.l0[q] = (int32_t)((((q * P.c - hw) % n) + n) % n);
+  }
+  if (P.fly) {
+    // per chunk: the column state e = 2 t l' - 2 n q + n at column q0 - B,
+    // and Delta l' mod n for the first unknown l' at or after row q0
+    // (_hvdh_e, src/hvdh.jl:147-151)
+    P.se.resize(P.nchunk);
+    P.so.resize(P.nchunk);
+    for (i64 ch = 0; ch < P.nchunk; ++ch) {
+      const i64 q0 = ((ch * L - P.H) % t + t) % t;
+      auto lprime = [&](i64 q) { return -fld_(-(2 * n * q - n), 2 * t); };  // cld(2nq - n, 2t)
+      const i64 qb = q0 - P.B;
+      const i64 lb = lprime(qb);
+      P.se[ch] = 2 * t * lb - 2 * n * qb + n;
+      P.so[ch] = (i64)((__int128)P.delta * lprime(q0) % n);
+      if (P.so[ch] < 0) P.so[ch] += n;
+    }
+    P.ok = true;
+    return P;
   }
   // rows: hit[q] (an unknown sits nearest row q) and that unknown's index
   std::vector<i64> ell(t, -1);
@@ -923,7 +956,29 @@ int build_c2c_hvdh(fftj_plan_s* P, const Hvdh& hv, i64 batch, i64 idist, i64 odi
   q.y_bstride = odist;
   q.B = hv.B;
   q.sc = hv.sc;
-  {
+  q.fly = hv.fly ? 1 : 0;
+  q.a = hv.a;
+  q.delta = hv.delta;
+  if (hv.fly) {
+    q.se = (const int64_t*)upload_raw(P, hv.se.data(), hv.se.size() * sizeof(int64_t));
+    q.so = (const int64_t*)upload_raw(P, hv.so.data(), hv.so.size() * sizeof(int64_t));
+    if (!q.se || !q.so) return fail(FFTJ_ERR_CUDA, "table upload failed");
+    // per-thread U rows and output indices of the back pass
+    DevBuf ub, ob;
+    ub.bytes = (size_t)hv.R * (hv.B + 1) * batch * hv.nchunk * sizeof(T);
+    ob.bytes = (size_t)hv.R * batch * hv.nchunk * sizeof(int32_t);
+    if (g_sched.dry) {
+      ub.bytes = ob.bytes = 0;
+      ub.p = ob.p = const_cast<void*>(kDryTable);
+    } else if (cudaMalloc(&ub.p, ub.bytes) != cudaSuccess || cudaMalloc(&ob.p, ob.bytes) != cudaSuccess) {
+      if (ub.p) cudaFree(ub.p);
+      return fail(FFTJ_ERR_CUDA, "workspace allocation failed");
+    }
+    P->tables.push_back(ub);
+    P->tables.push_back(ob);
+    q.uw = ub.p;
+    q.ow = (int32_t*)ob.p;
+  } else {
     std::vector<T> lf(hv.lf.size()), uf(hv.uf.size());
     for (size_t i = 0; i < lf.size(); ++i) lf[i] = (T)hv.lf[i];
     for (size_t i = 0; i < uf.size(); ++i) uf[i] = (T)hv.uf[i];
@@ -1607,6 +1662,7 @@ struct SchedScope {
     g_sched.precision = (o->precision >= 0 && o->precision <= 2) ? o->precision : 0;
     g_sched.plain_loads = o->plain_loads != 0 ? 1 : 0;
     g_sched.f64_arith = o->f64_arith != 0 ? 1 : 0;
+    g_sched.hvdh_factors = (o->hvdh_factors >= 0 && o->hvdh_factors <= 2) ? o->hvdh_factors : 0;
   }
   ~SchedScope() { g_sched = SchedOpts(); }
 };

@@ -491,3 +491,32 @@ def test_hvdh_no_coprime_t(fftj):
     for T in T_LIST:
         with pytest.raises(fftj.ArgumentError, match="no coprime smooth t"):
             fftj.Plan(T, (390,), kind="c2c", opts={"route": 3})
+
+
+@pytest.mark.parametrize("T,n,B,route", [(np.float64, 997, 2, 3), (np.float64, 10007, 3, 0), (np.float32, 20011, 2, 0),
+                                         (np.float64, 2 * 10007, 2, 0), (np.float32, 13, 2, 3)])
+def test_hvdh_factors_fly(fftj, T, n, B, route):
+    """FFTJ's factors = :fly (test/runtests.jl:122): the banded solve's
+    factors rebuilt on every call (opts.hvdh_factors = 2) agree with the
+    tabulated ones (= 1) to rounding, both within 50 eps of FP64 -- by the
+    plan's own launches and in a persistent group."""
+    import torch
+    rng = np.random.default_rng([0xF1F, n])
+    x = cn(rng, (B, n))
+    pt = fftj.Plan(T, (n,), kind="c2c", batch=B, opts={"route": route, "hvdh_factors": 1})
+    pf = fftj.Plan(T, (n,), kind="c2c", batch=B, opts={"route": route, "hvdh_factors": 2})
+    assert pf.route == pt.route and pf.route in ("HvdhPlan", "SplitPlan"), pf.route
+    xd = dev(x, T)
+    yt = host(pt(xd))
+    yf = host(pf(xd))
+    ref = np.fft.fft(x, axis=-1)
+    tol = 50 * EPS[T]  # runtests.jl:121
+    assert rel_l2(yt, ref) <= tol and rel_l2(yf, ref) <= tol, (rel_l2(yt, ref) / EPS[T], rel_l2(yf, ref) / EPS[T])
+    assert rel_l2(yf, yt) <= 10 * EPS[T], rel_l2(yf, yt) / EPS[T]
+    # the same plan as one persistent group (its solve runs the group's copy of the body)
+    pg = fftj.Plan(T, (n,), kind="c2c", batch=B, opts={"route": route, "hvdh_factors": 2, "threads_max": 256})
+    yg = torch.empty_like(xd)
+    g = fftj.Group([pg], [xd], [yg], mode="persistent")
+    g()
+    g.status()
+    assert rel_l2(host(yg), yf) <= 10 * EPS[T], rel_l2(host(yg), yf) / EPS[T]
