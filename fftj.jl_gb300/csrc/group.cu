@@ -81,27 +81,60 @@ __device__ __noinline__ void group_pass(const PassParams& pp, const void* src, v
   }
 }
 
+// the solve with factors rebuilt per call, out of line (keeps the other
+// elementwise bodies' registers)
 template <typename T>
-__device__ __noinline__ void group_elementwise(const GroupOp& op, uint32_t t0, uint32_t t1, int tid) {
+__device__ __noinline__ void group_solve_fly(const GroupOp& op, int64_t idx) {
   const Cx<T>* src = reinterpret_cast<const Cx<T>*>(op.src);
   Cx<T>* dst = reinterpret_cast<Cx<T>*>(op.dst);
-  for (uint32_t t = t0; t < t1; ++t) {
-    const int64_t idx = (int64_t)t * kEwTile + tid;
-    switch (op.kind) {
-      case OP_INTERP: interp_at<T, true>(op.ip, src, dst, idx); break;
-      case OP_RPOST: real_post_at<T, true>(op.rp, src, dst, idx); break;
-      case OP_COPY: copy_at<T, true>(op.cp, op.src, op.dst, idx); break;
-      case OP_SOLVE:
-        if (op.sv.fly) {
-          if (op.B == 1) solve_fly_at<T, 1, true>(op.sv, src, dst, idx);
-          else if (op.B == 2) solve_fly_at<T, 2, true>(op.sv, src, dst, idx);
-          else solve_fly_at<T, 3, true>(op.sv, src, dst, idx);
-        } else if (op.B == 1) solve_at<T, 1, true>(op.sv, src, dst, idx);
-        else if (op.B == 2) solve_at<T, 2, true>(op.sv, src, dst, idx);
-        else solve_at<T, 3, true>(op.sv, src, dst, idx);
-        break;
-      default: break;
-    }
+  if (op.B == 1) solve_fly_at<T, 1, true>(op.sv, src, dst, idx);
+  else if (op.B == 2) solve_fly_at<T, 2, true>(op.sv, src, dst, idx);
+  else solve_fly_at<T, 3, true>(op.sv, src, dst, idx);
+}
+
+// Each elementwise kind runs its item's tiles in a function of its own, so
+// that each gets its own register allocation (the banded solve needs many
+// more than a copy).
+template <typename T>
+__device__ __noinline__ void group_interp(const GroupOp& op, uint32_t t0, uint32_t t1, int tid) {
+  for (uint32_t t = t0; t < t1; ++t)
+    interp_at<T, true>(op.ip, reinterpret_cast<const Cx<T>*>(op.src), reinterpret_cast<Cx<T>*>(op.dst),
+                       (int64_t)t * kEwTile + tid);
+}
+template <typename T>
+__device__ __noinline__ void group_rpost(const GroupOp& op, uint32_t t0, uint32_t t1, int tid) {
+  for (uint32_t t = t0; t < t1; ++t)
+    real_post_at<T, true>(op.rp, reinterpret_cast<const Cx<T>*>(op.src), reinterpret_cast<Cx<T>*>(op.dst),
+                          (int64_t)t * kEwTile + tid);
+}
+template <typename T>
+__device__ __noinline__ void group_copy(const GroupOp& op, uint32_t t0, uint32_t t1, int tid) {
+  for (uint32_t t = t0; t < t1; ++t) copy_at<T, true>(op.cp, op.src, op.dst, (int64_t)t * kEwTile + tid);
+}
+template <typename T, int B>
+__device__ __noinline__ void group_solve(const GroupOp& op, uint32_t t0, uint32_t t1, int tid) {
+  for (uint32_t t = t0; t < t1; ++t)
+    solve_at<T, B, true>(op.sv, reinterpret_cast<const Cx<T>*>(op.src), reinterpret_cast<Cx<T>*>(op.dst),
+                         (int64_t)t * kEwTile + tid);
+}
+template <typename T>
+__device__ __forceinline__ void group_elementwise(const GroupOp& op, uint32_t t0, uint32_t t1, int tid) {
+  switch (op.kind) {
+    case OP_INTERP: group_interp<T>(op, t0, t1, tid); break;
+    case OP_RPOST: group_rpost<T>(op, t0, t1, tid); break;
+    case OP_COPY: group_copy<T>(op, t0, t1, tid); break;
+    case OP_SOLVE:
+      if (op.sv.fly) {
+        for (uint32_t t = t0; t < t1; ++t) group_solve_fly<T>(op, (int64_t)t * kEwTile + tid);
+      } else if (op.B == 1) {
+        group_solve<T, 1>(op, t0, t1, tid);
+      } else if (op.B == 2) {
+        group_solve<T, 2>(op, t0, t1, tid);
+      } else {
+        group_solve<T, 3>(op, t0, t1, tid);
+      }
+      break;
+    default: break;
   }
 }
 

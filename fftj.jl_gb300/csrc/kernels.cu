@@ -32,8 +32,15 @@ __global__ void k_interp(const __grid_constant__ InterpParams ip, const Cx<T>* _
 template <typename T, int B>
 __global__ void k_hvdh_solve(const __grid_constant__ SolveParams sp, const Cx<T>* __restrict__ g,
                              Cx<T>* __restrict__ y) {
-  if (sp.fly) solve_fly_at<T, B, false>(sp, g, y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
-  else solve_at<T, B, false>(sp, g, y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  solve_at<T, B, false>(sp, g, y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// the same solve with its factors rebuilt per call (a kernel of its own, so
+// that the tabulated solve keeps its registers)
+template <typename T, int B>
+__global__ void k_hvdh_solve_fly(const __grid_constant__ SolveParams sp, const Cx<T>* __restrict__ g,
+                                 Cx<T>* __restrict__ y) {
+  solve_fly_at<T, B, false>(sp, g, y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <typename T>
@@ -153,6 +160,15 @@ cudaError_t launch_solve(const SolveParams& sp, const void* g, void* y, cudaStre
   const unsigned grid = (unsigned)((total + th - 1) / th);
   auto gg = reinterpret_cast<const Cx<T>*>(g);
   auto yy = reinterpret_cast<Cx<T>*>(y);
+  if (sp.fly) {
+    switch (sp.B) {
+      case 1: k_hvdh_solve_fly<T, 1><<<grid, th, 0, st>>>(sp, gg, yy); break;
+      case 2: k_hvdh_solve_fly<T, 2><<<grid, th, 0, st>>>(sp, gg, yy); break;
+      case 3: k_hvdh_solve_fly<T, 3><<<grid, th, 0, st>>>(sp, gg, yy); break;
+      default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+  }
   switch (sp.B) {
     case 1: k_hvdh_solve<T, 1><<<grid, th, 0, st>>>(sp, gg, yy); break;
     case 2: k_hvdh_solve<T, 2><<<grid, th, 0, st>>>(sp, gg, yy); break;
