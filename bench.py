@@ -57,11 +57,12 @@ STEP_FLOPS = sum(flops(n, BATCH) for _, n in PARTS)
 # workload's dominant kernel, from one ncu capture on a GB300 (the capture
 # commands are kept with the profile summaries): the C64 2^18 pass kernels of
 # the mixed workload (averaged over their launches).
-NCU_TRAFFIC_PER_LAUNCH = {"c64_262144": 1025.6e6}
-# FP64 pipe busy fraction (sm__inst_executed_pipe_fp64, % of peak sustained
-# while active) of the same part's two pass kernels, averaged, from one ncu
-# capture on a GB300: the limiter of the ComplexF64 passes.
-NCU_FP64_PIPE_ACTIVE = {"c64_262144": 0.853}
+NCU_TRAFFIC_PER_LAUNCH = {"c64_262144": 1027.6e6}
+# ALU pipe busy fraction (sm__inst_executed_pipe_alu, % of peak sustained
+# while active) of the same part's two pass kernels, averaged, from the same
+# capture: the limiter of the ComplexF64 passes, which compute in 64-bit block
+# fixed point (integer pipes; no FP64-pipe instruction).
+NCU_ALU_PIPE_ACTIVE = {"c64_262144": 0.583}
 
 
 def measured_peaks():
@@ -289,14 +290,14 @@ def run_mixed(args):
         "kernel": "k_fused pass of %s N=%d x%d (%d launches/step)" % (PARTS[idx][0], dn, BATCH, dom["launches"]),
     }
     if fp64:
-        # ComplexF64 passes are limited by the FP64 pipe (1.19 TFLOP/s measured
-        # with an FMA loop on this GPU), not by HBM
-        roofline["fp64_gflops_5nlogn"] = round(flops(dn, BATCH) / dom["ms"] / 1e6, 1)
-        roofline["fp64_peak_gflops_measured"] = 1193.0
-        roofline["fp64_frac"] = round(roofline["fp64_gflops_5nlogn"] / 1193.0, 4)
-        roofline["note"] = "FP64-pipe bound on GB300 (FP64 is 1/62 of FP32); frac is the HBM fraction"
-        if dom_key in NCU_FP64_PIPE_ACTIVE:
-            roofline["fp64_pipe_active_ncu"] = NCU_FP64_PIPE_ACTIVE[dom_key]
+        # ComplexF64 passes compute in 64-bit block fixed point on the integer
+        # pipes (FP64 runs at 1.19 TFLOP/s on this GPU, measured with an FMA
+        # loop); their limiter is the ALU pipe, not HBM
+        roofline["gflops_5nlogn"] = round(flops(dn, BATCH) / dom["ms"] / 1e6, 1)
+        roofline["note"] = ("ComplexF64 passes in 64-bit block fixed point, ALU-pipe bound; "
+                            "frac is the HBM fraction")
+        if dom_key in NCU_ALU_PIPE_ACTIVE:
+            roofline["alu_pipe_active_ncu"] = NCU_ALU_PIPE_ACTIVE[dom_key]
     if dom_key in NCU_TRAFFIC_PER_LAUNCH:
         roofline["traffic"] = NCU_TRAFFIC_PER_LAUNCH[dom_key]
 
@@ -863,7 +864,8 @@ def run_uneven(args):
         "peak_source": peak_kind, "kernel": "k_group (persistent work queue, one launch per step)",
         "alg_bytes_per_launch": int(alg_bytes),
         "note": "algorithmic bytes = one read of each input + one write of each output; multi-pass "
-                "transforms re-read their data, and ComplexF64 passes are bound by the FP64 pipe, not HBM",
+                "transforms re-read their data, and ComplexF64 passes (64-bit block fixed point) "
+                "are bound by the ALU pipe, not HBM",
     }
 
     learned = None

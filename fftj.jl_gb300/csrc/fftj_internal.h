@@ -211,7 +211,10 @@ DtypeCfg dtype_cfg(bool f64);
 int pass_radices(int64_t n, bool f64, bool strided, int64_t* Rs, int cap);
 int sub_radices(int64_t R, int* out, int cap);
 int pass_geometry(PassParams& pp, bool f64, int64_t R, int64_t m, int64_t s, int64_t ncur, int64_t nbatch,
-                  int64_t ibs, int64_t obs);
+                  int64_t ibs, int64_t obs, bool wide = false);
+// the one-pass strided F32 axis: its length and tile columns
+constexpr int64_t kWideR = 4096;
+constexpr int kWideCols = 4;
 void outer_twiddle_layout(PassParams& pp, bool f64);
 const void* pick_pass_kernel(bool f64, int dir, const PassParams& pp);
 bool stage_inner_twiddles(const PassParams& pp, bool recipe);

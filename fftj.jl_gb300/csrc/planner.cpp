@@ -300,7 +300,7 @@ i64 hvdh_halo(i64 n, i64 t, double a, int B, double tol) {
   return -1;
 }
 
-constexpr i64 kHvdhTableMax = i64(64) << 20;
+constexpr i64 kHvdhTableMax = i64(1) << 30;
 
 struct Hvdh {
   i64 n, t, delta, c, w, h, H, L, R, nchunk;
@@ -363,7 +363,8 @@ Hvdh hvdh_parts(i64 n, bool f64, double scale, i64 nbatch) {
   // exceed kHvdhTableMax or the plan asks for factors rebuilt per call.
   // FFTJ caps its tables at 8 MiB (_HVDH_TABLE_MAX, src/hvdh.jl:75) for the
   // CPU's caches; on GB300 the table stream is cheaper than rebuilding
-  // (FP64 runs at 1/64 of FP32), so the cap only bounds device memory.
+  // (FP64 runs at 1/64 of FP32; 2^20-point primes solve about 2x faster from
+  // tables), so the 1 GiB cap only bounds device memory.
   {
     const double tbytes = (double)P.nchunk * P.R * ((2 * P.B + 1) * 8.0 + 4.0);
     P.fly = g_sched.hvdh_factors == 2 || (g_sched.hvdh_factors == 0 && tbytes > (double)kHvdhTableMax);
@@ -574,7 +575,8 @@ int sub_radices(i64 R, int* out, int cap) {
 // Everything of a pass but its tables, scale and load op: sub-stages, tile
 // (columns of batch x p x q), threads per column, kernel mappings and
 // shared memory. Heap-free.
-int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 nbatch, i64 ibs, i64 obs) {
+int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 nbatch, i64 ibs, i64 obs,
+                  bool wide) {
   const DtypeCfg cfg = dtype_cfg(f64);
   if (ncur >= ((i64)1 << 31)) return fail(FFTJ_ERR_UNSUPPORTED, "transform length must be below 2^31");
   pp.R = (int)R;
@@ -619,6 +621,7 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
     i64 tmax = std::max<i64>(cfg.tile_max, R);
     if (!one_pass) tmax = std::min<i64>(std::max<i64>(tmax, R * cfg.min_run), std::max<i64>(cfg.tile_cap, R));
     i64 cols = std::max<i64>(1, std::min<i64>(tmax / R, cfg.threads_max / Tf));
+    if (wide) cols = kWideCols;  // the wide kernel's tile (its own CTA size)
     if (Tf > cfg.threads_max) return fail(FFTJ_ERR_UNSUPPORTED, "pass radix needs too many threads");
     i64 Pt = 1, Qt = 1, NBt = 1;
     if (s == 1) {
@@ -672,6 +675,19 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
       for (int i = 1; i < pp.nsub; ++i) pp.fx_sht += lg(pp.sub[i].r);
     }
   return FFTJ_OK;
+}
+
+// A strided F32 axis of length kWideR runs as one pass of kWideCols-column
+// tiles (the kernel built for it has 1024 threads and one CTA per SM), so a
+// 2-D 4096 x 4096 transform sweeps HBM twice -- the row pass and this column
+// pass -- as FFTJ's Fs2Plan does (src/fourstep.jl:500-552), instead of
+// splitting the column transform into two passes of 64-point columns. Only
+// under the default schedule options (the tuner's knobs and the precision
+// form keep the usual decomposition) and when the kernel exists.
+bool wide_axis(bool f64, i64 n, i64 Bi) {
+  return !f64 && n == kWideR && Bi > 1 && Bi % kWideCols == 0 && g_sched.precision == 0 &&
+         g_sched.extra_passes <= 0 && g_sched.order == 0 && g_sched.tf_mult <= 1 && g_sched.tile == 0 &&
+         (g_sched.threads_max == 0 || g_sched.threads_max >= kWideCols * (kWideR / 16));
 }
 
 // outer twiddle table layout of a pass: none (last pass), full table
@@ -847,7 +863,16 @@ int build_axis_passes(fftj_plan_s* P, i64 n, i64 Bi, i64 nbatch, i64 ibs, i64 ob
                       std::vector<Op>* out_ops) {
   const bool f64 = sizeof(T) == 8;
   i64 Rbuf[16];
-  const int npass = pass_radices(n, f64, Bi > 1, Rbuf, 16);
+  bool wide = wide_axis(f64, n, Bi);
+  if (wide) {
+    // one pass, if the wide kernel serves its geometry
+    PassParams probe;
+    std::memset(&probe, 0, sizeof(probe));
+    wide = pass_geometry(probe, f64, n, 1, Bi, n, nbatch, ibs, obs, true) == FFTJ_OK &&
+           pick_pass_kernel(f64, dir, probe) != nullptr;
+  }
+  const int npass = wide ? 1 : pass_radices(n, f64, Bi > 1, Rbuf, 16);
+  if (wide) Rbuf[0] = n;
   if (npass == 0) return fail(FFTJ_ERR_UNSUPPORTED, "no pass decomposition for length " + std::to_string(n));
   std::vector<i64> Rs(Rbuf, Rbuf + npass);
   i64 s1 = 1;  // 1-D stride before this pass
@@ -863,7 +888,7 @@ int build_axis_passes(fftj_plan_s* P, i64 n, i64 Bi, i64 nbatch, i64 ibs, i64 ob
     const i64 m = ncur / R;
     const i64 s = s1 * Bi;  // effective stride
     {
-      int grc = pass_geometry(pp, f64, R, m, s, ncur, nbatch, ibs, obs);
+      int grc = pass_geometry(pp, f64, R, m, s, ncur, nbatch, ibs, obs, wide);
       if (grc) return grc;
     }
     // inner twiddles w_R^t (Q61 integers for block fixed-point passes)

@@ -101,7 +101,7 @@ typedef struct {
   int32_t f64_arith;     /* ComplexF64 passes: 0 block fixed point on the integer pipes (default), 1 FP64
                             butterflies on the FP64 pipe (run-time-radix kernel) */
   int32_t hvdh_factors;  /* Gaussian resampling's banded-solve factors (FFTJ factors=): 0 auto (tables up to
-                            64 MiB, else rebuilt per call), 1 tables, 2 rebuilt per call (:fly) */
+                            1 GiB, else rebuilt per call), 1 tables, 2 rebuilt per call (:fly) */
 } fftj_plan_opts_t;
 
 int fftj_plan_c2c_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch,
