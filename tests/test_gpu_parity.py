@@ -266,7 +266,7 @@ def test_config_precision_2d_4096(fftj, orc):
     assert rel_l2(y, ref) <= parity_tol(np.float32, 4096 * 4096)
     # two HBM sweeps, as FFTJ's Fs2Plan (src/fourstep.jl:500-552): the
     # contiguous rows, then the strided 4096-point columns in one pass
-    inf = fftj.Plan(np.float32, (4096, 4096), kind="c2c").info()
+    inf = fftj.Plan(np.float32, (4096, 4096), kind="c2c").info
     assert inf.npasses == 2 and list(inf.pass_radix[:2]) == [4096, 4096]
     assert list(inf.pass_threads[:2])[1] == 1024 and inf.specialized_passes == 2
 
@@ -284,7 +284,7 @@ def test_strided_4096_axis_one_pass(fftj, orc, shape):
     assert rel_l2(y, orc.PlanND(np.float32, list(reversed(shape)), "fft")(x)) <= tol, shape
     assert rel_l2(host(fftj.ifft(dev(y, np.float32))), x) <= tol, shape
     inner = int(np.prod(shape[shape.index(4096) + 1:]))
-    inf = fftj.Plan(np.float32, tuple(reversed(shape)), kind="c2c").info()
+    inf = fftj.Plan(np.float32, tuple(reversed(shape)), kind="c2c").info
     assert (4096 in list(inf.pass_radix[:inf.npasses])) == (inner % 4 == 0), shape
 
 
