@@ -622,6 +622,7 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
     if (!one_pass) tmax = std::min<i64>(std::max<i64>(tmax, R * cfg.min_run), std::max<i64>(cfg.tile_cap, R));
     i64 cols = std::max<i64>(1, std::min<i64>(tmax / R, cfg.threads_max / Tf));
     if (wide) cols = kWideCols;  // the wide kernel's tile (its own CTA size)
+    pp.cluster = 0;
     if (Tf > cfg.threads_max) return fail(FFTJ_ERR_UNSUPPORTED, "pass radix needs too many threads");
     i64 Pt = 1, Qt = 1, NBt = 1;
     if (s == 1) {
@@ -653,6 +654,10 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
     pp.tiles_b = (uint32_t)((nbatch + NBt - 1) / NBt);
     pp.ftq = FastDiv(pp.tiles_q);
     pp.ftp = FastDiv(pp.tiles_p);
+    if (wide && kWideCluster > 1 && pp.tiles_q % kWideCluster == 0) {
+      // clusters of neighbouring column strips (tile index = strip fastest)
+      pp.cluster = kWideCluster;
+    }
     const double ntiles = (double)pp.tiles_q * pp.tiles_p * pp.tiles_b;
     if (ntiles >= 2147483647.0) return fail(FFTJ_ERR_UNSUPPORTED, "grid too large");
     const i64 E = (i64)pp.NB * R;
@@ -677,15 +682,19 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
   return FFTJ_OK;
 }
 
-// A strided F32 axis of length kWideR runs as one pass of kWideCols-column
-// tiles (the kernel built for it has 1024 threads and one CTA per SM), so a
-// 2-D 4096 x 4096 transform sweeps HBM twice -- the row pass and this column
-// pass -- as FFTJ's Fs2Plan does (src/fourstep.jl:500-552), instead of
-// splitting the column transform into two passes of 64-point columns. Only
-// under the default schedule options (the tuner's knobs and the precision
-// form keep the usual decomposition) and when the kernel exists.
+// opts.wide_axis: a strided F32 axis of length kWideR runs as one pass of
+// kWideCols-column tiles (the kernel built for it has 1024 threads and one
+// CTA per SM), so a 2-D 4096 x 4096 transform sweeps HBM twice -- the row
+// pass and this column pass -- as FFTJ's Fs2Plan does
+// (src/fourstep.jl:500-552), instead of splitting the column transform into
+// two passes of 64-point columns. Not the default: its tile rows are 32
+// bytes, so each warp's loads and stores touch eight cache lines and the
+// pass is bound by the load/store unit (0.37 of HBM on GB300), where the two
+// radix-64 passes reach 0.86 each and finish sooner together. Only with the
+// tuner's other knobs and the precision form at their defaults, and when
+// the kernel exists.
 bool wide_axis(bool f64, i64 n, i64 Bi) {
-  return !f64 && n == kWideR && Bi > 1 && Bi % kWideCols == 0 && g_sched.precision == 0 &&
+  return g_sched.wide_axis == 1 && !f64 && n == kWideR && Bi > 1 && Bi % kWideCols == 0 && g_sched.precision == 0 &&
          g_sched.extra_passes <= 0 && g_sched.order == 0 && g_sched.tf_mult <= 1 && g_sched.tile == 0 &&
          (g_sched.threads_max == 0 || g_sched.threads_max >= kWideCols * (kWideR / 16));
 }
@@ -760,7 +769,12 @@ bool has_tc16_substage(const PassParams& pp) {
 // when the table is small next to the tile; beyond kStageTwiddleMax entries
 // they read it from global memory (L1/L2-resident).
 constexpr int kStageTwiddleMax = 1024;
-bool stage_inner_twiddles(const PassParams& pp, bool recipe) { return recipe && pp.R <= kStageTwiddleMax; }
+// The wide strided pass (one CTA per SM, 1024 threads) stages its 32 KB
+// table too (it has the shared memory to spare; 3% faster measured).
+bool stage_inner_twiddles(const PassParams& pp, bool recipe) {
+  const bool wide = pp.R == kWideR && pp.NB == kWideCols && pp.threads == kWideCols * (kWideR / 16);
+  return recipe && (pp.R <= kStageTwiddleMax || wide);
+}
 
 void set_error(const char* msg) { g_err = msg; }
 
@@ -1688,6 +1702,7 @@ struct SchedScope {
     g_sched.plain_loads = o->plain_loads != 0 ? 1 : 0;
     g_sched.f64_arith = o->f64_arith != 0 ? 1 : 0;
     g_sched.hvdh_factors = (o->hvdh_factors >= 0 && o->hvdh_factors <= 2) ? o->hvdh_factors : 0;
+    g_sched.wide_axis = o->wide_axis == 1 ? 1 : 0;
   }
   ~SchedScope() { g_sched = SchedOpts(); }
 };

@@ -61,7 +61,7 @@ class PlanOpts(ctypes.Structure):
     """fftj_plan_opts_t: schedule options (all zero = the planner's default)."""
     _fields_ = [(k, ctypes.c_int32) for k in
                 ("tile", "extra_passes", "order", "tf_mult", "route", "threads_max", "dry", "precision",
-                 "plain_loads", "f64_arith", "hvdh_factors")]
+                 "plain_loads", "f64_arith", "hvdh_factors", "wide_axis")]
 
 
 class TuneQuery(ctypes.Structure):

@@ -102,6 +102,9 @@ typedef struct {
                             butterflies on the FP64 pipe (run-time-radix kernel) */
   int32_t hvdh_factors;  /* Gaussian resampling's banded-solve factors (FFTJ factors=): 0 auto (tables up to
                             1 GiB, else rebuilt per call), 1 tables, 2 rebuilt per call (:fly) */
+  int32_t wide_axis;     /* 1: a strided F32 axis of length 4096 (inner extent a multiple of 4) runs as one
+                            pass of 4-column tiles, so 4096 x 4096 sweeps HBM twice as FFTJ's Fs2Plan;
+                            0 (default): two passes of 64-point columns (measured faster on GB300) */
 } fftj_plan_opts_t;
 
 int fftj_plan_c2c_ex(fftj_plan* out, int dtype, int rank, const int64_t* dims, int64_t batch,

@@ -264,28 +264,35 @@ def test_config_precision_2d_4096(fftj, orc):
     y = host(fftj.fft(dev(x, np.float32)))
     ref = np.fft.fft2(x.astype(np.complex128))
     assert rel_l2(y, ref) <= parity_tol(np.float32, 4096 * 4096)
-    # two HBM sweeps, as FFTJ's Fs2Plan (src/fourstep.jl:500-552): the
-    # contiguous rows, then the strided 4096-point columns in one pass
-    inf = fftj.Plan(np.float32, (4096, 4096), kind="c2c").info
+    # two HBM sweeps on request, as FFTJ's Fs2Plan (src/fourstep.jl:500-552):
+    # the contiguous rows, then the strided 4096-point columns in one pass
+    p2 = fftj.Plan(np.float32, (4096, 4096), kind="c2c", opts={"wide_axis": 1})
+    inf = p2.info
     assert inf.npasses == 2 and list(inf.pass_radix[:2]) == [4096, 4096]
     assert list(inf.pass_threads[:2])[1] == 1024 and inf.specialized_passes == 2
+    assert rel_l2(host(p2(dev(x, np.float32))), ref) <= parity_tol(np.float32, 4096 * 4096)
 
 
 @pytest.mark.parametrize("shape", [(4096, 64), (4096, 3, 4), (2, 4096, 12), (4096, 6)])
 def test_strided_4096_axis_one_pass(fftj, orc, shape):
-    """Strided ComplexF32 axes of length 4096 (one pass of 4-column tiles
-    when the inner extent is a multiple of 4, else two passes), forward and
-    inverse, against FP64 numpy and the oracle's N-d plan."""
+    """opts.wide_axis: strided ComplexF32 axes of length 4096 (one pass of
+    4-column tiles when the inner extent is a multiple of 4, else two
+    passes), forward and inverse, against FP64 numpy and the oracle's N-d
+    plan."""
     rng = np.random.default_rng(list(shape))
     x = cn(rng, shape).astype(np.complex64)
     tol = parity_tol(np.float32, int(np.prod(shape)))
-    y = host(fftj.fft(dev(x, np.float32)))
+    dims = tuple(reversed(shape))
+    pf = fftj.Plan(np.float32, dims, kind="c2c", opts={"wide_axis": 1})
+    pb = fftj.Plan(np.float32, dims, kind="c2c", direction=1, scale=1.0 / x.size, opts={"wide_axis": 1})
+    y = host(pf(dev(x, np.float32)))
     assert rel_l2(y, np.fft.fftn(x.astype(np.complex128))) <= tol, shape
-    assert rel_l2(y, orc.PlanND(np.float32, list(reversed(shape)), "fft")(x)) <= tol, shape
-    assert rel_l2(host(fftj.ifft(dev(y, np.float32))), x) <= tol, shape
+    assert rel_l2(y, orc.PlanND(np.float32, list(dims), "fft")(x)) <= tol, shape
+    assert rel_l2(host(pb(dev(y, np.float32))), x) <= tol, shape
     inner = int(np.prod(shape[shape.index(4096) + 1:]))
-    inf = fftj.Plan(np.float32, tuple(reversed(shape)), kind="c2c").info
-    assert (4096 in list(inf.pass_radix[:inf.npasses])) == (inner % 4 == 0), shape
+    for p in (pf, pb):
+        inf = p.info
+        assert (4096 in list(inf.pass_radix[:inf.npasses])) == (inner % 4 == 0), shape
 
 
 def test_config_rfft3d_256(fftj):

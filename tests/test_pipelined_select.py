@@ -44,8 +44,7 @@ def dry_info(F, kind, dtype, dims, batch=1, **opts):
     ("c2c", np.float32, (1 << 20,), 2, 2),        # 1024 x 1024: both passes
     ("c2c", np.float32, (1 << 18,), 4, 2),        # 512 x 512
     ("c2c", np.float32, (1 << 26,), 1, 2),        # 512 x 512 x 256: the last radix-256 pass keeps plain loads
-    ("c2c", np.float32, (4096, 4096), 1, 1),      # radix-4096 row pass; the one-pass 4096-point columns
-                                                  # (128 KB tiles) are not pipelined
+    ("c2c", np.float32, (4096, 4096), 1, 3),      # radix-4096 row pass + two radix-64 column passes
     ("c2c", np.float32, (4096,), 5, 1),           # three-sub-stage single pass
     ("c2c", np.float32, (256,), 8, 0),            # two-sub-stage single pass
     ("c2c", np.float32, (42525,), 2, 0),          # odd radices

@@ -122,31 +122,36 @@ def test_every_smooth_length_plans_by_default(T):
 
 
 def test_strided_4096_axis_plans_one_pass(T):
-    """A strided F32 axis of length 4096 is one pass of 4-column tiles (1024
-    threads) under the default options, so 4096 x 4096 takes two sweeps as
-    FFTJ's Fs2Plan; the thread cap of persistent groups, the precision form,
-    F64 and inner extents not divisible by 4 keep the two-pass column split."""
-    inf = info(T, "c2c", np.float32, (4096, 4096))
+    """opts.wide_axis: a strided F32 axis of length 4096 is one pass of
+    4-column tiles (1024 threads), so 4096 x 4096 takes two sweeps as FFTJ's
+    Fs2Plan; the default, the thread cap of persistent groups, the precision
+    form, F64 and inner extents not divisible by 4 keep the two-pass column
+    split."""
+    import ctypes
+    from fftj import PlanInfo, lib
+
+    def wide(dtype, dims, **extra):
+        q = T.query("c2c", dtype, dims)
+        o = T.make_opts((0,) * len(T.OPT_FIELDS), dry=1)
+        o.wide_axis = 1
+        for k, v in extra.items():
+            setattr(o, k, v)
+        h = ctypes.c_void_p()
+        assert lib().fftj_tune_plan(ctypes.byref(q), ctypes.byref(o), ctypes.byref(h)) == 0
+        inf = PlanInfo()
+        lib().fftj_plan_get_info(h, ctypes.byref(inf))
+        lib().fftj_plan_destroy(h)
+        return inf
+
+    assert list(info(T, "c2c", np.float32, (4096, 4096)).pass_radix[:3]) == [4096, 64, 64]
+    inf = wide(np.float32, (4096, 4096))
     assert list(inf.pass_radix[:inf.npasses]) == [4096, 4096]
     assert list(inf.pass_threads[:2]) == [256, 1024] and list(inf.pass_tile[:2]) == [4096, 16384]
     assert inf.specialized_passes == 2
-    inf = info(T, "c2c", np.float32, (4096, 4096), threads_max=256)
-    assert list(inf.pass_radix[:inf.npasses]) == [4096, 64, 64]
-    assert list(info(T, "c2c", np.float32, (6, 4096)).pass_radix[:3]) == [6, 64, 64]
-    inf = info(T, "c2c", np.float64, (4096, 4096))
-    assert 4096 not in list(inf.pass_radix[1:inf.npasses])
-    # the precision form (its tensor-core sub-stage runs in the run-time kernel)
-    import ctypes
-    from fftj import PlanInfo, lib
-    q = T.query("c2c", np.float32, (4096, 4096))
-    o = T.make_opts((0,) * len(T.OPT_FIELDS), dry=1)
-    o.precision = 1
-    h = ctypes.c_void_p()
-    assert lib().fftj_tune_plan(ctypes.byref(q), ctypes.byref(o), ctypes.byref(h)) == 0
-    inf = PlanInfo()
-    lib().fftj_plan_get_info(h, ctypes.byref(inf))
-    lib().fftj_plan_destroy(h)
-    assert list(inf.pass_radix[:inf.npasses]) == [4096, 64, 64]
+    assert list(wide(np.float32, (4096, 4096), threads_max=256).pass_radix[:3]) == [4096, 64, 64]
+    assert list(wide(np.float32, (6, 4096)).pass_radix[:3]) == [6, 64, 64]
+    assert 4096 not in list(wide(np.float64, (4096, 4096)).pass_radix[1:8])
+    assert list(wide(np.float32, (4096, 4096), precision=1).pass_radix[:3]) == [4096, 64, 64]
 
 
 def test_split_route_choice(T):
