@@ -37,6 +37,32 @@ __device__ __forceinline__ void interp_at(const InterpParams& ip, const Cx<T>* _
   y[b * ip.y_bstride + k * inner + i] = mk<T>(re, im);
 }
 
+// Thread -> (sequence b, chunk ch, lane i) of a banded solve. Along a
+// strided axis (HvPass lanes, sp.inner > 1: row r of lane i at r * inner +
+// i) lanes are fastest, so a warp's grid reads and output writes are
+// adjacent and its factor reads are one broadcast; b is then the outer
+// block (nbatch = outer blocks x inner). Contiguous sequences (inner == 1)
+// take chunks fastest.
+struct SolveLane {
+  int64_t b, ch, i, rs;
+};
+__device__ __forceinline__ SolveLane solve_lane(const SolveParams& sp, int64_t tid) {
+  SolveLane l;
+  if (sp.inner > 1) {
+    const int64_t r = tid / sp.inner;
+    l.i = tid - r * sp.inner;
+    l.b = r / sp.nchunk;
+    l.ch = r - l.b * sp.nchunk;
+    l.rs = sp.inner;
+  } else {
+    l.b = tid / sp.nchunk;
+    l.ch = tid - l.b * sp.nchunk;
+    l.i = 0;
+    l.rs = 1;
+  }
+  return l;
+}
+
 // HvdH banded solve (FFTJ _hvdh_subst! / _hvdh_back!, src/hvdh.jl:604-686):
 // thread (b, c) runs forward substitution over its chunk's R rows (rows q0
 // .. q0+R-1 of the length-t transform, cyclic), keeping z in a strided
@@ -58,7 +84,8 @@ __device__ __forceinline__ void solve_fly_at(const SolveParams& sp, const Cx<T>*
                                              Cx<T>* __restrict__ y, const int64_t tid) {
   const int64_t nt = sp.nbatch * sp.nchunk;
   if (tid >= nt) return;
-  const int64_t b = tid / sp.nchunk, ch = tid - b * sp.nchunk;
+  const SolveLane ln = solve_lane(sp, tid);
+  const int64_t b = ln.b, ch = ln.ch, rs = ln.rs;
   const int R = (int)sp.R, H = (int)sp.H, L = (int)sp.L;
   const int t = (int)sp.t;
   const int64_t n = sp.n, d2 = 2 * sp.delta, n2 = 2 * n;
@@ -78,7 +105,7 @@ __device__ __forceinline__ void solve_fly_at(const SolveParams& sp, const Cx<T>*
   Cx<T>* zwp = reinterpret_cast<Cx<T>*>(sp.zw) + tid;
   T* uwp = reinterpret_cast<T*>(sp.uw) + tid;
   int32_t* owp = sp.ow + tid;
-  const Cx<T>* gb = g + b * sp.g_bstride;
+  const Cx<T>* gb = g + b * sp.g_bstride + ln.i;
   int q = (int)((((int64_t)ch * L - H) % t + t) % t);
   T up[B][B + 1];  // U rows i-1 .. i-B: 1/U_jj, U_{j,j+1..j+B}
 #pragma unroll
@@ -103,7 +130,7 @@ __device__ __forceinline__ void solve_fly_at(const SolveParams& sp, const Cx<T>*
     if (!hi) r[B] = (T)1;  // identity row
     // eliminate columns i-B .. i-1 against the previous U rows
     Cx<T> z = mk<T>(0, 0);
-    if (hi) z = ldd<CG>(gb + q);
+    if (hi) z = ldd<CG>(gb + (int64_t)q * rs);
 #pragma unroll
     for (int k = B; k >= 1; --k) {
       const T f = r[B - k] * up[k - 1][0];
@@ -140,7 +167,7 @@ __device__ __forceinline__ void solve_fly_at(const SolveParams& sp, const Cx<T>*
 #pragma unroll
   for (int k = 0; k < B; ++k) xp[k] = mk<T>(0, 0);
   const T sc = (T)sp.sc;
-  Cx<T>* yb = y + b * sp.y_bstride;
+  Cx<T>* yb = y + b * sp.y_bstride + ln.i;
   const Cx<T>* twb = sp.tw ? reinterpret_cast<const Cx<T>*>(sp.tw) : nullptr;
   const int64_t twr = sp.tw ? (b % sp.tw_s) : 0;
   for (int i = R - 1; i >= H; --i) {
@@ -161,7 +188,7 @@ __device__ __forceinline__ void solve_fly_at(const SolveParams& sp, const Cx<T>*
     if (i < H + L && o >= 0) {
       Cx<T> v = mk<T>(x.x * sc, x.y * sc);
       if (twb) v = cmul(v, __ldg(twb + twr * o));
-      yb[o] = v;
+      yb[(int64_t)o * rs] = v;
     }
   }
 }
@@ -176,7 +203,8 @@ __device__ __forceinline__ void solve_at(const SolveParams& sp, const Cx<T>* __r
   constexpr int K = 8;
   const int64_t nt = sp.nbatch * sp.nchunk;
   if (tid >= nt) return;
-  const int64_t b = tid / sp.nchunk, ch = tid - b * sp.nchunk;
+  const SolveLane ln = solve_lane(sp, tid);
+  const int64_t b = ln.b, ch = ln.ch, rs = ln.rs;
   const int R = (int)sp.R, H = (int)sp.H, L = (int)sp.L;
   const int t = (int)sp.t;
   // factor tables are row-major across chunks: row i of chunk ch at
@@ -187,7 +215,7 @@ __device__ __forceinline__ void solve_at(const SolveParams& sp, const Cx<T>* __r
   const int32_t* oip = sp.oi + ch;
   const int64_t lstep = nc * B, ustep = nc * (B + 1);
   Cx<T>* zwp = reinterpret_cast<Cx<T>*>(sp.zw) + tid;
-  const Cx<T>* gb = g + b * sp.g_bstride;
+  const Cx<T>* gb = g + b * sp.g_bstride + ln.i;
   int q = (int)((((int64_t)ch * L - H) % t + t) % t);
   Cx<T> zp[B];
 #pragma unroll
@@ -201,7 +229,7 @@ __device__ __forceinline__ void solve_at(const SolveParams& sp, const Cx<T>* __r
       if (i0 + u < R) {
         int qq = q + u;
         if (qq >= t) qq -= t;
-        const Cx<T> v = ldd<CG>(gb + qq);  // in range for every row: load, then mask
+        const Cx<T> v = ldd<CG>(gb + (int64_t)qq * rs);  // in range for every row: load, then mask
         if (__ldg(oip + u * nc) >= 0) gv[u] = v;
 #pragma unroll
         for (int k = 0; k < B; ++k) f[u][k] = __ldg(lfp + u * lstep + k);
@@ -232,7 +260,7 @@ __device__ __forceinline__ void solve_at(const SolveParams& sp, const Cx<T>* __r
 #pragma unroll
   for (int k = 0; k < B; ++k) xp[k] = mk<T>(0, 0);  // xp[k] = x_{i+1+k}
   const T sc = (T)sp.sc;
-  Cx<T>* yb = y + b * sp.y_bstride;
+  Cx<T>* yb = y + b * sp.y_bstride + ln.i;
   const Cx<T>* twb = sp.tw ? reinterpret_cast<const Cx<T>*>(sp.tw) + 0 : nullptr;
   const int64_t twr = sp.tw ? (b % sp.tw_s) : 0;
   // back substitution from row R-1 down to H
@@ -271,7 +299,7 @@ __device__ __forceinline__ void solve_at(const SolveParams& sp, const Cx<T>* __r
         if (i < H + L && o >= 0) {
           Cx<T> v = mk<T>(x.x * sc, x.y * sc);
           if (twb) v = cmul(v, __ldg(twb + twr * o));
-          yb[o] = v;
+          yb[(int64_t)o * rs] = v;
         }
       }
     }
@@ -345,6 +373,16 @@ __device__ __forceinline__ void copy_at(const CopyParams& cp, const void* __rest
   } else if (cp.mode == 3) {  // complex copy of the first n entries
     reinterpret_cast<Cx<T>*>(out)[b * cp.out_bstride + j] =
         ldd<CG>(reinterpret_cast<const Cx<T>*>(in) + b * cp.in_bstride + j);
+  } else if (cp.mode == 6) {
+    // CompositePlan's twiddle and transpose (src/composite.jl:93-96, the
+    // twiddles fused into the next pass as FFTJ fuses them into its
+    // deconvolution): output (j1, k2) at k2 + s j1 = input (k2, j1) at
+    // j1 + p k2, times w_n^(j1 k2) (j1 k2 < n)
+    const int64_t sd = cp.nc, pl = cp.n / sd;
+    const int64_t j1 = j / sd, k2 = j - j1 * sd;
+    const Cx<T> v = ldd<CG>(reinterpret_cast<const Cx<T>*>(in) + b * cp.in_bstride + j1 + pl * k2);
+    const Cx<T> w = __ldg(reinterpret_cast<const Cx<T>*>(cp.tab) + j1 * k2);
+    reinterpret_cast<Cx<T>*>(out)[b * cp.out_bstride + j] = cmul(v, w);
   } else if (cp.mode == 5) {  // decimation in time (FFTJ _split_gather!, src/composite.jl:245-252)
     const int64_t sd = cp.nc, pl = cp.n / sd;
     const int64_t r = j / pl, jj = j - r * pl;

@@ -107,6 +107,8 @@ struct PassParams {
 struct SolveParams {
   int64_t n, t, L, H, R, nchunk, nbatch;
   int64_t g_bstride, y_bstride;
+  int64_t inner;             // lanes of a strided axis (HvPass; row r of lane i at r*inner + i), 0/1: none;
+                             //   nbatch = outer blocks x inner, the strides are per outer block
   int B;
   double sc;                 // scale * n / t
   const void* lf;            // nchunk*R*B multipliers
@@ -150,9 +152,10 @@ struct CopyParams {
   // 0: real -> complex, 1: hermitian expand (n real), 2: complex -> real,
   // 3: complex copy of n entries, 4: irfft pre-pass Z[k], k < n = h,
   // 5: decimation, row r of the output = x[r + s j], j < n / s (s = nc)
+  // 6: twiddled transpose, output k2 + s j1 = x[j1 + p k2] w_n^(j1 k2) (s = nc)
   int mode;
-  int64_t nc;          // complex length per batch (mode 1); s (mode 5)
-  const void* tab;     // mode 4: e^{+2 pi i k / 2h}
+  int64_t nc;          // complex length per batch (mode 1); s (modes 5, 6)
+  const void* tab;     // mode 4: e^{+2 pi i k / 2h}; mode 6: w_n^e, e < n
   double pre;          // mode 4: pair factor (1/2 irfft, 1 brfft)
 };
 

@@ -432,16 +432,20 @@ __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in,
     return mk<T>(x.x * c, x.y * c);
   } else if (LOADOP == LOAD_SPREAD) {
     // HvdH Gaussian spread (src/hvdh.jl:355-470, per output row as the
-    // batched HvPass): grid row g = sum_o wt[g*w + o] * x[(l0[g] + o) mod n]
-    const int64_t n = pp.ld_n;
+    // batched HvPass): grid row a = sum_o wt[a*w + o] * x[(l0[a] + o) mod n];
+    // along a strided axis (HvPass lanes, src/hvdh.jl:696-702) g = a * inner
+    // + i and input row r of lane i sits at r * inner + i
+    const int64_t n = pp.ld_n, inner = pp.ld_inner > 1 ? pp.ld_inner : 1;
+    int64_t a = g, i = 0;
+    if (inner > 1) { a = g / inner; i = g - a * inner; }
     const int w = pp.ld_w;
-    const Cx<T>* x = reinterpret_cast<const Cx<T>*>(in) + b * pp.ld_stride;
-    const T* wt = reinterpret_cast<const T*>(pp.ld_tab) + g * w;
-    int64_t r = __ldg(pp.ld_l0 + g);
+    const Cx<T>* x = reinterpret_cast<const Cx<T>*>(in) + b * pp.ld_stride + i;
+    const T* wt = reinterpret_cast<const T*>(pp.ld_tab) + a * w;
+    int64_t r = __ldg(pp.ld_l0 + a);
     T re = 0, im = 0;
     for (int o = 0; o < w; ++o) {
       const T c = __ldg(wt + o);
-      const Cx<T> v = ldd<CG>(x + r);
+      const Cx<T> v = ldd<CG>(x + r * inner);
       re = fma(c, v.x, re);
       im = fma(c, v.y, im);
       if (++r == n) r = 0;
@@ -1000,15 +1004,17 @@ __device__ __forceinline__ Cx<T> load_elem_off(const PassParams& pp, const void*
     const T c = __ldg(reinterpret_cast<const T*>(pp.ld_tab) + j);
     return mk<T>(x.x * c, x.y * c);
   } else if (LOADOP == LOAD_SPREAD) {
-    const int64_t n = pp.ld_n;
+    const int64_t n = pp.ld_n, inner = pp.ld_inner > 1 ? pp.ld_inner : 1;
+    int64_t a = g, i = 0;
+    if (inner > 1) { a = g / inner; i = g - a * inner; }
     const int w = pp.ld_w;
-    const Cx<T>* x = reinterpret_cast<const Cx<T>*>(in) + boff;
-    const T* wt = reinterpret_cast<const T*>(pp.ld_tab) + g * w;
-    int64_t r = __ldg(pp.ld_l0 + g);
+    const Cx<T>* x = reinterpret_cast<const Cx<T>*>(in) + boff + i;
+    const T* wt = reinterpret_cast<const T*>(pp.ld_tab) + a * w;
+    int64_t r = __ldg(pp.ld_l0 + a);
     T re = 0, im = 0;
     for (int o = 0; o < w; ++o) {
       const T c = __ldg(wt + o);
-      const Cx<T> v = __ldg(x + r);
+      const Cx<T> v = __ldg(x + r * inner);
       re = fma(c, v.x, re);
       im = fma(c, v.y, im);
       if (++r == n) r = 0;

@@ -958,20 +958,28 @@ int alloc_workspace(fftj_plan_s* P) {
   return FFTJ_OK;
 }
 
-// HvdH route (src/hvdh.jl:222-241): spread fused into the first pass of the
-// length-t transform, the smooth passes, the chunked banded solve.
+// Gaussian resampling along an axis (hv.n rows, Bi lanes: row r of lane i at
+// r Bi + i; nb outer blocks at strides ibs / obs): the spread fused into the
+// first pass of the length-t transform, the smooth passes along the axis,
+// the chunked banded solve. Bi = 1 is HvdhPlan (src/hvdh.jl:222-241); Bi >
+// 1 is the batched HvPass (src/hvdh.jl:696-836), whose lanes share the
+// spread weights and the band factors -- on the GPU the lanes are adjacent
+// threads of the solve (every lane reads the same factor entry) and the
+// axis is chunked as in HvdhPlan, where FFTJ's HvPass factors one cyclic
+// chunk per lane vector (same mathematics, more parallelism).
 template <typename T>
-int build_c2c_hvdh(fftj_plan_s* P, const Hvdh& hv, i64 batch, i64 idist, i64 odist, int dir,
-                   std::vector<Op>* ops, int* route) {
+int build_axis_hvdh(fftj_plan_s* P, const Hvdh& hv, i64 Bi, i64 nb, i64 ibs, i64 obs, int dir,
+                    std::vector<Op>* ops) {
+  const i64 batch = nb * Bi;  // sequences: outer blocks x lanes
   std::vector<Op> tmp;
-  int rc = build_axis_passes<T>(P, hv.t, 1, batch, hv.t, hv.t, dir, 1.0, &tmp);
+  int rc = build_axis_passes<T>(P, hv.t, Bi, nb, Bi * hv.t, Bi * hv.t, dir, 1.0, &tmp);
   if (rc) return rc;
   PassParams& f = tmp.front().pp;
   f.load_op = LOAD_SPREAD;
   f.ld_n = hv.n;
   f.ld_m = hv.t;
-  f.ld_stride = idist;
-  f.ld_inner = 1;
+  f.ld_stride = ibs;
+  f.ld_inner = Bi;
   f.ld_w = (int)hv.w;
   {
     std::vector<T> w(hv.wt.size());
@@ -991,8 +999,9 @@ int build_c2c_hvdh(fftj_plan_s* P, const Hvdh& hv, i64 batch, i64 idist, i64 odi
   q.R = hv.R;
   q.nchunk = hv.nchunk;
   q.nbatch = batch;
-  q.g_bstride = hv.t;
-  q.y_bstride = odist;
+  q.inner = Bi;
+  q.g_bstride = Bi * hv.t;
+  q.y_bstride = obs;
   q.B = hv.B;
   q.sc = hv.sc;
   q.fly = hv.fly ? 1 : 0;
@@ -1035,11 +1044,20 @@ int build_c2c_hvdh(fftj_plan_s* P, const Hvdh& hv, i64 batch, i64 idist, i64 odi
     P->tables.push_back(zb);
     q.zw = zb.p;
   }
-  sv.dst_bytes = (size_t)(batch * odist) * sizeof(T) * 2;
+  sv.dst_bytes = (size_t)(nb * obs) * sizeof(T) * 2;
   for (auto& o : tmp) ops->push_back(o);
   ops->push_back(sv);
   P->resample_m = hv.t;
   P->resample_w = hv.w;
+  return FFTJ_OK;
+}
+
+// HvdH route (src/hvdh.jl:222-241): one lane per batch entry
+template <typename T>
+int build_c2c_hvdh(fftj_plan_s* P, const Hvdh& hv, i64 batch, i64 idist, i64 odist, int dir,
+                   std::vector<Op>* ops, int* route) {
+  const int rc = build_axis_hvdh<T>(P, hv, 1, batch, idist, odist, dir, ops);
+  if (rc) return rc;
   *route = FFTJ_ROUTE_HVDH;
   return FFTJ_OK;
 }
@@ -1110,6 +1128,68 @@ int build_c2c_split(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int 
   return FFTJ_OK;
 }
 
+template <typename T>
+int build_axis_resample(fftj_plan_s* P, i64 nd, i64 Bi, i64 nb, int dir, double scale, std::vector<Op>* ops);
+
+// FFTJ's CompositePlan (src/composite.jl:10-101): non-smooth n = p s with s
+// its 7-smooth part, one Cooley-Tukey step in decimation in frequency (j =
+// j1 + p j2, k = k2 + s k1). The length-s transforms over j2 run as the
+// passes of an axis of p lanes (exact); a twiddled transpose writes (j1,
+// k2) at k2 + s j1 times w_n^(j1 k2); the length-p transforms over j1 are
+// one pass along rows j1 with s lanes -- the batched HvPass for p >= 500
+// (_COMPOSITE_HV_MINP), batched resampling (RsPass) below -- whose output
+// rows k1 of s lanes are already in natural order.
+constexpr i64 kCompositeMinS = 16;     // _COMPOSITE_MIN_S
+constexpr i64 kCompositeHvMinP = 500;  // _COMPOSITE_HV_MINP
+bool use_composite(bool f64, i64 n) {
+  const i64 s = smooth7_part(n), p = n / s;
+  if (s < 2 || p < 2) return false;
+  if (g_sched.route == 4) return true;
+  if (g_sched.route != 0) return false;
+  return s >= kCompositeMinS && n >= (f64 ? 4096 : 32768);  // _use_composite
+}
+
+template <typename T>
+int build_c2c_composite(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir, double scale,
+                        std::vector<Op>* ops, int* route) {
+  const bool f64 = sizeof(T) == 8;
+  const i64 s = smooth7_part(n), p = n / s;
+  std::vector<Op> sops;
+  int rc = build_axis_passes<T>(P, s, p, batch, n, n, dir, 1.0, &sops);
+  if (rc) return rc;
+  sops.front().pp.in_bstride = idist;
+  Op tr;
+  tr.kind = OP_COPY;
+  std::memset(&tr.cp, 0, sizeof(tr.cp));
+  tr.cp.mode = 6;
+  tr.cp.n = n;
+  tr.cp.nc = s;
+  tr.cp.nbatch = batch;
+  tr.cp.in_bstride = n;
+  tr.cp.out_bstride = n;
+  tr.cp.tab = omega_table<T>(P, n, n, 1, dir);
+  if (!tr.cp.tab) return fail(FFTJ_ERR_CUDA, "table upload failed");
+  tr.dst_bytes = (size_t)(batch * n) * sizeof(T) * 2;
+  std::vector<Op> pops;
+  if (p >= kCompositeHvMinP) {
+    Hvdh hv = hvdh_parts(p, f64, scale, batch * s);
+    if (!hv.ok) return fail(FFTJ_ERR_UNSUPPORTED, "no Gaussian resampling for the odd part");
+    rc = build_axis_hvdh<T>(P, hv, s, batch, n, odist, dir, &pops);
+  } else {
+    rc = build_axis_resample<T>(P, p, s, batch, dir, scale, &pops);
+    if (rc == FFTJ_OK) {
+      pops.back().ip.y_bstride = odist;
+      pops.back().dst_bytes = (size_t)(batch * odist) * sizeof(T) * 2;
+    }
+  }
+  if (rc) return rc;
+  for (auto& o : sops) ops->push_back(o);
+  ops->push_back(tr);
+  for (auto& o : pops) ops->push_back(o);
+  *route = FFTJ_ROUTE_COMPOSITE;
+  return FFTJ_OK;
+}
+
 // complex 1-D transform of length n (batch at idist/odist) appended to ops;
 // if load_op != PLAIN, the first pass uses it with the given parameters.
 template <typename T>
@@ -1136,6 +1216,13 @@ int build_c2c_1d(fftj_plan_s* P, i64 n, i64 batch, i64 idist, i64 odist, int dir
     *route = tmp.size() > 1 ? FFTJ_ROUTE_FOURSTEP : FFTJ_ROUTE_DIRECT;
     for (auto& o : tmp) ops->push_back(o);
     return FFTJ_OK;
+  }
+  // FFTJ's _anyplan tries CompositePlan first (src/plan.jl:196)
+  if (!g_tables.rs && use_composite(sizeof(T) == 8, n)) {
+    const size_t mark = ops->size();
+    const int rc = build_c2c_composite<T>(P, n, batch, idist, odist, dir, scale, ops, route);
+    if (rc == FFTJ_OK) return rc;
+    ops->resize(mark);  // fall back to the next route
   }
   // odd non-smooth lengths FFTJ sends to Gaussian resampling (HvdH)
   const bool hv_ok = !g_tables.rs && (g_sched.route == 2 ? (n % 2 == 1 && n >= 64)

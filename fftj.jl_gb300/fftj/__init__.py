@@ -41,7 +41,8 @@ class DimensionMismatch(ValueError):
     """FFTJ's DimensionMismatch (array sizes do not match the plan)."""
 
 
-ROUTES = {0: "FFTPlan", 1: "FourStepPlan", 2: "ResamplePlan", 3: "HvdhPlan", 4: "NdPlan", 5: "SplitPlan"}
+ROUTES = {0: "FFTPlan", 1: "FourStepPlan", 2: "ResamplePlan", 3: "HvdhPlan", 4: "NdPlan", 5: "SplitPlan",
+          6: "CompositePlan"}
 
 
 class PlanInfo(ctypes.Structure):

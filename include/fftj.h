@@ -52,7 +52,8 @@ typedef enum {
   FFTJ_ROUTE_RESAMPLE = 2,  /* ResamplePlan: non-smooth length */
   FFTJ_ROUTE_HVDH = 3,      /* HvdhPlan */
   FFTJ_ROUTE_ND = 4,        /* NdPlan / RfftNdPlan / IrfftNdPlan */
-  FFTJ_ROUTE_SPLIT = 5      /* SplitPlan / CompositePlan: n = s p, s 7-smooth, p by Gaussian resampling */
+  FFTJ_ROUTE_SPLIT = 5,     /* SplitPlan: n = s p, s 7-smooth, decimation in time, p by Gaussian resampling */
+  FFTJ_ROUTE_COMPOSITE = 6  /* CompositePlan: n = p s, decimation in frequency, p along s lanes by HvPass / RsPass */
 } fftj_route;
 
 typedef struct {
@@ -91,8 +92,9 @@ typedef struct {
   int32_t order;         /* k-th lexicographic permutation of the pass radices (0 = largest first) */
   int32_t tf_mult;       /* threads per transform column = the minimum x tf_mult (0/1 = minimum) */
   int32_t route;         /* non-smooth lengths: 0 planner, 1 resampling, 2 Gaussian (HvdH; even lengths
-                            by the split route); any length: 3 Gaussian resampling at full length, as
-                            FFTJ._hvdh (FFTJ_ERR_ARG when no smooth t is coprime to n) */
+                            by the split route), 4 CompositePlan (any 7-smooth part >= 2); any length:
+                            3 Gaussian resampling at full length, as FFTJ._hvdh (FFTJ_ERR_ARG when no
+                            smooth t is coprime to n) */
   int32_t threads_max;   /* cap on threads per CTA (0 = 512 F32 / 256 F64) */
   int32_t dry;           /* 1: plan the schedule only (no tables, no workspace, cannot execute) */
   int32_t precision;     /* F32 radix-16 sub-stages: 0 FP32 butterflies, 1 FP16 hi+lo tensor-core GEMM,

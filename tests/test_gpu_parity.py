@@ -466,15 +466,14 @@ def test_odd_radix_lengths_that_need_two_passes(fftj, orc, T, n):
     assert rel_l2(xi, x) <= 2 * parity_tol(T, n)
 
 
-@pytest.mark.parametrize("T,n,B", [(np.float64, 2 * 10007, 2), (np.float64, 6 * 3001, 3), (np.float64, 16 * 509, 4),
-                                   (np.float64, 30 * 4099, 1), (np.float64, 1024 * 1009, 1),
-                                   (np.float32, 4 * 32771, 2), (np.float32, 64 * 1031, 1)])
+@pytest.mark.parametrize("T,n,B", [(np.float64, 2 * 10007, 2), (np.float64, 6 * 3001, 3),
+                                   (np.float32, 4 * 32771, 2)])
 def test_split_route(fftj, orc, T, n, B):
-    """Even non-smooth lengths n = s p (s 7-smooth, p odd and Gaussian-
-    resampled): decimation, s HvdH sub-transforms with the w_n^(r k1)
-    twiddles in their banded solve, length-s passes along r (FFTJ
-    SplitPlan / CompositePlan mathematics). Forward against FP64 numpy,
-    normalised inverse round trip."""
+    """Even non-smooth lengths n = s p with a small 7-smooth part (s < 16,
+    p odd and Gaussian-resampled; FFTJ SplitPlan): decimation, s HvdH
+    sub-transforms with the w_n^(r k1) twiddles in their banded solve,
+    length-s passes along r. Forward against FP64 numpy and the oracle's
+    SplitPlan, normalised inverse round trip."""
     p = fftj.plan_fft(T, n, batch=B)
     assert p.route == "SplitPlan", p.route
     rng = np.random.default_rng(n)
@@ -482,13 +481,57 @@ def test_split_route(fftj, orc, T, n, B):
     y = p(dev(x, T))
     tol = parity_tol(T, n)
     assert rel_l2(host(y), np.fft.fft(x, axis=-1)) <= tol
-    # the FFTJ CPU plan FFTJ routes this length to: CompositePlan (s >= 16)
-    # or SplitPlan (s < 16), restated in the oracle (src/composite.jl)
     po = orc.Plan1D(T, n, "fft")
-    assert po.route in ("CompositePlan", "SplitPlan"), po.route
+    assert po.route == "SplitPlan", po.route
     assert rel_l2(host(y).reshape(B, n)[:1], po(x[:1])) <= tol
     xi = host(fftj.plan_ifft(T, n, batch=B)(y))
     assert rel_l2(xi, x) <= 2 * tol
+
+
+@pytest.mark.parametrize("T,n,B", [(np.float64, 16 * 509, 4), (np.float64, 27 * 509, 2), (np.float64, 30 * 4099, 1),
+                                   (np.float64, 1024 * 1009, 1), (np.float64, 32 * 131, 3),
+                                   (np.float32, 64 * 1031, 2), (np.float32, 256 * 257, 2)])
+def test_composite_route(fftj, orc, T, n, B):
+    """FFTJ's CompositePlan lengths (7-smooth part s >= 16, src/composite.jl:
+    10-101): s-part passes along p lanes, the twiddled transpose, the odd part
+    p along rows of s lanes by the batched HvPass (p >= 500) or RsPass.
+    Forward against FP64 numpy and the oracle's CompositePlan, normalised
+    inverse round trip, both solve factor forms for HvPass."""
+    p = fftj.plan_fft(T, n, batch=B)
+    assert p.route == "CompositePlan", p.route
+    rng = np.random.default_rng([n, 6])
+    x = rng.standard_normal((B, n)) + 1j * rng.standard_normal((B, n))
+    y = p(dev(x, T))
+    tol = parity_tol(T, n)
+    assert rel_l2(host(y), np.fft.fft(x, axis=-1)) <= tol
+    po = orc.Plan1D(T, n, "fft")
+    assert po.route == "CompositePlan", po.route
+    assert rel_l2(host(y).reshape(B, n)[:2], po(x[:2])) <= tol
+    xi = host(fftj.plan_ifft(T, n, batch=B)(y))
+    assert rel_l2(xi, x) <= 2 * tol
+    if n // 1024 >= 500 or n in (16 * 509, 27 * 509, 30 * 4099, 64 * 1031):
+        pf = fftj.Plan(T, (n,), kind="c2c", batch=B, opts={"hvdh_factors": 2})
+        assert pf.route == "CompositePlan"
+        assert rel_l2(host(pf(dev(x, T))), host(y)) <= tol
+
+
+@pytest.mark.parametrize("T", T_LIST)
+@pytest.mark.parametrize("n", [16 * 509, 3 * 1009, 12 * 97])
+def test_composite_forced(fftj, orc, T, n):
+    """opts.route = 4: CompositePlan below FFTJ's size thresholds (odd and
+    small smooth parts, HvPass and RsPass), against the oracle's
+    FFTJ._composite restatement and FP64 numpy, both directions."""
+    B = 3
+    rng = np.random.default_rng([n, 4])
+    x = cn(rng, (B, n))
+    tol = parity_tol(T, n)
+    pf = fftj.Plan(T, (n,), kind="c2c", batch=B, opts={"route": 4})
+    assert pf.route == "CompositePlan"
+    y = host(pf(dev(x, T)))
+    assert rel_l2(y, np.fft.fft(x, axis=-1)) <= tol
+    assert rel_l2(y, orc.PlanDirect(T, n, "composite")(x)) <= tol
+    pb = fftj.Plan(T, (n,), kind="c2c", batch=B, direction=1, scale=1.0 / n, opts={"route": 4})
+    assert rel_l2(host(pb(dev(y, T))), x) <= 2 * tol
 
 
 # FFTJ's HvdH test sizes (test/runtests.jl:110-137), the route forced to

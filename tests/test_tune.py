@@ -154,13 +154,30 @@ def test_strided_4096_axis_plans_one_pass(T):
     assert list(wide(np.float32, (4096, 4096), precision=1).pass_radix[:3]) == [4096, 64, 64]
 
 
+def test_composite_route_choice(T):
+    """FFTJ's _anyplan takes CompositePlan first for non-smooth n with a
+    7-smooth part s >= 16 and n >= 4096 F64 / 32768 F32 (odd n included):
+    s-part passes, the twiddled transpose (a copy op), then the p-part by
+    HvPass (p >= 500: spread pass + t passes + solve) or RsPass (deconvolving
+    pass + m passes + interpolation); opts.route = 4 forces it."""
+    hv = info(T, "c2c", np.float64, 16 * 509)
+    assert hv.route == 6 and list(hv.pass_radix[:3]) == [16, 24, 24]  # t = 576 = 24 * 24
+    assert info(T, "c2c", np.float64, 27 * 509).route == 6            # odd n: composite before HvdH
+    rs = info(T, "c2c", np.float64, 32 * 131)
+    assert rs.route == 6 and list(rs.pass_radix[:2]) == [32, 270]     # RsPass: m = nextsmooth7(262)
+    assert info(T, "c2c", np.float32, 64 * 1031).route == 6
+    assert info(T, "c2c", np.float32, 16 * 509).route == 2            # F32 below 32768: resampling
+    assert info(T, "c2c", np.float32, 16 * 509, route=4).route == 6   # forced
+    assert info(T, "c2c", np.float64, 2 * 10007).route == 5           # s < 16: SplitPlan
+
+
 def test_split_route_choice(T):
     """Even non-smooth lengths take the split route when their odd part is
     one FFTJ would Gaussian-resample (F64 >= 1000, F32 >= 16384), else
     full-length resampling; the route knob forces either."""
     assert info(T, "c2c", np.float64, 2 * 10007).route == 5
     assert info(T, "c2c", np.float64, 10006).route == 2               # n < 16384: resampling, as FFTJ
-    assert info(T, "c2c", np.float64, 16 * 509).route == 5            # s >= 16: FFTJ's composite lengths
+    assert info(T, "c2c", np.float64, 16 * 509).route == 6            # s >= 16: CompositePlan, as FFTJ
     assert info(T, "c2c", np.float32, 2 * 10007).route == 2          # odd part below the F32 threshold
     assert info(T, "c2c", np.float32, 4 * 32771).route == 5
     assert info(T, "c2c", np.float64, 2 * 10007, route=1).route == 2  # forced resampling
