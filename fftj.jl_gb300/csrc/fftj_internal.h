@@ -170,6 +170,7 @@ struct RecipeEntry {
   int Tf;        // threads per tile column the kernel was built for
   int nb;        // tile columns the kernel was built for (0: any)
   const void* fn;
+  int tc = 0;    // precision form of the kernel (1: FP16 hi + lo tensor-core first sub-stage), 0 plain
 };
 template <typename T, int DIR>
 const RecipeEntry* recipe_table(int* count);
@@ -177,6 +178,8 @@ const RecipeEntry* recipe_table(int* count);
 // = the exact tile column count). Signature:
 // (PassParams, CUtensorMap, const float2* in, float2* out, unsigned* status).
 const RecipeEntry* tma_table(int dir, int* count);
+// Their precision-form variants (tc = 1), same signature.
+const RecipeEntry* tma_tc_table(int* count);
 size_t tma_smem_bytes(const PassParams& pp);
 int tma_prepare(const void* fn, const PassParams& pp);
 cudaError_t tma_launch(const void* fn, const PassParams& pp, const CUtensorMap& map, const void* in, void* out,

@@ -29,6 +29,7 @@
 #include <cuda.h>
 
 #include "pass_common.cuh"
+#include "umma.cuh"
 
 namespace fftj {
 
@@ -89,6 +90,136 @@ __device__ __forceinline__ void tma_load4(void* dst, const CUtensorMap* map, uin
       : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Precision form on the fifth-generation tensor cores: a radix-16 sub-stage
+// as the GEMM Y = X C^T per 128 butterflies (rows), in real form: a row of
+// A holds a butterfly's 16 inputs (real parts, then imaginary parts), a row
+// of B one of the 32 real outputs (Yr[n] = Cr Xr - Ci Xi, Yi[n] = Ci Xr + Cr
+// Xi, C = w_16^(n j)). Operands are FP16 hi + lo: each butterfly is scaled
+// by a power of two so that its largest component is below 1, split into hi
+// = fp16(x) and lo = fp16((x - hi) 2^11) (lo stays a normal number), and
+// likewise the DFT matrix; D1 = A_hi B_hi^T and D2 = A_hi B_lo^T + A_lo
+// B_hi^T accumulate in FP32 in tensor memory (lo * lo dropped), and Y = (D1
+// + D2 2^-11) unscaled. Same arithmetic as the legacy mma.sync form, on
+// tcgen05.mma (M = 128, N = 32, K = 16 per instruction; one thread issues,
+// completion on an mbarrier, accumulators read back with tcgen05.ld).
+
+// B operands: the real-form DFT hi at tcB, scaled lo at tcB + 2048 (32 rows
+// x 32 halves each, core matrices 128 bytes apart along K, row groups 512)
+template <int DIR>
+__device__ __forceinline__ void tc16_b_operand(unsigned char* tcB, int tid, int nthr) {
+  for (int e = tid; e < 32 * 16; e += nthr) {
+    const int n = e >> 4, k2 = (e & 15) * 2;  // row n, columns k2 and k2 + 1
+    float val[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = k2 + h;
+      const int yo = n & 15, xi = k & 15;  // output and input points
+      float sn, cs;
+      sincospif((float)((yo * xi) & 15) * 0.125f, &sn, &cs);
+      const float cr = cs, ci = DIR * sn;
+      // rows 0..15: Yr = Cr Xr - Ci Xi; rows 16..31: Yi = Ci Xr + Cr Xi
+      val[h] = n < 16 ? (k < 16 ? cr : -ci) : (k < 16 ? ci : cr);
+    }
+    uint32_t hi, lo;
+    split_pair<1>(val[0], val[1], hi, lo);
+    const int off = (n >> 3) * 512 + (k2 >> 3) * 128 + (n & 7) * 16 + (k2 & 7) * 2;
+    *reinterpret_cast<uint32_t*>(tcB + off) = hi;
+    *reinterpret_cast<uint32_t*>(tcB + 2048 + off) = lo;
+  }
+}
+
+// The first sub-stage (radix 16, S = 1) of a pipelined tile on the tensor
+// cores: thread tid's butterfly (column c, k) is row tid of the GEMM. Reads
+// the dense tile, writes the outputs (twiddled by w_R^(j k) in FP32) to the
+// padded layout as the FP32 sub-stage does. False when the MMAs did not
+// complete within the wait limit.
+template <int DIR, int MODE, int NBC, int R, int Rr, int nthr>
+__device__ __forceinline__ bool tc16_first(Cx<float>* buf, const Cx<float>* tw, unsigned char* tcA,
+                                           unsigned char* tcB, uint64_t* tcbar, uint32_t tmem, uint32_t par,
+                                           int tid, int b, int kg, uint64_t limit) {
+  using T = float;
+  using L = LayC<T, NBC>;
+  constexpr int NB = NBC, r0 = 16;
+  const int c = MODE == 0 ? tid / Rr : b;
+  const int k = MODE == 0 ? tid - c * Rr : kg;
+  const Cx<T>* src = MODE == 0 ? buf + c * R + k : buf + k * NB + b;
+  constexpr int js = MODE == 0 ? Rr : Rr * NB;
+  float xr[16], xi[16];
+  float mx = 0.f;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const Cx<T> v = src[j * js];
+    xr[j] = v.x;
+    xi[j] = v.y;
+    mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+  }
+  int ex = 0;
+  if (mx > 0.f) frexpf(mx, &ex);  // mx < 2^ex
+  const float sc = ldexpf(1.f, -ex);
+  // row tid of A: halves [xr hi 0..15 | xi hi | xr lo | xi lo], as 8 core
+  // rows of 16 bytes (row group (tid mod 128) / 8 of block tid / 128)
+  uint32_t hw[32];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    split_pair<1>(xr[2 * j] * sc, xr[2 * j + 1] * sc, hw[j], hw[16 + j]);
+    split_pair<1>(xi[2 * j] * sc, xi[2 * j + 1] * sc, hw[8 + j], hw[24 + j]);
+  }
+  unsigned char* arow = tcA + (tid >> 7) * 16384 + ((tid & 127) >> 3) * 1024 + (tid & 7) * 16;
+#pragma unroll
+  for (int kc = 0; kc < 8; ++kc)
+    *reinterpret_cast<uint4*>(arow + kc * 128) = make_uint4(hw[4 * kc], hw[4 * kc + 1], hw[4 * kc + 2], hw[4 * kc + 3]);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // A visible to the tensor cores
+  __syncthreads();  // every input is read and every A row written
+  if (tid == 0) {
+    tc_fence_after();
+    constexpr uint32_t kId = umma_idesc_f16(128, 32, 0);
+    const uint32_t bhi = sh_addr(tcB), blo = bhi + 2048;
+#pragma unroll 1
+    for (int blk = 0; blk < nthr / 128; ++blk) {
+      const uint32_t a0 = sh_addr(tcA) + blk * 16384;
+      const uint32_t d1 = tmem + blk * 64, d2 = d1 + 32;
+      umma_f16(d1, umma_desc(a0, 128, 1024), umma_desc(bhi, 128, 512), kId, false);
+      umma_f16(d1, umma_desc(a0 + 256, 128, 1024), umma_desc(bhi + 256, 128, 512), kId, true);
+      umma_f16(d2, umma_desc(a0, 128, 1024), umma_desc(blo, 128, 512), kId, false);
+      umma_f16(d2, umma_desc(a0 + 256, 128, 1024), umma_desc(blo + 256, 128, 512), kId, true);
+      umma_f16(d2, umma_desc(a0 + 512, 128, 1024), umma_desc(bhi, 128, 512), kId, true);
+      umma_f16(d2, umma_desc(a0 + 768, 128, 1024), umma_desc(bhi + 256, 128, 512), kId, true);
+    }
+    umma_commit(tcbar);
+  }
+  const bool ok = mbar_wait(tcbar, par, limit);
+  if (__syncthreads_or(!ok)) return false;  // every thread leaves together
+  tc_fence_after();
+  // row tid = lane 32 (w mod 4) + lane of block w / 4 (warp w)
+  const int warp = tid >> 5;
+  const uint32_t ta = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(warp >> 2) * 64;
+  float y[32];
+  tmem_ld32(ta, y);
+  constexpr float kInvLo = 1.f / lo_scale<1>();
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float l[8];
+    tmem_ld8(ta + 32 + 8 * q, l);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[8 * q + i] = fmaf(l[i], kInvLo, y[8 * q + i]);
+  }
+  const float us = ldexpf(1.f, ex);
+  constexpr bool kLay = L::exact(r0);
+  const int a = r0 * k * NB + c;
+  const int base = kLay ? L::row(r0 * k) + L::col(c) : pidx<T>(a);
+  buf[base] = mk<T>(y[0] * us, y[16] * us);
+#pragma unroll
+  for (int j = 1; j < r0; ++j) {
+    Cx<T> w = mk<T>(y[j] * us, y[16 + j] * us);
+    if (k != 0) w = cmul(w, tw[j * k]);
+    buf[kLay ? base + L::step(j) : pidx<T>(a + j * NB)] = w;
+  }
+  tc_fence_before();
+  __syncthreads();
+  return true;
+}
+
 // MODE 0: tile = NB whole contiguous transforms (batch entries), one 1-D
 // bulk copy per entry; MODE 1: tile = P consecutive columns p (Q == 1, one
 // batch entry), tensor (p, j, batch); MODE 2: tile = Q consecutive columns q
@@ -99,7 +230,10 @@ __device__ __forceinline__ void tma_load4(void* dst, const CUtensorMap* map, uin
 template <int R>
 __host__ __device__ constexpr bool tma_stages_twiddles() { return R <= 4096; }
 
-template <int DIR, int MODE, int NBC, int... Rs>
+// TC = 1: the precision form (FP16 hi + lo operands): the first sub-stage,
+// radix 16 with one butterfly per thread, runs on the tensor cores as one
+// tcgen05 GEMM per 128 butterflies (tc16_first below).
+template <int DIR, int MODE, int NBC, int TC, int... Rs>
 __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap* map, const Cx<float>* in,
                                          Cx<float>* __restrict__ out, unsigned* status) {
   using T = float;
@@ -115,6 +249,10 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
   constexpr uint32_t kTx = (uint32_t)(NB * R * sizeof(Cx<T>));
   static_assert(NS >= 2, "the first and last sub-stages are separate");
   static_assert(MODE != 0 || Rr % TF == 0, "single-pass tiles: whole butterfly rounds per thread");
+  constexpr bool kTc = TC != 0;
+  static_assert(!kTc || (r0 == 16 && IPT == 1 && Rr == TF && nthr % 128 == 0),
+                "tensor-core first sub-stage: radix 16, one butterfly per thread, whole 128-thread blocks");
+  constexpr uint32_t kTcCols = (uint32_t)(nthr / 128) * 64;  // D1 and D2, 32 columns each, per 128 rows
   // box copies land 16-byte aligned: dynamic shared memory starts 16-byte
   // aligned and buffers are multiples of 128 bytes
   extern __shared__ __align__(16) unsigned char tma_smem[];
@@ -127,6 +265,12 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
   const int tid = threadIdx.x;
   const int kg = tid / NB;
   const int b = tid - kg * NB;
+  // tensor-core operands after the kernel's own shared memory
+  unsigned char* const tcA =
+      tma_smem + tc_smem_offset((size_t)(2 * bufE + (kStageTw ? R : 0)) * sizeof(Cx<T>) + 3 * sizeof(uint64_t));
+  unsigned char* const tcB = tcA + nthr * 128;
+  uint64_t* const tcbar = reinterpret_cast<uint64_t*>(tcB + 4096);
+  uint32_t* const tmem_slot = reinterpret_cast<uint32_t*>(tcbar + 1);
   const uint32_t ntiles = pp.tiles_q * pp.tiles_p * pp.tiles_b;
   const int rows = pp.tma_rows;
   const uint64_t limit = pp.tma_wait_ns;
@@ -139,15 +283,35 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
   // and waited on after each slot's barrier, so every tile wait times out
   // while the slot barriers still see their copies land
   const uint32_t extra_tx = (uint32_t)pp.tma_extra_tx;
+  if constexpr (kTc) tc16_b_operand<DIR>(tcB, tid, nthr);
   if (tid == 0) {
     mbar_init(bar, 1);
     mbar_init(bar + 1, 1);
     mbar_init(bar + 2, 1);
+    if constexpr (kTc) mbar_init(tcbar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (extra_tx) mbar_arrive_expect_tx(bar + 2, extra_tx);
   }
+  if constexpr (kTc) {
+    if (tid < 32) tmem_alloc(tmem_slot, kTcCols);
+    tc_fence_before();
+  }
   __syncthreads();
+  uint32_t tmem = 0, tc_par = 0;
+  if constexpr (kTc) {
+    tc_fence_after();
+    tmem = *tmem_slot;
+  }
+  // tensor memory back before any exit (every thread; warp 0 allocated it)
+  auto tc_release = [&]() {
+    if constexpr (kTc) {
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+      if (tid < 32) tmem_dealloc(tmem, kTcCols);
+    }
+  };
   // one thread arms the slot's barrier with the tile's bytes and issues the
   // tile's box copies (R / rows boxes of NB x rows elements)
   auto issue = [&](uint32_t tile, int slot) {
@@ -196,6 +360,7 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
         if (!drained) atomicOr(status, 2u);  // copies still in flight at exit
       }
       __syncthreads();
+      tc_release();
       return;
     }
     const uint32_t t1 = pp.ftq.div(tile);
@@ -212,6 +377,22 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
     // butterfly (column c, k): MODE 0 takes k fastest across lanes (entries
     // are rows [c][j] of the dense tile), modes 1 and 2 the column (rows
     // [j][c]); both read consecutive addresses across a warp
+    if constexpr (kTc) {
+      const bool tok = tc16_first<DIR, MODE, NBC, R, Rr, nthr>(buf, tw, tcA, tcB, tcbar, tmem, tc_par, tid, b, kg,
+                                                               limit);
+      tc_par ^= 1u;
+      if (!tok) {  // uniform: decided by a block-wide vote
+        // the MMAs did not complete: record it, drain the next tile's copy
+        // (bounded) and leave
+        if (tid == 0) {
+          atomicOr(status, 1u);
+          if (nxt < ntiles && !mbar_wait(bar + (slot ^ 1), ((it + 1) >> 1) & 1, limit)) atomicOr(status, 2u);
+        }
+        __syncthreads();
+        tc_release();
+        return;
+      }
+    } else {
     Cx<T> v[IPT][r0];
 #pragma unroll
     for (int i = 0; i < IPT; ++i) {
@@ -246,19 +427,21 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
       }
     }
     __syncthreads();
+    }
     if constexpr (NS > 2) run_mid_ct<T, DIR, TF, R, r0, 1, NBC, Rs...>(buf, b, kg, NB, tw);
     store_last<T, DIR, MODE, NBC, Rs...>(pp, out, buf, tid, nthr, kg, b, b0, p0, q0, ql, b0, pcol, colok);
     __syncthreads();  // the buffer is free for the copy after next
   }
+  tc_release();
 }
 
-template <int DIR, int MODE, int NBC, class Rec>
+template <int DIR, int MODE, int NBC, class Rec, int TC = 0>
 struct TmaLaunch;
-template <int DIR, int MODE, int NBC, int... Rs>
-struct TmaLaunch<DIR, MODE, NBC, Recipe<Rs...>> {
+template <int DIR, int MODE, int NBC, int TC, int... Rs>
+struct TmaLaunch<DIR, MODE, NBC, Recipe<Rs...>, TC> {
   __device__ __forceinline__ static void run(const PassParams& pp, const CUtensorMap* map, const Cx<float>* in,
                                              Cx<float>* out, unsigned* status) {
-    pass_tma<DIR, MODE, NBC, Rs...>(pp, map, in, out, status);
+    pass_tma<DIR, MODE, NBC, TC, Rs...>(pp, map, in, out, status);
   }
 };
 

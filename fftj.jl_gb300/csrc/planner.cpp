@@ -1652,12 +1652,15 @@ void pick_tma(Op& op, bool dry) {
   if (pp.m == 1 && pp.nsub == 2 && cols * 8 <= 128) return;
   if (mode && (mode == 1 ? pp.m : pp.s) % 2) return;
   if (pp.nbatch > 1 && (pp.in_bstride % 2 || pp.in_bstride < pp.ncur)) return;
+  // the precision form (FP16 hi + lo) has tensor-core variants of these
+  // kernels; its BF16 form keeps the run-time kernel
+  if (pp.tc > 1) return;
   int count = 0;
-  const RecipeEntry* tab = tma_table(op.dir, &count);
+  const RecipeEntry* tab = pp.tc ? tma_tc_table(&count) : tma_table(op.dir, &count);
   const void* fn = nullptr;
   for (int i = 0; i < count && !fn; ++i) {
     const RecipeEntry& e = tab[i];
-    if (e.dir != op.dir || e.mode != mode || e.nb != pp.NB || e.Tf != pp.Tf) continue;
+    if (e.dir != op.dir || e.mode != mode || e.nb != pp.NB || e.Tf != pp.Tf || e.tc != pp.tc) continue;
     int n = 0;
     while (n < 6 && e.radix[n]) n++;
     bool same = n == pp.nsub;
@@ -1745,7 +1748,7 @@ int finalize_passes(fftj_plan_s* P) {
       }
     }
     op.pp.smem_tw_elems = stage_inner_twiddles(op.pp, op.kfn != nullptr) ? op.pp.R : 0;
-    if (sizeof(T) == 4 && op.kfn && !op.pp.tc && !P->plain_loads) pick_tma(op, P->dry);
+    if (sizeof(T) == 4 && (op.kfn || op.pp.tc == 1) && !P->plain_loads) pick_tma(op, P->dry);
     any_tma = any_tma || op.kfn_tma != nullptr;
     if (P->dry) continue;
     if (prepare_pass<T>(op.pp, op.dir, op.kfn) != cudaSuccess) return fail(FFTJ_ERR_CUDA, "cudaFuncSetAttribute failed");
@@ -2092,8 +2095,16 @@ int fftj_plan_get_info(fftj_plan plan, fftj_plan_info_t* info) {
       const PassParams& pp = op.pp;
       if (op.kfn) info->specialized_passes++;
       info->fx_passes += pp.fx ? 1 : 0;
-      if (pp.tc)
-        for (int i = 0; i < pp.nsub; ++i) info->tc_substages += tc16_substage_fits(pp, i) ? 1 : 0;
+      if (pp.tc) {
+        // the pipelined precision-form kernel runs its first sub-stage on
+        // the tensor cores; the run-time kernel every radix-16 sub-stage
+        // that fits
+        if (op.kfn_tma) {
+          info->tc_substages += 1;
+        } else {
+          for (int i = 0; i < pp.nsub; ++i) info->tc_substages += tc16_substage_fits(pp, i) ? 1 : 0;
+        }
+      }
       if (pi < 8) {
         info->pass_tile[pi] = pp.NB * pp.R;
         info->pass_threads[pi] = pp.threads;

@@ -38,7 +38,9 @@ const RecipeEntry* tma_table(int dir, int* count) {
 
 size_t tma_smem_bytes(const PassParams& pp) {
   const int tw = pp.R <= 4096 ? pp.R : 0;  // tma_stages_twiddles
-  return (size_t)(2 * pp.tma_buf + tw) * sizeof(Cx<float>) + 3 * sizeof(uint64_t);  // 3 mbarriers
+  const size_t own = (size_t)(2 * pp.tma_buf + tw) * sizeof(Cx<float>) + 3 * sizeof(uint64_t);  // 3 mbarriers
+  // the precision form's tensor-core operands follow (umma.cuh)
+  return pp.tc == 1 ? tc_smem_offset(own) + tc_smem_bytes(pp.threads) : own;
 }
 
 // Opts the kernel into the shared memory it needs and returns how many CTAs

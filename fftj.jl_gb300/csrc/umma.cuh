@@ -1,0 +1,107 @@
+// tcgen05 (fifth-generation tensor core) building blocks: tensor-memory
+// allocation, the shared-memory matrix descriptor of a no-swizzle K-major
+// operand, the kind::f16 instruction descriptor, MMA issue, commit to an
+// mbarrier and tensor-memory loads.
+//
+// Operand layout (no swizzle, K-major): a matrix is tiled into core
+// matrices of 8 rows x 16 bytes (8 halves along K, rows 16 bytes apart);
+// the descriptor's leading byte offset (LBO) is the distance between core
+// matrices adjacent along K and its stride byte offset (SBO) the distance
+// between adjacent 8-row groups. These conventions, the instruction
+// descriptor (D format at bit 4, A/B formats at bits 7/10, N >> 3 at bit 17,
+// M >> 4 at bit 24) and the 32x32b load's row mapping (warp w of a
+// warpgroup reads accumulator rows 32 (w mod 4) ..) were checked on a GB300
+// with exact small-integer GEMMs for FP16 and BF16 operands.
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace fftj {
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of the fifth-generation tensor core
+  return d;                // base offset 0, no swizzle
+}
+
+// kind::f16 instruction descriptor: FP32 accumulator, FP16 (bf16 = 0) or
+// BF16 (bf16 = 1) A and B, both K-major, M x N
+__host__ __device__ constexpr uint32_t umma_idesc_f16(int M, int N, int bf16) {
+  return (1u << 4) | ((uint32_t)bf16 << 7) | ((uint32_t)bf16 << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+// D (tensor memory) = A B^T (+ D when acc), A and B from shared memory
+__device__ __forceinline__ void umma_f16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         bool acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(acc ? 1u : 0u)
+      : "memory");
+}
+
+// the mbarrier gets one arrival when every MMA this thread issued is done
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(bar))
+               : "memory");
+}
+
+// warp-wide: ncols (a power of two >= 32) tensor-memory columns; the base
+// address is written to *slot
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(slot)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive accumulator columns of this thread's row (32x32b.x32),
+// waited for in the same statement
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared memory of the precision form's tensor-core sub-stage in a
+// pipelined pass, after the kernel's own (offset rounded up to 128 bytes):
+// the A operand (one 128-byte row of 64 halves per thread: 16 real hi, 16
+// imaginary hi, 16 real lo, 16 imaginary lo), B = the radix-16 DFT in real
+// form, hi and scaled lo (32 x 32 halves each), an mbarrier and the
+// tensor-memory address.
+__host__ __device__ constexpr size_t tc_smem_offset(size_t own) { return (own + 127) / 128 * 128; }
+__host__ __device__ constexpr size_t tc_smem_bytes(int nthr) { return (size_t)nthr * 128 + 4096 + 16; }
+
+}  // namespace fftj

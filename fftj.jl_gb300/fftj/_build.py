@@ -14,7 +14,7 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD = os.path.join(PKG_DIR, "_build")
 LIB = os.path.join(PKG_DIR, "libfftj_gb300.so")
 SOURCES = ["kernels.cu", "recipes_f32_fwd.cu", "recipes_f32_bwd.cu", "recipes_f64_fwd.cu",
-           "recipes_f64_bwd.cu", "tma_f32.cu", "noalloc.cu", "mlp.cu", "group.cu", "planner.cpp", "tune.cpp"]
+           "recipes_f64_bwd.cu", "tma_f32.cu", "tma_tc_f32.cu", "noalloc.cu", "mlp.cu", "group.cu", "planner.cpp", "tune.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
