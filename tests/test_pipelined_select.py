@@ -60,8 +60,16 @@ def test_pipelined_pass_selection(F, kind, dtype, dims, batch, want):
 def test_options_turn_the_pipeline_off(F):
     assert dry_info(F, "c2c", np.float32, (1 << 20,), 2).tma_passes == 2
     assert dry_info(F, "c2c", np.float32, (1 << 20,), 2, plain_loads=1).tma_passes == 0
-    # the precision form's tensor-core sub-stages run in the run-time-radix kernel
-    assert dry_info(F, "c2c", np.float32, (1 << 20,), 2, precision=1).tma_passes == 0
+    # the FP16 precision form runs in the pipelined kernels' tensor-core
+    # variants (first sub-stage radix 16 on tcgen05); BF16 and plain_loads
+    # keep the run-time-radix kernel
+    fp16 = dry_info(F, "c2c", np.float32, (1 << 20,), 2, precision=1)
+    assert fp16.tma_passes == 2 and fp16.tc_substages == 2
+    assert dry_info(F, "c2c", np.float32, (1 << 20,), 2, precision=2).tma_passes == 0
+    assert dry_info(F, "c2c", np.float32, (1 << 20,), 2, precision=1, plain_loads=1).tma_passes == 0
+    # passes without a radix-16 first sub-stage keep the plain pipelined kernel
+    rows = dry_info(F, "c2c", np.float32, (4096, 4096), 1, precision=1)
+    assert rows.tma_passes == 3 and rows.tc_substages == 1
 
 
 def test_schedule_hash_tells_the_kernels_apart(F):
