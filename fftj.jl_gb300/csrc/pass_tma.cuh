@@ -92,52 +92,62 @@ __device__ __forceinline__ void tma_load4(void* dst, const CUtensorMap* map, uin
 
 // ---------------------------------------------------------------------------
 // Precision form on the fifth-generation tensor cores: a radix-16 sub-stage
-// as the GEMM Y = X C^T per 128 butterflies (rows), in real form: a row of
-// A holds a butterfly's 16 inputs (real parts, then imaginary parts), a row
-// of B one of the 32 real outputs (Yr[n] = Cr Xr - Ci Xi, Yi[n] = Ci Xr + Cr
-// Xi, C = w_16^(n j)). Operands are FP16 hi + lo: each butterfly is scaled
-// by a power of two so that its largest component is below 1, split into hi
-// = fp16(x) and lo = fp16((x - hi) 2^11) (lo stays a normal number), and
-// likewise the DFT matrix; D1 = A_hi B_hi^T and D2 = A_hi B_lo^T + A_lo
-// B_hi^T accumulate in FP32 in tensor memory (lo * lo dropped), and Y = (D1
-// + D2 2^-11) unscaled. Same arithmetic as the legacy mma.sync form, on
-// tcgen05.mma (M = 128, N = 32, K = 16 per instruction; one thread issues,
-// completion on an mbarrier, accumulators read back with tcgen05.ld).
+// as the GEMM Y = X C^T per 128 butterflies (rows), in real form. Operands
+// are FP16 hi + lo: each butterfly is scaled by a power of two so that its
+// largest component is below 1, split into hi = fp16(x) and lo = fp16((x -
+// hi) 2^11) (lo stays a normal number), and likewise the DFT matrix. A row
+// of A holds a butterfly's 64 halves [Xr hi | Xi hi | Xr lo | Xi lo]; B has
+// 64 rows: rows 0..31 [C hi | 0] give D1 = A_hi C_hi^T, rows 32..63 [C lo |
+// C hi] give D2 = A_hi C_lo^T + A_lo C_hi^T (lo * lo dropped), where the 32
+// rows of C are the real outputs Yr[n] = Cr Xr - Ci Xi and Yi[n] = Ci Xr +
+// Cr Xi, C = w_16^(n j). One accumulator of 64 FP32 columns per block in
+// tensor memory, four tcgen05.mma (M = 128, N = 64, K = 16) issued by one
+// thread, completion on an mbarrier, read back with tcgen05.ld; Y = (D1 +
+// D2 2^-11) unscaled. Same arithmetic as the legacy mma.sync form.
+//
+// A lives in the tile buffer itself: a butterfly's 16 FP32 inputs are 128
+// bytes, as is its row of A, so once every thread holds its inputs in
+// registers the tile's bytes become A, and once every MMA is done they take
+// the sub-stage's outputs.
 
-// B operands: the real-form DFT hi at tcB, scaled lo at tcB + 2048 (32 rows
-// x 32 halves each, core matrices 128 bytes apart along K, row groups 512)
+// B operand (64 rows x 64 halves, core matrices 128 bytes apart along K,
+// 8-row groups 1024 bytes apart) at tcB
 template <int DIR>
 __device__ __forceinline__ void tc16_b_operand(unsigned char* tcB, int tid, int nthr) {
-  for (int e = tid; e < 32 * 16; e += nthr) {
-    const int n = e >> 4, k2 = (e & 15) * 2;  // row n, columns k2 and k2 + 1
+  for (int e = tid; e < 64 * 32; e += nthr) {
+    const int n = e >> 5, k2 = (e & 31) * 2;  // row n, columns k2 and k2 + 1
     float val[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int k = k2 + h;
-      const int yo = n & 15, xi = k & 15;  // output and input points
+      const int row = n & 31, kk = k & 31;     // row of C, column of C
+      const int yo = row & 15, xi = kk & 15;  // output and input points
       float sn, cs;
       sincospif((float)((yo * xi) & 15) * 0.125f, &sn, &cs);
       const float cr = cs, ci = DIR * sn;
-      // rows 0..15: Yr = Cr Xr - Ci Xi; rows 16..31: Yi = Ci Xr + Cr Xi
-      val[h] = n < 16 ? (k < 16 ? cr : -ci) : (k < 16 ? ci : cr);
+      // rows 0..15 of C: Yr = Cr Xr - Ci Xi; rows 16..31: Yi = Ci Xr + Cr Xi
+      val[h] = row < 16 ? (kk < 16 ? cr : -ci) : (kk < 16 ? ci : cr);
     }
     uint32_t hi, lo;
     split_pair<1>(val[0], val[1], hi, lo);
-    const int off = (n >> 3) * 512 + (k2 >> 3) * 128 + (n & 7) * 16 + (k2 & 7) * 2;
-    *reinterpret_cast<uint32_t*>(tcB + off) = hi;
-    *reinterpret_cast<uint32_t*>(tcB + 2048 + off) = lo;
+    // rows 0..31: [C hi | 0]; rows 32..63: [C lo | C hi]
+    uint32_t v;
+    if (n < 32) v = k2 < 32 ? hi : 0u;
+    else v = k2 < 32 ? lo : hi;
+    const int off = (n >> 3) * 1024 + (k2 >> 3) * 128 + (n & 7) * 16 + (k2 & 7) * 2;
+    *reinterpret_cast<uint32_t*>(tcB + off) = v;
   }
 }
 
 // The first sub-stage (radix 16, S = 1) of a pipelined tile on the tensor
 // cores: thread tid's butterfly (column c, k) is row tid of the GEMM. Reads
 // the dense tile, writes the outputs (twiddled by w_R^(j k) in FP32) to the
-// padded layout as the FP32 sub-stage does. False when the MMAs did not
-// complete within the wait limit.
+// padded layout as the FP32 sub-stage does. False (for every thread) when
+// the MMAs did not complete within the wait limit.
 template <int DIR, int MODE, int NBC, int R, int Rr, int nthr>
-__device__ __forceinline__ bool tc16_first(Cx<float>* buf, const Cx<float>* tw, unsigned char* tcA,
-                                           unsigned char* tcB, uint64_t* tcbar, uint32_t tmem, uint32_t par,
-                                           int tid, int b, int kg, uint64_t limit) {
+__device__ __forceinline__ bool tc16_first(Cx<float>* buf, const Cx<float>* tw, unsigned char* tcB,
+                                           uint64_t* tcbar, uint32_t tmem, uint32_t par, int tid, int b, int kg,
+                                           uint64_t limit) {
   using T = float;
   using L = LayC<T, NBC>;
   constexpr int NB = NBC, r0 = 16;
@@ -157,34 +167,33 @@ __device__ __forceinline__ bool tc16_first(Cx<float>* buf, const Cx<float>* tw, 
   int ex = 0;
   if (mx > 0.f) frexpf(mx, &ex);  // mx < 2^ex
   const float sc = ldexpf(1.f, -ex);
-  // row tid of A: halves [xr hi 0..15 | xi hi | xr lo | xi lo], as 8 core
-  // rows of 16 bytes (row group (tid mod 128) / 8 of block tid / 128)
-  uint32_t hw[32];
+  uint32_t hw[32];  // row tid of A as packed half pairs
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     split_pair<1>(xr[2 * j] * sc, xr[2 * j + 1] * sc, hw[j], hw[16 + j]);
     split_pair<1>(xi[2 * j] * sc, xi[2 * j + 1] * sc, hw[8 + j], hw[24 + j]);
   }
+  __syncthreads();  // every input is in registers: the tile's bytes become A
+  // row tid: 8 core rows of 16 bytes (row group (tid mod 128) / 8 of block
+  // tid / 128, 16 KB per block)
+  unsigned char* const tcA = reinterpret_cast<unsigned char*>(buf);
   unsigned char* arow = tcA + (tid >> 7) * 16384 + ((tid & 127) >> 3) * 1024 + (tid & 7) * 16;
 #pragma unroll
   for (int kc = 0; kc < 8; ++kc)
     *reinterpret_cast<uint4*>(arow + kc * 128) = make_uint4(hw[4 * kc], hw[4 * kc + 1], hw[4 * kc + 2], hw[4 * kc + 3]);
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // A visible to the tensor cores
-  __syncthreads();  // every input is read and every A row written
+  __syncthreads();
   if (tid == 0) {
     tc_fence_after();
-    constexpr uint32_t kId = umma_idesc_f16(128, 32, 0);
-    const uint32_t bhi = sh_addr(tcB), blo = bhi + 2048;
+    constexpr uint32_t kId = umma_idesc_f16(128, 64, 0);
+    const uint32_t b0 = sh_addr(tcB);
 #pragma unroll 1
     for (int blk = 0; blk < nthr / 128; ++blk) {
       const uint32_t a0 = sh_addr(tcA) + blk * 16384;
-      const uint32_t d1 = tmem + blk * 64, d2 = d1 + 32;
-      umma_f16(d1, umma_desc(a0, 128, 1024), umma_desc(bhi, 128, 512), kId, false);
-      umma_f16(d1, umma_desc(a0 + 256, 128, 1024), umma_desc(bhi + 256, 128, 512), kId, true);
-      umma_f16(d2, umma_desc(a0, 128, 1024), umma_desc(blo, 128, 512), kId, false);
-      umma_f16(d2, umma_desc(a0 + 256, 128, 1024), umma_desc(blo + 256, 128, 512), kId, true);
-      umma_f16(d2, umma_desc(a0 + 512, 128, 1024), umma_desc(bhi, 128, 512), kId, true);
-      umma_f16(d2, umma_desc(a0 + 768, 128, 1024), umma_desc(bhi + 256, 128, 512), kId, true);
+      const uint32_t d = tmem + blk * 64;
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks)
+        umma_f16(d, umma_desc(a0 + ks * 256, 128, 1024), umma_desc(b0 + ks * 256, 128, 1024), kId, ks > 0);
     }
     umma_commit(tcbar);
   }
@@ -204,6 +213,8 @@ __device__ __forceinline__ bool tc16_first(Cx<float>* buf, const Cx<float>* tw, 
 #pragma unroll
     for (int i = 0; i < 8; ++i) y[8 * q + i] = fmaf(l[i], kInvLo, y[8 * q + i]);
   }
+  tc_fence_before();
+  __syncthreads();  // every MMA is done: the outputs may overwrite A
   const float us = ldexpf(1.f, ex);
   constexpr bool kLay = L::exact(r0);
   const int a = r0 * k * NB + c;
@@ -215,7 +226,6 @@ __device__ __forceinline__ bool tc16_first(Cx<float>* buf, const Cx<float>* tw, 
     if (k != 0) w = cmul(w, tw[j * k]);
     buf[kLay ? base + L::step(j) : pidx<T>(a + j * NB)] = w;
   }
-  tc_fence_before();
   __syncthreads();
   return true;
 }
@@ -265,11 +275,11 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
   const int tid = threadIdx.x;
   const int kg = tid / NB;
   const int b = tid - kg * NB;
-  // tensor-core operands after the kernel's own shared memory
-  unsigned char* const tcA =
+  // tensor-core B operand after the kernel's own shared memory (A lives in
+  // the tile buffer)
+  unsigned char* const tcB =
       tma_smem + tc_smem_offset((size_t)(2 * bufE + (kStageTw ? R : 0)) * sizeof(Cx<T>) + 3 * sizeof(uint64_t));
-  unsigned char* const tcB = tcA + nthr * 128;
-  uint64_t* const tcbar = reinterpret_cast<uint64_t*>(tcB + 4096);
+  uint64_t* const tcbar = reinterpret_cast<uint64_t*>(tcB + 8192);
   uint32_t* const tmem_slot = reinterpret_cast<uint32_t*>(tcbar + 1);
   const uint32_t ntiles = pp.tiles_q * pp.tiles_p * pp.tiles_b;
   const int rows = pp.tma_rows;
@@ -378,8 +388,7 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
     // are rows [c][j] of the dense tile), modes 1 and 2 the column (rows
     // [j][c]); both read consecutive addresses across a warp
     if constexpr (kTc) {
-      const bool tok = tc16_first<DIR, MODE, NBC, R, Rr, nthr>(buf, tw, tcA, tcB, tcbar, tmem, tc_par, tid, b, kg,
-                                                               limit);
+      const bool tok = tc16_first<DIR, MODE, NBC, R, Rr, nthr>(buf, tw, tcB, tcbar, tmem, tc_par, tid, b, kg, limit);
       tc_par ^= 1u;
       if (!tok) {  // uniform: decided by a block-wide vote
         // the MMAs did not complete: record it, drain the next tile's copy

@@ -97,11 +97,10 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
 
 // Shared memory of the precision form's tensor-core sub-stage in a
 // pipelined pass, after the kernel's own (offset rounded up to 128 bytes):
-// the A operand (one 128-byte row of 64 halves per thread: 16 real hi, 16
-// imaginary hi, 16 real lo, 16 imaginary lo), B = the radix-16 DFT in real
-// form, hi and scaled lo (32 x 32 halves each), an mbarrier and the
-// tensor-memory address.
+// the B operand (the radix-16 DFT in real form, 64 rows of 64 halves), an
+// mbarrier and the tensor-memory address. (The A operand takes the tile
+// buffer's own bytes.)
 __host__ __device__ constexpr size_t tc_smem_offset(size_t own) { return (own + 127) / 128 * 128; }
-__host__ __device__ constexpr size_t tc_smem_bytes(int nthr) { return (size_t)nthr * 128 + 4096 + 16; }
+__host__ __device__ constexpr size_t tc_smem_bytes(int nthr) { return (void)nthr, (size_t)8192 + 16; }
 
 }  // namespace fftj
