@@ -203,16 +203,12 @@ __device__ __forceinline__ bool tc16_first(Cx<float>* buf, const Cx<float>* tw, 
   // row tid = lane 32 (w mod 4) + lane of block w / 4 (warp w)
   const int warp = tid >> 5;
   const uint32_t ta = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(warp >> 2) * 64;
-  float y[32];
-  tmem_ld32(ta, y);
+  float d[64];  // D1 (columns 0..31) and D2 (32..63) in one load
+  tmem_ld64(ta, d);
   constexpr float kInvLo = 1.f / lo_scale<1>();
+  float y[32];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    float l[8];
-    tmem_ld8(ta + 32 + 8 * q, l);
-#pragma unroll
-    for (int i = 0; i < 8; ++i) y[8 * q + i] = fmaf(l[i], kInvLo, y[8 * q + i]);
-  }
+  for (int i = 0; i < 32; ++i) y[i] = fmaf(d[32 + i], kInvLo, d[i]);
   tc_fence_before();
   __syncthreads();  // every MMA is done: the outputs may overwrite A
   const float us = ldexpf(1.f, ex);

@@ -53,6 +53,29 @@ int tma_prepare(const void* fn, const PassParams& pp) {
   const size_t smem = tma_smem_bytes(pp);
   if (smem > (size_t)optin) return 0;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) return 0;
+  if (pp.tc == 1) {
+    // Kernels with tensor-memory instructions: the runtime's occupancy query
+    // answers 1 (or 0) CTA per SM for them whatever their resources (checked
+    // on a GB300 with the same kernel with and without tcgen05), so the
+    // residency comes from the kernel's own limits: shared memory,
+    // registers, threads and its tensor-memory columns (512 per SM).
+    int smsm = 0, resv = 0;
+    cudaFuncAttributes fa;
+    if (cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, fn) != cudaSuccess)
+      return 0;
+    const int warps = (pp.threads + 31) / 32;
+    const int regs_warp = (fa.numRegs * 32 + 255) / 256 * 256;
+    const int by_smem = smsm / (int)(smem + fa.sharedSizeBytes + resv);
+    const int by_regs = 65536 / std::max(1, warps * regs_warp);
+    const int by_threads = 2048 / std::max(1, pp.threads);
+    const int by_tmem = 512 / std::max(64, (pp.threads / 128) * 64);
+    // (two 256-thread CTAs per SM run the radix-4096 rows of 4096^2 in
+    // 0.079 ms where the query's one took 0.099 ms)
+    per_sm = std::min(std::min(by_smem, by_regs), std::min(by_threads, by_tmem));
+    return per_sm > 0 ? per_sm * nsm : 0;
+  }
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, pp.threads, smem) != cudaSuccess) return 0;
   return per_sm * nsm;
 }

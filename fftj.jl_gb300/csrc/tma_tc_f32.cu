@@ -22,10 +22,12 @@ __global__ void __launch_bounds__(NBC * Rec::Tf, NBC * Rec::Tf <= 256 ? 2 : 1)
 #define TC0_(NB, ...) TC_(-1, 0, NB, __VA_ARGS__) TC_(1, 0, NB, __VA_ARGS__)
 
 static const RecipeEntry kTmaTc[] = {
-    // multi-pass transforms: radix 128, 256 and 1024 passes
-    TCT_(32, 16, 8) TCT_(16, 16, 16) TCT_(8, 16, 8, 8)
-    // single-pass transforms of three sub-stages
-    TC0_(1, 16, 16, 16) TC0_(2, 16, 16, 8) TC0_(4, 16, 8, 8)
+    // multi-pass transforms: radix 128, 256 and 1024 passes (4096- and
+    // 8192-element tiles)
+    TCT_(32, 16, 8) TCT_(16, 16, 16) TCT_(8, 16, 8, 8) TCT_(64, 16, 8) TCT_(32, 16, 16)
+    // single-pass transforms of three sub-stages (4096- and 8192-element tiles)
+    TC0_(1, 16, 16, 16) TC0_(2, 16, 16, 8) TC0_(4, 16, 8, 8) TC0_(2, 16, 16, 16) TC0_(4, 16, 16, 8)
+    TC0_(8, 16, 8, 8)
 };
 
 const RecipeEntry* tma_tc_table(int* count) {
