@@ -1186,7 +1186,8 @@ def main():
                     help="uneven: 10,000 uneven transforms + 256^3 rfft as one persistent group (default); "
                          "mixed: the mixed-radix/prime batch; configs: the other configurations")
     ap.add_argument("--count", type=int, default=UNEVEN_COUNT, help="transforms of the uneven workload")
-    ap.add_argument("--e2e-chunks", type=int, default=6, help="uneven workload: chunks of the e2e pipeline")
+    ap.add_argument("--e2e-chunks", type=int, default=12,
+                    help="uneven workload: chunks of the e2e pipeline (12 measured best of 6 / 12 / 24)")
     ap.add_argument("--quick", action="store_true",
                     help="uneven workload: the timed step, e2e and accuracy only (no other forms or breakdowns)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned planner report")
