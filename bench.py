@@ -56,8 +56,12 @@ STEP_FLOPS = sum(flops(n, BATCH) for _, n in PARTS)
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of a
 # workload's dominant kernel, from one ncu capture on a GB300 (the capture
 # commands are kept with the profile summaries): the C64 2^18 pass kernels of
-# the mixed workload (averaged over their launches).
-NCU_TRAFFIC_PER_LAUNCH = {"c64_262144": 1027.6e6}
+# the mixed workload (averaged over their launches), and the uneven batch's
+# persistent kernel.
+NCU_TRAFFIC_PER_LAUNCH = {"c64_262144": 1027.6e6,
+                          # the uneven batch's persistent kernel, one full-size launch (75.25 GB
+                          # read + 44.59 GB written; one ncu pass)
+                          "k_group_uneven": 119.838e9}
 # ALU pipe busy fraction (sm__inst_executed_pipe_alu, % of peak sustained
 # while active) of the same part's two pass kernels, averaged, from the same
 # capture: the limiter of the ComplexF64 passes, which compute in 64-bit block
