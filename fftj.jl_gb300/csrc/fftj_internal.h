@@ -91,6 +91,7 @@ struct PassParams {
   int64_t ld_inner;              // DECONV along a strided axis: inner stride (1 = contiguous)
   const void* ld_tab;            // DECONV: corr[n]; C2R_PRE: w[h], or hi[h >> ld_sh] when ld_sh > 0
   const void* ld_tab2;           // C2R_PRE two-level: lo[2^ld_sh]
+  const void* ld_tab3;           // C2R_PRE first pass of several: w_n^(m t) = w_2R^t, t < R (or nullptr)
   int ld_sh;                     // C2R_PRE: 0 one table, else the two-level split
   double ld_pre;                 // C2R_PRE pair factor (1/2 or 1)
   int ld_w;                      // SPREAD: taps per grid row

@@ -397,6 +397,18 @@ __device__ __forceinline__ Cx<T> c2r_twiddle(const PassParams& pp, int64_t g) {
   return __ldg(reinterpret_cast<const Cx<T>*>(pp.ld_tab) + g);
 }
 
+// irfft pre-pass of one entry (FFTJ src/real.jl:149-192): Z = xe + i (w xd)
+// from a = X[g], its mirror bb = X[h - g] and the twiddle w = w_n^g
+template <typename T>
+__device__ __forceinline__ Cx<T> c2r_pre_combine(Cx<T> a, Cx<T> bb, Cx<T> w, T pre) {
+  bb.y = -bb.y;
+  const Cx<T> xe = mk<T>((a.x + bb.x) * pre, (a.y + bb.y) * pre);
+  const Cx<T> xd = mk<T>((a.x - bb.x) * pre, (a.y - bb.y) * pre);
+  const T tr = fma(w.x, xd.x, -(w.y * xd.y));
+  const T ti = fma(w.x, xd.y, w.y * xd.x);
+  return mk<T>(xe.x - ti, xe.y + tr);
+}
+
 template <typename T, int LOADOP, bool CG = false>
 __device__ __forceinline__ Cx<T> load_elem(const PassParams& pp, const void* in, int64_t b, int64_t g);
 
@@ -1396,6 +1408,33 @@ __device__ __forceinline__ void pass_fused(const PassParams& pp, const void* __r
       if ((i + 1) * TF <= Rr || k < Rr) {
         int64_t g = gcol + (int64_t)k * ms;
         const int64_t gstep = (int64_t)Rr * ms;
+        if constexpr (LOADOP == LOAD_C2R_PRE && MODE == 1) {
+          if (pp.ld_tab3) {
+            // entries g = pcol + (k + j Rr) m of the first pass: every
+            // load of the butterfly first (both halves of each pair), then
+            // the twiddle w_n^g = w_n^pcol w_2R^(k + j Rr) from the
+            // thread's column factor and an R-entry table (L1-resident)
+            // instead of two table reads per entry
+            const int64_t hl = pp.ld_n;
+            const Cx<H>* X = reinterpret_cast<const Cx<H>*>(in) + boff;
+            const Cx<H>* tR = reinterpret_cast<const Cx<H>*>(pp.ld_tab3);
+            Cx<H> xa[r0], xb[r0];
+#pragma unroll
+            for (int j = 0; j < r0; ++j) {
+              const int64_t gj = g + j * gstep;
+              xa[j] = colok ? __ldg(X + gj) : mk<H>(0, 0);
+              xb[j] = colok ? __ldg(X + (hl - gj)) : mk<H>(0, 0);
+            }
+            const Cx<H> wp = colok ? c2r_twiddle<H>(pp, pcol) : mk<H>(1, 0);
+            const H pre = half_or_one<H>(pp.ld_pre);
+#pragma unroll
+            for (int j = 0; j < r0; ++j) {
+              const Cx<H> w = cmul(wp, __ldg(tR + k + j * Rr));
+              h[i][j] = c2r_pre_combine<H>(xa[j], xb[j], w, pre);
+            }
+            continue;
+          }
+        }
 #pragma unroll
         for (int j = 0; j < r0; ++j) {
           h[i][j] = colok ? load_elem_off<H, LOADOP>(pp, in, boff, g) : mk<H>(0, 0);

@@ -1489,6 +1489,15 @@ int build_c2r_1d(fftj_plan_s* P, i64 n, i64 nb, i64 idist, i64 odist, bool norma
       f.ld_tab2 = twd_lo;
       f.ld_sh = sh;
       f.ld_pre = normalized ? 0.5 : 1.0;
+      f.ld_tab3 = nullptr;
+      if (f.m > 1 && f.s == 1) {
+        // first pass of several: entry g = p + t m takes w_n^g = w_n^p w_2R^t
+        // (R-entry table; the column factor from the tables above)
+        std::vector<double> tr(2 * f.R);
+        for (i64 t = 0; t < f.R; ++t) omega(t * f.m, n, +1, &tr[2 * t], &tr[2 * t + 1]);
+        f.ld_tab3 = upload_cplx<T>(P, tr);
+        if (!f.ld_tab3) return fail(FFTJ_ERR_CUDA, "table upload failed");
+      }
       for (auto& o : inner) ops->push_back(o);
       return FFTJ_OK;
     }
