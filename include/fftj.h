@@ -298,10 +298,9 @@ const char* fftj_version(void);
  * for two passes batch * n * sizeof(complex) <= 63 MiB; larger requests
  * return FFTJ_ERR_ARG / FFTJ_ERR_UNSUPPORTED with a message. d_in/d_out hold
  * batch dense transforms; in == out is allowed. The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) and keeps it,
- * so it should come before any stream capture, and a device reset
- * (cudaDeviceReset) after that first call is not supported: the kept address
- * would be stale. A CUDA error already pending on the calling thread is
+ * looks up the array's device address (cudaGetSymbolAddress) and keeps it;
+ * a device reset (cudaDeviceReset) after that first call is not supported:
+ * the kept address would be stale. A CUDA error already pending on the calling thread is
  * reported as FFTJ_ERR_CUDA and left pending. All calls share the one array: calls that
  * overlap on the GPU (other streams, other threads) race and must be
  * serialised by the caller. Nothing in the array needs to start at zero.
