@@ -26,6 +26,9 @@ ITEMS = [
     ("c2c", np.float32, 1 << 20, 1, -1),   # the largest length of the uneven workload
     ("c2c", np.float64, 3 * 5 * 7 * 11 * 13, 1, -1),
     ("c2c", np.float64, 2 * 10007, 2, -1),  # split route: decimation copy, twiddled banded solve
+    ("c2c", np.float64, 16 * 509, 2, -1),   # CompositePlan: s-part passes, twiddled transpose, HvPass lanes
+    ("c2c", np.float64, 32 * 131, 2, 1),    # CompositePlan backward with RsPass lanes
+    ("c2c", np.float32, 64 * 1031, 1, -1),  # CompositePlan F32 (HvPass)
 ]
 
 
