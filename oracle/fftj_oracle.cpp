@@ -1544,6 +1544,25 @@ struct DimPass {
   std::unique_ptr<RsPass<T>> fb;
 };
 
+// _use_fs2 (src/fourstep.jl:518-529): a 2-D n1 x n2 transform runs as
+// Fs2Plan -- the strided dim 2 in strips first, then each contiguous row
+// ending in a fused power-of-two stage -- from 1 MB threaded / 4 MB serial.
+static const i64 FS2_MIN_BYTES = 1 << 20;  // _FS2_MIN_BYTES
+template <typename T>
+static bool use_fs2(i64 n1, i64 n2, bool threaded) {
+  const i64 bytes = 2 * n1 * n2 * (i64)sizeof(T);
+  if (bytes < (threaded ? FS2_MIN_BYTES : 4 * FS2_MIN_BYTES)) return false;
+  const int W = pick_width<T>();
+  if (!threaded && n1 % ((i64)fs_width<T>(n2) * W) != 0) return false;
+  if (4 * (i64)W * n2 * (i64)sizeof(T) > FS_INNER_MAX) return false;
+  i64 N1 = 0, N2 = 0;
+  if (!fourstep_split<T>(n1 * n2, 1, n2, &N1, &N2)) return false;
+  if (!factor_radices(n1).ok || !factor_radices(n2).ok) return false;
+  const std::vector<Stage<T>> rows = build_stages<T>(n1, -1, true);
+  const int f = rows.back().radix;
+  return (f == 2 || f == 4 || f == 8) && n1 / f >= W;
+}
+
 template <typename T>
 struct NdPlan : PlanBase {
   int D;
@@ -1551,6 +1570,7 @@ struct NdPlan : PlanBase {
   std::vector<i64> dims;
   i64 len;
   int nt;
+  bool fs2 = false;  // 2-D plan in Fs2Plan order (use_fs2)
   std::vector<std::unique_ptr<DimPass<T>>> passes;
   std::vector<T> are, aim, bre, bim;
   // _ndplan (src/ndplan.jl:57-118); dims before first_dim are pure batch
@@ -1577,6 +1597,15 @@ struct NdPlan : PlanBase {
         ps->fb.reset(new RsPass<T>(nd, D, Bi == 1 ? Bo : Bi));
       }
       passes.push_back(std::move(ps));
+    }
+    route = ORC_NDPLAN;
+    // N == 2 from dim 1 (_ndplan, src/ndplan.jl:112-113): FFTJ's NdPlan then
+    // executes through its Fs2Plan -- the same two chains, dim 2 first
+    if (dims.size() == 2 && first_dim == 0 && passes.size() == 2 && !passes[0]->fb && !passes[1]->fb &&
+        use_fs2<T>(dims[0], dims[1], nt > 1)) {
+      fs2 = true;
+      route = ORC_FS2;
+      std::swap(passes[0], passes[1]);
     }
     are.resize(len); aim.resize(len); bre.resize(len); bim.resize(len);
   }

@@ -24,6 +24,8 @@ enum orc_route {
   ORC_HVDH = 3,       // Gaussian resampling (src/hvdh.jl:30-58)
   ORC_COMPOSITE = 5,  // smooth part first, then batched resampling (src/composite.jl:10-101)
   ORC_SPLIT = 6,      // decimation in time into HvdH sub-transforms (src/composite.jl:103-280)
+  ORC_NDPLAN = 4,     // N-d plan, one pass per dimension (src/ndplan.jl:57-118)
+  ORC_FS2 = 7,        // 2-D N-d plan run as Fs2Plan: strided dim 2 first, then the rows (src/fourstep.jl:500-552)
 };
 
 // Host SIMD width FFTJ would see (src/kernels.jl:11-22). 128 = NEON (the GPU

@@ -14,8 +14,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "liboracle_fftj.so")
 _lib = None
 
-ROUTES = {0: "FFTPlan", 1: "FourStepPlan", 2: "ResamplePlan", 3: "HvdhPlan", 5: "CompositePlan",
-          6: "SplitPlan"}
+ROUTES = {0: "FFTPlan", 1: "FourStepPlan", 2: "ResamplePlan", 3: "HvdhPlan", 4: "NdPlan", 5: "CompositePlan",
+          6: "SplitPlan", 7: "Fs2Plan"}
 
 
 def build(quiet=True):
@@ -202,6 +202,14 @@ class PlanND:
             raise ValueError("oracle N-d plan failed")
         self.rtype = np.float32 if self.dt == 0 else np.float64
         self.ctype = np.complex64 if self.dt == 0 else np.complex128
+
+    @property
+    def route(self):
+        """'NdPlan', or 'Fs2Plan' for a 2-D complex plan FFTJ runs in two
+        sweeps (dim 2 strips, then rows)."""
+        if self.kind not in ("fft", "ifft", "bfft"):
+            return "NdPlan"
+        return ROUTES[lib().orc_plan_route(self.h)]
 
     def __call__(self, x):
         cshape = tuple(reversed([self.dims[0] // 2 + 1] + self.dims[1:]))

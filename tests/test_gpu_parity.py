@@ -264,13 +264,20 @@ def test_config_precision_2d_4096(fftj, orc):
     y = host(fftj.fft(dev(x, np.float32)))
     ref = np.fft.fft2(x.astype(np.complex128))
     assert rel_l2(y, ref) <= parity_tol(np.float32, 4096 * 4096)
+    # the FFTJ CPU plan of this shape: NdPlan run through Fs2Plan
+    po = orc.PlanND(np.float32, [4096, 4096], "fft")
+    assert po.route == "Fs2Plan"
+    yo = po(x)
+    assert rel_l2(y, yo) <= parity_tol(np.float32, 4096 * 4096)
     # two HBM sweeps on request, as FFTJ's Fs2Plan (src/fourstep.jl:500-552):
     # the contiguous rows, then the strided 4096-point columns in one pass
     p2 = fftj.Plan(np.float32, (4096, 4096), kind="c2c", opts={"wide_axis": 1})
     inf = p2.info
     assert inf.npasses == 2 and list(inf.pass_radix[:2]) == [4096, 4096]
     assert list(inf.pass_threads[:2])[1] == 1024 and inf.specialized_passes == 2
-    assert rel_l2(host(p2(dev(x, np.float32))), ref) <= parity_tol(np.float32, 4096 * 4096)
+    y2 = host(p2(dev(x, np.float32)))
+    assert rel_l2(y2, ref) <= parity_tol(np.float32, 4096 * 4096)
+    assert rel_l2(y2, yo) <= parity_tol(np.float32, 4096 * 4096)
 
 
 @pytest.mark.parametrize("shape", [(4096, 64), (4096, 3, 4), (2, 4096, 12), (4096, 6)])

@@ -274,3 +274,27 @@ def test_split_reference_sizes(orc, T):
         if _use_split(T, n):
             assert orc.Plan1D(T, n, "fft").route == "SplitPlan", n
         assert rel_l2(orc.PlanDirect(T, n, "split", direction="ifft")(y), x) <= 100 * EPS[T], n
+
+
+def test_fs2_routing_and_parity(orc):
+    """FFTJ's _ndplan runs a 2-D complex plan through Fs2Plan (the strided
+    dim 2 in strips, then the rows) when _use_fs2 holds (src/fourstep.jl:
+    518-529: >= 4 MB serially, strip and inner-buffer limits, a fused
+    power-of-two last row stage); the restated plan routes the same way and
+    matches FP64 numpy within the parity bar."""
+    from conftest import parity_tol, rel_l2
+    assert orc.PlanND(np.float32, [4096, 4096], "fft").route == "Fs2Plan"
+    assert orc.PlanND(np.float64, [1024, 1024], "fft").route == "Fs2Plan"
+    assert orc.PlanND(np.float32, [512, 512], "fft").route == "NdPlan"    # 2 MB: below the serial 4 MB
+    assert orc.PlanND(np.float32, [64, 4096], "fft").route == "NdPlan"    # strips too wide for the inner buffer
+    assert orc.PlanND(np.float32, [16, 16, 4], "fft").route == "NdPlan"   # 3-D
+    rng = np.random.default_rng(0xF52)
+    for T, shape in ((np.float64, (1024, 1024)), (np.float32, (1024, 2048))):
+        x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+        p = orc.PlanND(T, list(reversed(shape)), "fft")
+        assert p.route == "Fs2Plan"
+        y = p(x)
+        ref = np.fft.fft2(x)
+        assert rel_l2(y, ref) <= parity_tol(T, x.size), (T, shape)
+        xi = orc.PlanND(T, list(reversed(shape)), "ifft")(y)
+        assert rel_l2(xi, x) <= 2 * parity_tol(T, x.size)
