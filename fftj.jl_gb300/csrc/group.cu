@@ -71,14 +71,22 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
   return v;
 }
 
-template <typename T, int DIR>
+// LOADOP: LOAD_PLAIN for the passes that read plain data (most of them: a
+// function of their own keeps the other load ops' code and registers out),
+// LOAD_RUNTIME for first passes with a fused load op
+template <typename T, int DIR, int LOADOP>
 __device__ __noinline__ void group_pass(const PassParams& pp, const void* src, void* dst, uint32_t t0, uint32_t t1,
                                         int tid) {
   for (uint32_t t = t0; t < t1; ++t) {
-    pass_tile<T, DIR, LOAD_RUNTIME, RuntimeRecipe, true>(pp, src, reinterpret_cast<Cx<Hs<T>>*>(dst), t, tid,
-                                                          pp.threads);
+    pass_tile<T, DIR, LOADOP, RuntimeRecipe, true>(pp, src, reinterpret_cast<Cx<Hs<T>>*>(dst), t, tid, pp.threads);
     __syncthreads();  // the next tile reuses the shared buffer
   }
+}
+template <typename T, int DIR>
+__device__ __forceinline__ void group_pass_any(const PassParams& pp, const void* src, void* dst, uint32_t t0,
+                                               uint32_t t1, int tid) {
+  if (pp.load_op == LOAD_PLAIN) group_pass<T, DIR, LOAD_PLAIN>(pp, src, dst, t0, t1, tid);
+  else group_pass<T, DIR, LOAD_RUNTIME>(pp, src, dst, t0, t1, tid);
 }
 
 // the solve with factors rebuilt per call, out of line (keeps the other
@@ -179,11 +187,11 @@ __global__ void __launch_bounds__(kGroupThreads, 2)
     if (!s_skip) {
       if (sop.kind == OP_PASS) {
         if (sop.f64) {  // block fixed point (group creation rejects FP64-butterfly passes)
-          if (sop.dir < 0) group_pass<Fx, -1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
-          else group_pass<Fx, 1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
+          if (sop.dir < 0) group_pass_any<Fx, -1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
+          else group_pass_any<Fx, 1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
         } else {
-          if (sop.dir < 0) group_pass<float, -1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
-          else group_pass<float, 1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
+          if (sop.dir < 0) group_pass_any<float, -1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
+          else group_pass_any<float, 1>(sop.pp, sop.src, sop.dst, item.t0, item.t1, tid);
         }
       } else if (sop.f64) {
         group_elementwise<double>(sop, item.t0, item.t1, tid);
@@ -306,21 +314,34 @@ int build_persistent(fftj_group_s* g) {
     }
   }
   g->nops = (int)g->h_ops.size();
-  // queue: level-major; within a level, plans with more work first
+  // queue: level-major; within a level, by device code, then plans with
+  // more work first
   std::vector<size_t> order(g->plans.size());
   for (size_t i = 0; i < order.size(); ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
     return g->plans[a]->n * g->plans[a]->batch > g->plans[b]->n * g->plans[b]->batch;
   });
   std::vector<GroupItem> items;
-  for (size_t lev = 0; lev < maxlev; ++lev)
-    for (size_t p : order) {
+  for (size_t lev = 0; lev < maxlev; ++lev) {
+    // the level's ops grouped by the device code they run (op kind, dtype,
+    // direction, plain or fused load), larger plans first in each: CTAs
+    // that run at the same time then run the same functions (fewer
+    // instruction-cache misses; the uneven batch's step 115.9 -> 113.5 ms)
+    std::vector<size_t> lo(order);
+    auto code = [&](size_t p) {
+      if (lev >= g->plans[p]->ops.size()) return 1 << 20;
+      const GroupOp& o = g->h_ops[first[p] + (int)lev];
+      return ((o.kind * 2 + o.f64) * 2 + (o.dir > 0)) * 2 + (o.load_op != LOAD_PLAIN);
+    };
+    std::stable_sort(lo.begin(), lo.end(), [&](size_t a, size_t b) { return code(a) < code(b); });
+    for (size_t p : lo) {
       fftj_plan P = g->plans[p];
       if (lev >= P->ops.size()) continue;
       const int oi = first[p] + (int)lev;
       const uint32_t nt = g->h_ops[oi].ntiles, ch = item_chunk(P->ops[lev]);
       for (uint32_t t = 0; t < nt; t += ch) items.push_back(GroupItem{oi, t, std::min(nt, t + ch), 0});
     }
+  }
   g->nitems = (int)items.size();
 
   int dev = 0, sms = 0, optin = 0, per_sm = 0;
