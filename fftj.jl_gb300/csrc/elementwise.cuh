@@ -193,14 +193,14 @@ __device__ __forceinline__ void solve_fly_at(const SolveParams& sp, const Cx<T>*
   }
 }
 
-template <typename T, int B, bool CG>
+template <typename T, int B, bool CG, int K = 8>
 __device__ __forceinline__ void solve_at(const SolveParams& sp, const Cx<T>* __restrict__ g,
                                          Cx<T>* __restrict__ y, const int64_t tid) {
   // Rows go in blocks of K: a block's operands (input rows, LU factors,
   // output indices) are loaded together, then its K dependent recurrence
   // steps run from registers. Row pointers advance by increments (the
-  // kernel is a latency chain: every instruction of a row counts).
-  constexpr int K = 8;
+  // kernel is a latency chain: every instruction of a row counts). The
+  // persistent group kernel (128 registers a thread) takes K = 4.
   const int64_t nt = sp.nbatch * sp.nchunk;
   if (tid >= nt) return;
   const SolveLane ln = solve_lane(sp, tid);

@@ -40,6 +40,10 @@ namespace fftj {
 
 constexpr int kGroupThreads = 256;  // CTA size of the persistent kernel
 constexpr int kEwTile = 256;        // elements (solve: chunks) per elementwise tile
+#ifndef FFTJ_GROUP_SOLVE_K
+#define FFTJ_GROUP_SOLVE_K 4
+#endif
+constexpr int kGroupSolveK = FFTJ_GROUP_SOLVE_K;  // rows per block of the banded solve (registers)
 
 struct alignas(16) GroupOp {
   int32_t kind, f64, dir, load_op;
@@ -122,8 +126,8 @@ __device__ __noinline__ void group_copy(const GroupOp& op, uint32_t t0, uint32_t
 template <typename T, int B>
 __device__ __noinline__ void group_solve(const GroupOp& op, uint32_t t0, uint32_t t1, int tid) {
   for (uint32_t t = t0; t < t1; ++t)
-    solve_at<T, B, true>(op.sv, reinterpret_cast<const Cx<T>*>(op.src), reinterpret_cast<Cx<T>*>(op.dst),
-                         (int64_t)t * kEwTile + tid);
+    solve_at<T, B, true, kGroupSolveK>(op.sv, reinterpret_cast<const Cx<T>*>(op.src),
+                                       reinterpret_cast<Cx<T>*>(op.dst), (int64_t)t * kEwTile + tid);
 }
 template <typename T>
 __device__ __forceinline__ void group_elementwise(const GroupOp& op, uint32_t t0, uint32_t t1, int tid) {
