@@ -264,12 +264,14 @@ uint32_t op_tiles(const Op& op) {
   return 0;
 }
 
-// tiles per queue item: about 4K elements of pass work, 2K elementwise
-// elements, one tile of solve chunks (2K / 4K / 8K / 16K elements of pass
-// work: 113.5 / 109.8-111.1 / 111.0 / 116.3 ms for the uneven batch)
-constexpr int64_t kItemPassElems = 4096;
-uint32_t item_chunk(const Op& op) {
-  if (op.kind == OP_PASS) return (uint32_t)std::max<int64_t>(1, kItemPassElems / ((int64_t)op.pp.NB * op.pp.R));
+// tiles per queue item: about 8K elements of F32 / 4K of ComplexF64 pass
+// work (two tiles of the default size each), 2K elementwise elements, one
+// tile of solve chunks. All passes at 2K / 4K / 8K / 16K elements: 113.5 /
+// 109.8-111.1 / 111.0 / 116.3 ms for the uneven batch; 4K cost the F32
+// passes (one tile per item) what it saved on the ComplexF64 ones.
+uint32_t item_chunk(const Op& op, bool f64) {
+  const int64_t elems = f64 ? 4096 : 8192;
+  if (op.kind == OP_PASS) return (uint32_t)std::max<int64_t>(1, elems / ((int64_t)op.pp.NB * op.pp.R));
   if (op.kind == OP_SOLVE) return 1;
   return 8;
 }
@@ -344,7 +346,7 @@ int build_persistent(fftj_group_s* g) {
       fftj_plan P = g->plans[p];
       if (lev >= P->ops.size()) continue;
       const int oi = first[p] + (int)lev;
-      const uint32_t nt = g->h_ops[oi].ntiles, ch = item_chunk(P->ops[lev]);
+      const uint32_t nt = g->h_ops[oi].ntiles, ch = item_chunk(P->ops[lev], P->dtype == FFTJ_F64);
       for (uint32_t t = 0; t < nt; t += ch) items.push_back(GroupItem{oi, t, std::min(nt, t + ch), 0});
     }
   }
