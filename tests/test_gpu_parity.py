@@ -382,22 +382,30 @@ def test_inplace_and_determinism(fftj, T):
         assert torch.equal(z, y1), n   # in == out
 
 
-def test_strided_batches_c_abi(fftj):
-    """idist/odist > n through the C ABI (padded rows)."""
+@pytest.mark.parametrize("T,n,B,idist,odist", [
+    (np.float32, 1000, 5, 1024, 1100),
+    (np.float64, 16 * 509, 3, 16 * 509 + 8, 16 * 509 + 24),   # CompositePlan (HvPass lanes)
+    (np.float64, 32 * 131, 3, 32 * 131 + 3, 32 * 131 + 5),    # CompositePlan (RsPass lanes)
+    (np.float64, 2 * 10007, 2, 2 * 10007 + 2, 2 * 10007 + 6),  # SplitPlan
+    (np.float64, 10007, 3, 10010, 10016),                      # HvdhPlan
+])
+def test_strided_batches_c_abi(fftj, T, n, B, idist, odist):
+    """idist/odist > n through the C ABI (padded rows), on the smooth,
+    composite, split and Gaussian-resampling routes."""
     L = fftj.lib()
-    n, B, idist, odist = 1000, 5, 1024, 1100
-    rng = np.random.default_rng(3)
-    x = cn(rng, (B, idist)).astype(np.complex64)
-    xd = dev(x, np.float32)
-    yd = torch.zeros((B, odist), dtype=torch.complex64, device="cuda")
+    rng = np.random.default_rng([3, n])
+    x = cn(rng, (B, idist)).astype(np.complex64 if T is np.float32 else np.complex128)
+    xd = dev(x, T)
+    yd = torch.zeros((B, odist), dtype=CT[T], device="cuda")
     h = ctypes.c_void_p()
     dims = (ctypes.c_int64 * 1)(n)
-    assert L.fftj_plan_c2c(ctypes.byref(h), 0, 1, dims, B, idist, odist, -1, 1.0) == 0
+    dt = 0 if T is np.float32 else 1
+    assert L.fftj_plan_c2c(ctypes.byref(h), dt, 1, dims, B, idist, odist, -1, 1.0) == 0
     try:
         assert L.fftj_execute(h, ctypes.c_void_p(xd.data_ptr()), ctypes.c_void_p(yd.data_ptr()), None) == 0
         torch.cuda.synchronize()
         y = host(yd)
-        assert rel_l2(y[:, :n], np.fft.fft(x[:, :n], axis=-1)) <= parity_tol(np.float32, n)
+        assert rel_l2(y[:, :n], np.fft.fft(x[:, :n], axis=-1)) <= parity_tol(T, n)
         assert np.all(y[:, n:] == 0)
     finally:
         L.fftj_plan_destroy(h)
