@@ -7,9 +7,12 @@
 // the stride lane q are left to the compiler's auto-vectoriser (NEON on the
 // Grace host), standing in for FFTJ's explicit SIMD.Vec code.
 //
-// Parity status: pinned against an FP64 direct DFT (double-double
-// accumulation, exact angle reduction) and numpy's pocketfft at the reference
-// test sizes; see tests/test_oracle.py.
+// Parity status: parity unpinned -- the reference's tests hold no stored
+// vectors (they draw random inputs and call FFTW at run time) and the
+// reference cannot be run here, so this restatement is checked against an
+// FP64 direct DFT (double-double accumulation, exact angle reduction) and
+// numpy's pocketfft at the reference test sizes and tolerance classes, not
+// against reference outputs; see tests/test_oracle.py.
 #include "fftj_oracle.hpp"
 
 #include <algorithm>

@@ -7,10 +7,11 @@
 // restates the reference's algorithms (factorization, radix tower, stage index
 // maps, butterflies, four-step, resampling, real and N-d plans, routing) and
 // serves as "the FFTJ CPU plan" for parity and for the threaded CPU baseline.
-// Parity pin: the restatement is checked against an FP64 direct DFT with
-// double-double accumulation and against numpy's pocketfft at the reference's
-// own test sizes and tolerance classes (test/runtests.jl); no outputs of the
-// reference itself could be produced here (no Julia toolchain).
+// Parity unpinned: the reference's tests hold no stored vectors and no
+// outputs of the reference itself could be produced here (no Julia
+// toolchain), so the restatement is checked against an FP64 direct DFT with
+// double-double accumulation and against numpy's pocketfft at the
+// reference's own test sizes and tolerance classes (test/runtests.jl).
 #pragma once
 #include <cstdint>
 

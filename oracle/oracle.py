@@ -2,7 +2,9 @@
 
 The oracle is a CPU restatement of FFTJ.jl's transform path (see
 fftj_oracle.cpp). Only tests/, __graft_entry__.smoke() and bench.py's CPU
-baseline leg import this module; the product library never does.
+baseline leg import this module; the product library never does. Parity
+unpinned: no reference-held vectors or reference outputs exist, so it is
+checked against FP64 references at the reference's test sizes.
 """
 import ctypes
 import os
