@@ -430,6 +430,16 @@ def uneven_items(count, seed=UNEVEN_SEED):
     return items
 
 
+def uneven_kind(item):
+    """The category of an item of the uneven batch (the step's by-kind split):
+    c2c_f32, c2c_f64_prime, r2c_f32, ..., rfft_f32_256^3."""
+    from fftj import tune
+    kind, dt, n = item
+    if kind == "r2c3d":
+        return "rfft_f32_256^3"
+    return "%s_%s%s" % (kind, "f64" if np.dtype(dt) == np.float64 else "f32", "_prime" if tune.is_prime(n) else "")
+
+
 def uneven_flops(kind, n):
     nn = int(np.prod(n)) if isinstance(n, tuple) else n
     return (2.5 if kind.startswith("r2c") else 5.0) * nn * math.log2(nn)
@@ -670,6 +680,13 @@ def run_uneven(args):
     fftj.build()
     items = uneven_items(args.count)
     config = uneven_config(items)
+    if args.kind:
+        # one category of the batch alone (profiling a subset)
+        items = [it for it in items if uneven_kind(it) == args.kind]
+        if not items:
+            raise SystemExit("no item of kind %s among the first %d" % (args.kind, args.count))
+        config = {"workload": "uneven batch subset: the %d %s items of the first %d transforms (seed %d)"
+                              % (len(items), args.kind, args.count, UNEVEN_SEED), "items": len(items)}
     t0 = time.perf_counter()
 
     def mk(it, opts=None):
@@ -841,13 +858,8 @@ def run_uneven(args):
         del g
     split = {}
     cats = {}
-    for i, (kind, dt, n) in enumerate(items):
-        if kind == "r2c3d":
-            key = "rfft_f32_256^3"
-        else:
-            key = "%s_%s%s" % (kind, "f64" if np.dtype(dt) == np.float64 else "f32",
-                               "_prime" if fftj.tune.is_prime(n) else "")
-        cats.setdefault(key, []).append(i)
+    for i, it in enumerate(items):
+        cats.setdefault(uneven_kind(it), []).append(i)
     for key, idx in sorted(cats.items()):
         for mode in ("persistent",) + (() if args.quick else ("graph",)):
             g = fftj.Group([plans[i] for i in idx], [xs[i] for i in idx], [ys[i] for i in idx], mode=mode)
@@ -874,7 +886,7 @@ def run_uneven(args):
     }
 
     learned = None
-    if not args.no_learned and not args.quick:
+    if not args.no_learned and not args.quick and not args.kind:
         learned, model = learned_planner_report()
         if model is not None:
             from fftj import tune
@@ -1191,6 +1203,8 @@ def main():
                     help="uneven: 10,000 uneven transforms + 256^3 rfft as one persistent group (default); "
                          "mixed: the mixed-radix/prime batch; configs: the other configurations")
     ap.add_argument("--count", type=int, default=UNEVEN_COUNT, help="transforms of the uneven workload")
+    ap.add_argument("--kind", default=None,
+                    help="uneven workload: only the items of one category (c2c_f64, c2c_f32_prime, r2c_f64, ...)")
     ap.add_argument("--e2e-chunks", type=int, default=12,
                     help="uneven workload: chunks of the e2e pipeline (12 measured best of 6 / 12 / 24)")
     ap.add_argument("--quick", action="store_true",
