@@ -607,3 +607,39 @@ def test_hvdh_factors_fly(fftj, T, n, B, route):
     g()
     g.status()
     assert rel_l2(host(yg), yf) <= 10 * EPS[T], rel_l2(host(yg), yf) / EPS[T]
+
+
+def _random_nonsmooth(rng, count):
+    """Seeded non-smooth lengths n = s p: s 7-smooth in [1, 4096], p a
+    product of primes >= 11 (the part no radix covers)."""
+    primes = [11, 13, 17, 19, 23, 97, 131, 257, 509, 1009, 2003, 4099]
+    out = []
+    while len(out) < count:
+        s = int(2 ** rng.integers(0, 7) * 3 ** rng.integers(0, 3) * 5 ** rng.integers(0, 2) * 7 ** rng.integers(0, 2))
+        p = int(rng.choice(primes))
+        if rng.random() < 0.3:
+            p *= int(rng.choice(primes[:5]))
+        n = s * p
+        if 64 <= n <= (1 << 21) and p > 13:
+            out.append(n)
+    return out
+
+
+@pytest.mark.parametrize("T", T_LIST)
+def test_random_nonsmooth_lengths_all_routes(fftj, T):
+    """Seeded random non-smooth lengths on FFTJ's routing and with the route
+    forced to resampling (1), Gaussian (2: HvdH / split) and CompositePlan
+    (4): forward against FP64 numpy within the parity bar, and the
+    normalised inverse round trip."""
+    rng = np.random.default_rng(0x5EED if T is np.float32 else 0x5EEE)
+    for n in _random_nonsmooth(rng, 10):
+        B = 2
+        x = cn(rng, (B, n))
+        ref = np.fft.fft(x, axis=-1)
+        tol = parity_tol(T, n)
+        for route in (0, 1, 2, 4):
+            pf = fftj.Plan(T, (n,), kind="c2c", batch=B, opts={"route": route})
+            y = pf(dev(x, T))
+            assert rel_l2(host(y), ref) <= tol, (n, route, pf.route)
+            pb = fftj.Plan(T, (n,), kind="c2c", batch=B, direction=1, scale=1.0 / n, opts={"route": route})
+            assert rel_l2(host(pb(y)), x) <= 2 * tol, (n, route, pb.route)

@@ -183,3 +183,27 @@ def test_split_route_choice(T):
     assert info(T, "c2c", np.float64, 2 * 10007, route=1).route == 2  # forced resampling
     assert info(T, "c2c", np.float32, 2 * 10007, route=2).route == 5  # forced Gaussian (split)
     assert info(T, "c2c", np.float64, 2 * 512).route in (0, 1)        # smooth: no split
+
+
+def test_composite_and_split_lengths_plan(T):
+    """Non-smooth n = s p (s 7-smooth, p prime or with 11/13 factors, HvPass
+    or RsPass for the odd part) up to 2^22 plan on every route that takes
+    them -- FFTJ's routing, CompositePlan forced (route 4), the Gaussian
+    route (split for even n) -- with and without the persistent kernel's
+    256-thread cap, both dtypes."""
+    smooth = sorted({2 ** a * 3 ** b * 5 ** c * 7 ** d for a in range(13) for b in range(8)
+                     for c in range(6) for d in range(5)})
+    S = [s for s in smooth if 2 <= s <= 4096]
+    n_planned = 0
+    for dt in (np.float32, np.float64):
+        for p in (97, 131, 257, 509, 1009, 2431, 4099, 10007):
+            for s in S[::3]:
+                n = s * p
+                if n > (1 << 22):
+                    continue
+                for route in (0, 2, 4):
+                    for tmax in (0, 256):
+                        inf = T.plan_info(T.query("c2c", dt, n), (0, 0, 0, 0, route, tmax))
+                        assert inf.route in (2, 3, 5, 6), (dt, n, route)
+                        n_planned += 1
+    assert n_planned > 2000
