@@ -100,7 +100,6 @@ struct PassParams {
   int tma_rows;                  // tile rows per box copy (a divisor of R, <= 256)
   int tma_buf;                   // elements per tile buffer (a multiple of 16)
   int tma_extra_tx;              // test hook: bytes a tile's barrier expects beyond its copies (0)
-  int cluster;                   // CTAs per thread-block cluster of the launch (0 or 1: none)
   uint64_t tma_wait_ns;          // bound of each wait for a tile's copies
 };
 
@@ -224,9 +223,6 @@ int pass_geometry(PassParams& pp, bool f64, int64_t R, int64_t m, int64_t s, int
 // the one-pass strided F32 axis: its length and tile columns
 constexpr int64_t kWideR = 4096;
 constexpr int kWideCols = 4;
-// CTAs per cluster of the wide pass (neighbouring strips scheduled together;
-// 2, 4 and 8 measured no faster than none: 0.107 / 0.116 / 0.129 vs 0.110 ms)
-constexpr int kWideCluster = 1;
 void outer_twiddle_layout(PassParams& pp, bool f64);
 const void* pick_pass_kernel(bool f64, int dir, const PassParams& pp);
 bool stage_inner_twiddles(const PassParams& pp, bool recipe);

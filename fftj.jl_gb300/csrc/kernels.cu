@@ -122,23 +122,6 @@ cudaError_t launch_pass(const PassParams& pp, int dir, const void* fn, const voi
   const uint32_t grid = pp.tiles_q * pp.tiles_p * pp.tiles_b;
   const void* f = fn ? fn : generic_pass<T>(pp, dir);
   void* args[3] = {const_cast<PassParams*>(&pp), const_cast<void**>(&in), &out};
-  if (pp.cluster > 1) {
-    // adjacent tiles (neighbouring column strips) as one cluster: they are
-    // scheduled together, so their short row segments reach HBM together
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(pp.threads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = (unsigned)pp.cluster;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelExC(&cfg, f, args);
-  }
   return cudaLaunchKernel(f, dim3(grid), dim3(pp.threads), args, smem, st);
 }
 

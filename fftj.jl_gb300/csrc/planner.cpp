@@ -622,7 +622,6 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
     if (!one_pass) tmax = std::min<i64>(std::max<i64>(tmax, R * cfg.min_run), std::max<i64>(cfg.tile_cap, R));
     i64 cols = std::max<i64>(1, std::min<i64>(tmax / R, cfg.threads_max / Tf));
     if (wide) cols = kWideCols;  // the wide kernel's tile (its own CTA size)
-    pp.cluster = 0;
     if (Tf > cfg.threads_max) return fail(FFTJ_ERR_UNSUPPORTED, "pass radix needs too many threads");
     i64 Pt = 1, Qt = 1, NBt = 1;
     if (s == 1) {
@@ -654,10 +653,6 @@ int pass_geometry(PassParams& pp, bool f64, i64 R, i64 m, i64 s, i64 ncur, i64 n
     pp.tiles_b = (uint32_t)((nbatch + NBt - 1) / NBt);
     pp.ftq = FastDiv(pp.tiles_q);
     pp.ftp = FastDiv(pp.tiles_p);
-    if (wide && kWideCluster > 1 && pp.tiles_q % kWideCluster == 0) {
-      // clusters of neighbouring column strips (tile index = strip fastest)
-      pp.cluster = kWideCluster;
-    }
     const double ntiles = (double)pp.tiles_q * pp.tiles_p * pp.tiles_b;
     if (ntiles >= 2147483647.0) return fail(FFTJ_ERR_UNSUPPORTED, "grid too large");
     const i64 E = (i64)pp.NB * R;
