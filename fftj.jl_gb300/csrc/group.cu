@@ -264,13 +264,13 @@ uint32_t op_tiles(const Op& op) {
   return 0;
 }
 
-// tiles per queue item: about 8K elements of F32 / 4K of ComplexF64 pass
-// work (two tiles of the default size each), 2K elementwise elements, one
+// tiles per queue item: about 16K elements of F32 / 4K of ComplexF64 pass
+// work (four / two tiles of the default size), 2K elementwise elements, one
 // tile of solve chunks. All passes at 2K / 4K / 8K / 16K elements: 113.5 /
-// 109.8-111.1 / 111.0 / 116.3 ms for the uneven batch; 4K cost the F32
-// passes (one tile per item) what it saved on the ComplexF64 ones.
+// 109.8-111.1 / 111.0 / 116.3 ms for the uneven batch; F32 at 4K / 8K / 16K
+// with ComplexF64 at 4K: 15.9 / 13.7 / 13.3 ms of F32 c2c (107.1 ms step).
 uint32_t item_chunk(const Op& op, bool f64) {
-  const int64_t elems = f64 ? 4096 : 8192;
+  const int64_t elems = f64 ? 4096 : 16384;
   if (op.kind == OP_PASS) return (uint32_t)std::max<int64_t>(1, elems / ((int64_t)op.pp.NB * op.pp.R));
   if (op.kind == OP_SOLVE) return 1;
   return 8;
