@@ -561,20 +561,9 @@ struct Lay {
 template <typename T, int NBC>
 using LayC = Lay<T, NBC == 0 ? 1 : NBC>;
 
-// Inner twiddle table w_R^t as staged in shared memory: PAD places entry t at
-// t + t / 16, so that the reads at stride j across lanes of a first
-// sub-stage (twiddle j k for consecutive k) fall in distinct banks for even
-// j as well (8-byte entries: 16 per bank row); PAD = false is the plain table.
-template <typename T, bool PAD>
-struct TwA {
-  const Cx<T>* p;
-  __device__ __forceinline__ Cx<T> operator[](int i) const { return p[PAD ? i + (i >> 4) : i]; }
-};
-__host__ __device__ constexpr int tw_padded(int R) { return R + (R >> 4); }
-
-template <typename T, int DIR, int r, int S, int Rr, int TF, int NBC = 0, int SH = 0, class TW = const Cx<T>*>
+template <typename T, int DIR, int r, int S, int Rr, int TF, int NBC = 0, int SH = 0>
 __device__ __forceinline__ void substage_ct(Cx<T>* __restrict__ buf, const int b, const int kg, const int NB,
-                                            TW twR) {
+                                            const Cx<T>* __restrict__ twR) {
   constexpr int IPT = (Rr + TF - 1) / TF;
   constexpr int PP = pad_period<T>();
   const int jstride_in = Rr * NB;
@@ -1064,19 +1053,21 @@ __device__ __forceinline__ Cx<T> load_elem_off(const PassParams& pp, const void*
 
 // sub-stages 2 .. NS-DROP of a recipe (the first ran fused with the load;
 // DROP = 1 leaves the last one to the fused store)
-template <typename T, int DIR, int TF, int R, int S, int DROP, int NBC, int r, int... rest, class TW>
-__device__ __forceinline__ void run_mid_skip(Cx<T>* buf, const int b, const int kg, const int NB, TW twR) {
+template <typename T, int DIR, int TF, int R, int S, int DROP, int NBC, int r, int... rest>
+__device__ __forceinline__ void run_mid_skip(Cx<T>* buf, const int b, const int kg, const int NB,
+                                             const Cx<T>* twR) {
   if constexpr (sizeof...(rest) >= DROP) {
     if constexpr (sizeof...(rest) == 0) {
-      substage_ct<T, DIR, r, S, R / r, TF, NBC, 0, TW>(buf, b, kg, NB, twR);
+      substage_ct<T, DIR, r, S, R / r, TF, NBC>(buf, b, kg, NB, twR);
     } else {
-      substage_ct<T, DIR, r, S, R / r, TF, NBC, next_shift<r, rest...>(), TW>(buf, b, kg, NB, twR);
+      substage_ct<T, DIR, r, S, R / r, TF, NBC, next_shift<r, rest...>()>(buf, b, kg, NB, twR);
       run_mid_skip<T, DIR, TF, R, S * r, DROP, NBC, rest...>(buf, b, kg, NB, twR);
     }
   }
 }
-template <typename T, int DIR, int TF, int R, int S1, int DROP, int NBC, int r0, int... rest, class TW>
-__device__ __forceinline__ void run_mid_ct(Cx<T>* buf, const int b, const int kg, const int NB, TW twR) {
+template <typename T, int DIR, int TF, int R, int S1, int DROP, int NBC, int r0, int... rest>
+__device__ __forceinline__ void run_mid_ct(Cx<T>* buf, const int b, const int kg, const int NB,
+                                           const Cx<T>* twR) {
   if constexpr (sizeof...(rest) > 0) run_mid_skip<T, DIR, TF, R, S1, DROP, NBC, rest...>(buf, b, kg, NB, twR);
 }
 

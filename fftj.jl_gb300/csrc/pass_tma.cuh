@@ -144,8 +144,8 @@ __device__ __forceinline__ void tc16_b_operand(unsigned char* tcB, int tid, int 
 // the dense tile, writes the outputs (twiddled by w_R^(j k) in FP32) to the
 // padded layout as the FP32 sub-stage does. False (for every thread) when
 // the MMAs did not complete within the wait limit.
-template <int DIR, int MODE, int NBC, int R, int Rr, int nthr, class TW>
-__device__ __forceinline__ bool tc16_first(Cx<float>* buf, TW tw, unsigned char* tcB,
+template <int DIR, int MODE, int NBC, int R, int Rr, int nthr>
+__device__ __forceinline__ bool tc16_first(Cx<float>* buf, const Cx<float>* tw, unsigned char* tcB,
                                            uint64_t* tcbar, uint32_t tmem, uint32_t par, int tid, int b, int kg,
                                            uint64_t limit) {
   using T = float;
@@ -231,9 +231,8 @@ __device__ __forceinline__ bool tc16_first(Cx<float>* buf, TW tw, unsigned char*
 // batch entry), tensor (p, j, batch); MODE 2: tile = Q consecutive columns q
 // (P == 1, one batch entry), tensor (q, p, j, batch). NBC = the tile's
 // column count. The pass's inner twiddles w_R^t are staged in shared memory
-// once per CTA (up to R = 4096, 34 KB in the bank-padded layout of TwA: the
-// radix-4096 single pass then runs two CTAs per SM, measured faster than
-// three reading them through L1).
+// once per CTA (up to R = 4096, 32 KB: the radix-4096 single pass then runs
+// two CTAs per SM, measured faster than three reading them through L1).
 template <int R>
 __host__ __device__ constexpr bool tma_stages_twiddles() { return R <= 4096; }
 
@@ -266,17 +265,16 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
   Cx<T>* const sbase = reinterpret_cast<Cx<T>*>(tma_smem);
   const int bufE = pp.tma_buf;  // elements per buffer, a multiple of 16 (128 bytes)
   constexpr bool kStageTw = tma_stages_twiddles<R>();
-  constexpr int kTwE = kStageTw ? tw_padded(R) : 0;  // staged entries (bank-padded layout)
   Cx<T>* const twS = sbase + 2 * bufE;
-  uint64_t* const bar = reinterpret_cast<uint64_t*>(twS + kTwE);
-  const TwA<T, kStageTw> tw{kStageTw ? twS : reinterpret_cast<const Cx<T>*>(pp.twR)};
+  uint64_t* const bar = reinterpret_cast<uint64_t*>(twS + (kStageTw ? R : 0));
+  const Cx<T>* const tw = kStageTw ? twS : reinterpret_cast<const Cx<T>*>(pp.twR);
   const int tid = threadIdx.x;
   const int kg = tid / NB;
   const int b = tid - kg * NB;
   // tensor-core B operand after the kernel's own shared memory (A lives in
   // the tile buffer)
   unsigned char* const tcB =
-      tma_smem + tc_smem_offset((size_t)(2 * bufE + kTwE) * sizeof(Cx<T>) + 3 * sizeof(uint64_t));
+      tma_smem + tc_smem_offset((size_t)(2 * bufE + (kStageTw ? R : 0)) * sizeof(Cx<T>) + 3 * sizeof(uint64_t));
   uint64_t* const tcbar = reinterpret_cast<uint64_t*>(tcB + 8192);
   uint32_t* const tmem_slot = reinterpret_cast<uint32_t*>(tcbar + 1);
   const uint32_t ntiles = pp.tiles_q * pp.tiles_p * pp.tiles_b;
@@ -284,7 +282,7 @@ __device__ __forceinline__ void pass_tma(const PassParams& pp, const CUtensorMap
   const uint64_t limit = pp.tma_wait_ns;
   if constexpr (kStageTw) {
     const Cx<T>* twG = reinterpret_cast<const Cx<T>*>(pp.twR);
-    for (int t = tid; t < R; t += nthr) twS[t + (t >> 4)] = __ldg(twG + t);
+    for (int t = tid; t < R; t += nthr) twS[t] = __ldg(twG + t);
   }
   // bar[0], bar[1]: the two tile slots (real copies only); bar[2]: the test
   // hook (fftj_plan_debug_stall) -- armed once with bytes that never arrive,

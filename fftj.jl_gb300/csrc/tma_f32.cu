@@ -37,7 +37,7 @@ const RecipeEntry* tma_table(int dir, int* count) {
 }
 
 size_t tma_smem_bytes(const PassParams& pp) {
-  const int tw = pp.R <= 4096 ? tw_padded(pp.R) : 0;  // tma_stages_twiddles, bank-padded
+  const int tw = pp.R <= 4096 ? pp.R : 0;  // tma_stages_twiddles
   const size_t own = (size_t)(2 * pp.tma_buf + tw) * sizeof(Cx<float>) + 3 * sizeof(uint64_t);  // 3 mbarriers
   // the precision form's tensor-core operands follow (umma.cuh)
   return pp.tc == 1 ? tc_smem_offset(own) + tc_smem_bytes(pp.threads) : own;
