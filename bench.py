@@ -782,9 +782,18 @@ def run_uneven(args):
     # transform (the compute stream) and output copy (a third stream) are
     # ordered by events, so copies of one chunk overlap the transforms of
     # another.
-    h_in = torch.empty(in_buf.numel(), dtype=torch.uint8, pin_memory=True)
+    # pinned host arenas (23 GB a rank); where the host cannot pin that much
+    # (several ranks on one host) the copies run from pageable memory and the
+    # line says so
+    try:
+        h_in = torch.empty(in_buf.numel(), dtype=torch.uint8, pin_memory=True)
+        h_out = torch.empty(out_buf.numel(), dtype=torch.uint8, pin_memory=True)
+        host_mem = "pinned"
+    except RuntimeError:
+        h_in = torch.empty(in_buf.numel(), dtype=torch.uint8)
+        h_out = torch.empty(out_buf.numel(), dtype=torch.uint8)
+        host_mem = "pageable (pinning failed)"
     h_in.copy_(in_buf)
-    h_out = torch.empty(out_buf.numel(), dtype=torch.uint8, pin_memory=True)
     n_items = len(items)
     chunks = _chunks(in_offs, n_items, args.e2e_chunks)
     cgroups = [fftj.Group(plans[a:b], xs[a:b], ys[a:b], mode="persistent") for a, b in chunks]
@@ -933,9 +942,10 @@ def run_uneven(args):
             "e2e": {"value": round(e2e_value, 1), "unit": "GFLOP/s",
                     "h2d_bytes_per_step": int(in_offs[-1]), "d2h_bytes_per_step": int(out_offs[-1]),
                     "ms_per_step": round(e2e_ms, 3), "outputs_checked": bool(e2e_ok),
+                    "host_buffers": host_mem,
                     "schedule": "plans split into %d chunks of about equal bytes, each a persistent group; "
-                                "per chunk: H2D from pinned host (stream 1), group (stream 2), D2H to pinned "
-                                "host (stream 3), ordered by events" % nc},
+                                "per chunk: H2D from the host arena (stream 1), group (stream 2), D2H to the "
+                                "host arena (stream 3), ordered by events" % nc},
             "gpu_launches": int(inf.kernels) * args.steps,
             "clocks": clk.summary(),
             "detail": {"plans_seconds": round(t_plan, 1), "modes": modes, "by_kind": split,
