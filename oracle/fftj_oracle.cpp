@@ -1566,6 +1566,36 @@ static bool use_fs2(i64 n1, i64 n2, bool threaded) {
   return (f == 2 || f == 4 || f == 8) && n1 / f >= W;
 }
 
+// pencil_fused (src/ndplan.jl:46-54): would a per-pencil chain of length n,
+// built with the small-stride layout allowed, get the fused-edge 1-D
+// treatment? Its first stage is small when use_small (src/plan.jl:9-11)
+// holds at stride 1: radix 4 with n/4 a whole number of vectors.
+template <typename T>
+static bool pencil_fused(i64 n, const std::vector<Stage<T>>& stages) {
+  const int W = pick_width<T>();
+  if (stages.empty()) return false;
+  const int f = stages.back().radix;
+  const i64 slast = (f == 2 || f == 4 || f == 8) ? n / f : 0;
+  const bool small0 = stages[0].radix == 4 && 1 < W && n / 4 >= W && (n / 4) % W == 0;
+  return W > 1 && stages.size() >= 2 && stages[0].radix == 4 && small0 && (n >> 2) % W == 0 && slast >= W &&
+         slast % W == 0;
+}
+
+// _real_batched (src/ndplan.jl:343-353): the N-d real edge along dim 1 runs
+// batched (pencils as lanes, half-length chain without the small-stride
+// layout) when the half length is smooth and the batch fills the vector
+// lanes, unless the per-pencil chain is fused -- then only for 16-lane
+// vectors with an L2-resident working set.
+template <typename T>
+static bool real_batched(i64 n1, i64 B) {
+  const int W = pick_width<T>();
+  if (!(W > 1 && n1 % 2 == 0 && n1 >= 2 && B >= W)) return false;
+  const i64 h = n1 >> 1;
+  if (!factor_radices(h).ok) return false;
+  if (!pencil_fused<T>(h, build_stages<T>(h, -1, true))) return true;
+  return W >= 16 && (h + 1) * B * (i64)sizeof(T) <= ((i64)1 << 19);
+}
+
 template <typename T>
 struct NdPlan : PlanBase {
   int D;
@@ -1574,6 +1604,7 @@ struct NdPlan : PlanBase {
   i64 len;
   int nt;
   bool fs2 = false;  // 2-D plan in Fs2Plan order (use_fs2)
+  bool dim1_batched = false;  // the dim-1 pass runs the no-small chain with pencils as lanes
   std::vector<std::unique_ptr<DimPass<T>>> passes;
   std::vector<T> are, aim, bre, bim;
   // _ndplan (src/ndplan.jl:57-118); dims before first_dim are pure batch
@@ -1595,7 +1626,14 @@ struct NdPlan : PlanBase {
       ps->nd = nd; ps->Bi = Bi; ps->Bo = Bo;
       if (factor_radices(nd).ok) {
         ps->stages = build_stages<T>(nd, D, Bi == 1);
-        (void)W;
+        // a dim-1 chain without the fused edge runs transposed, pencils as
+        // lanes, on the chain built without the small-stride layout
+        // (src/ndplan.jl:72-77); the transposes move data only, so each
+        // pencil here runs that chain in place of the transposed sweep
+        if (Bi == 1 && Bo >= W && !pencil_fused<T>(nd, ps->stages)) {
+          ps->stages = build_stages<T>(nd, D, false);
+          if (passes.empty()) dim1_batched = true;
+        }
       } else {
         ps->fb.reset(new RsPass<T>(nd, D, Bi == 1 ? Bo : Bi));
       }
@@ -1608,6 +1646,10 @@ struct NdPlan : PlanBase {
         use_fs2<T>(dims[0], dims[1], nt > 1)) {
       fs2 = true;
       route = ORC_FS2;
+      // Fs2Plan's rows are the length-n1 chain as a 1-D plan builds it
+      // (src/fourstep.jl:531-536)
+      passes[0]->stages = build_stages<T>(dims[0], D, true);
+      dim1_batched = false;
       std::swap(passes[0], passes[1]);
     }
     are.resize(len); aim.resize(len); bre.resize(len); bim.resize(len);
@@ -1647,26 +1689,66 @@ struct NdPlan : PlanBase {
   }
 };
 
-// RfftNdPlan / IrfftNdPlan (src/ndplan.jl:355-519), per-pencil real edge.
+// RfftNdPlan / IrfftNdPlan (src/ndplan.jl:355-519). The real edge along
+// dim 1 runs per pencil through the 1-D real plan, or -- when real_batched
+// holds -- batched: the half-length chain built without the small-stride
+// layout on every pencil, then the split/merge post-pass (pre-pass for the
+// inverse) with the 1-D plan's twiddles. FFTJ runs the batched form on
+// transposed planes with the pencils as vector lanes; the transposes move
+// data only, so each pencil here runs the same arithmetic in its own row.
 template <typename T>
 struct RfftNd {
   std::vector<i64> rdims, cdims;
   i64 B;
-  std::unique_ptr<RfftPlan<T>> r1;
+  bool batched;
+  std::vector<Stage<T>> bstages;  // forward chain for h = n1/2 (no small layout)
+  std::unique_ptr<RfftPlan<T>> r1;  // 1-D plan (twiddle source when batched)
   std::unique_ptr<NdPlan<T>> rest;
-  std::vector<T> C;
+  std::vector<T> C, are, aim, bre, bim;
   RfftNd(const std::vector<i64>& dims, int nthreads) : rdims(dims) {
     cdims = dims;
     cdims[0] = dims[0] / 2 + 1;
     B = 1;
     for (size_t d = 1; d < dims.size(); ++d) B *= dims[d];
+    batched = real_batched<T>(dims[0], B);
     r1.reset(new RfftPlan<T>(dims[0], nthreads));
     rest.reset(new NdPlan<T>(cdims, -1, (T)1, nthreads, 1));
     C.resize(2 * cdims[0] * B);
+    if (batched) {
+      const i64 h = dims[0] / 2;
+      bstages = build_stages<T>(h, -1, false);
+      are.resize(h); aim.resize(h); bre.resize(h); bim.resize(h);
+    }
   }
   void exec(const T* X, T* Y) {
     i64 n1 = rdims[0], h1p = cdims[0];
-    for (i64 o = 0; o < B; ++o) r1->exec(X + o * n1, C.data() + 2 * o * h1p);
+    if (!batched) {
+      for (i64 o = 0; o < B; ++o) r1->exec(X + o * n1, C.data() + 2 * o * h1p);
+    } else {
+      const i64 h = n1 / 2;
+      const T half = (T)0.5;
+      for (i64 o = 0; o < B; ++o) {
+        const T* x = X + o * n1;
+        for (i64 j = 0; j < h; ++j) { are[j] = x[2 * j]; aim[j] = x[2 * j + 1]; }
+        bool sw = run_chain(are.data(), aim.data(), bre.data(), bim.data(), bstages, 0, bstages.size(), h, 1, 1,
+                            -1, 1);
+        const T* zr = sw ? bre.data() : are.data();
+        const T* zi = sw ? bim.data() : aim.data();
+        T* y = C.data() + 2 * o * h1p;
+        // _rfft_post_range! (src/stockham.jl:590-614)
+        y[0] = zr[0] + zi[0]; y[1] = 0;
+        y[2 * h] = zr[0] - zi[0]; y[2 * h + 1] = 0;
+        for (i64 k = 1; k < h; ++k) {
+          T ar = zr[k], ai = zi[k];
+          T br = zr[h - k], bi = -zi[h - k];
+          T xer = (ar + br) * half, xei = (ai + bi) * half;
+          T xor_ = (ar - br) * half, xoi = (ai - bi) * half;
+          T wr = r1->twr[k], wi = r1->twi[k];
+          y[2 * k] = xer + std::fma(wr, xoi, wi * xor_);
+          y[2 * k + 1] = xei + std::fma(wi, xoi, -(wr * xor_));
+        }
+      }
+    }
     rest->exec(C.data(), Y);
   }
 };
@@ -1674,23 +1756,63 @@ template <typename T>
 struct IrfftNd {
   std::vector<i64> rdims, cdims;
   i64 B;
+  bool batched;
+  T bpre = (T)1;                  // batched pre-pass factor, every normalization folded in
+  std::vector<Stage<T>> bstages;  // backward chain for h = n1/2 (no small layout)
   std::unique_ptr<IrfftPlan<T>> r1;
   std::unique_ptr<NdPlan<T>> rest;
-  std::vector<T> C;
+  std::vector<T> C, are, aim, bre, bim;
   IrfftNd(const std::vector<i64>& dims, bool normalized, int nthreads) : rdims(dims) {
     cdims = dims;
     cdims[0] = dims[0] / 2 + 1;
     B = 1;
     for (size_t d = 1; d < dims.size(); ++d) B *= dims[d];
     T restscale = normalized ? (T)1 / (T)B : (T)1;
+    batched = real_batched<T>(dims[0], B);
     r1.reset(new IrfftPlan<T>(dims[0], normalized, nthreads));
+    // the batched form skips the rest chain's output scale and the 1-D
+    // plan's normalization: 1/(n1 B) = restscale / n1 goes into the pre-pass
+    // (src/ndplan.jl:466-469)
+    if (batched) {
+      bpre = normalized ? restscale / (T)dims[0] : (T)1;
+      restscale = (T)1;
+      const i64 h = dims[0] / 2;
+      bstages = build_stages<T>(h, +1, false);
+      are.resize(h); aim.resize(h); bre.resize(h); bim.resize(h);
+    }
     rest.reset(new NdPlan<T>(cdims, +1, restscale, nthreads, 1));
     C.resize(2 * cdims[0] * B);
   }
   void exec(const T* X, T* y) {
     i64 n1 = rdims[0], h1p = cdims[0];
     rest->exec(X, C.data());
-    for (i64 o = 0; o < B; ++o) r1->exec(C.data() + 2 * o * h1p, y + o * n1);
+    if (!batched) {
+      for (i64 o = 0; o < B; ++o) r1->exec(C.data() + 2 * o * h1p, y + o * n1);
+      return;
+    }
+    const i64 h = n1 / 2;
+    const T pv = bpre;
+    for (i64 o = 0; o < B; ++o) {
+      const T* x = C.data() + 2 * o * h1p;
+      // _irfft_pre_range! (src/stockham.jl:633-655)
+      for (i64 k = 0; k < h; ++k) {
+        T ar = x[2 * k], ai = x[2 * k + 1];
+        T br = x[2 * (h - k)], bi = -x[2 * (h - k) + 1];
+        T xer = (ar + br) * pv, xei = (ai + bi) * pv;
+        T xdr = (ar - br) * pv, xdi = (ai - bi) * pv;
+        T wr = r1->twr[k], wi = r1->twi[k];
+        T tr = std::fma(wr, xdr, -(wi * xdi));
+        T ti = std::fma(wr, xdi, wi * xdr);
+        are[k] = xer - ti;
+        aim[k] = xei + tr;
+      }
+      bool sw = run_chain(are.data(), aim.data(), bre.data(), bim.data(), bstages, 0, bstages.size(), h, 1, 1, +1,
+                          1);
+      const T* zr = sw ? bre.data() : are.data();
+      const T* zi = sw ? bim.data() : aim.data();
+      T* yo = y + o * n1;
+      for (i64 j = 0; j < h; ++j) { yo[2 * j] = zr[j]; yo[2 * j + 1] = zi[j]; }
+    }
   }
 };
 
@@ -1897,6 +2019,15 @@ int orc_execute_rfft_nd(void* p, const void* x, void* y) {
 int orc_execute_irfft_nd(void* p, const void* x, void* y) {
   Handle* h = (Handle*)p;
   if (h->dtype == 0) h->in32->exec((const float*)x, (float*)y); else h->in64->exec((const double*)x, (double*)y);
+  return 0;
+}
+int orc_plan_nd_batched(void* p) {
+  Handle* h = (Handle*)p;
+  const bool f32 = h->dtype == 0;
+  if (h->kind == 3) return (f32 ? ((NdPlan<float>*)h->p32.get())->dim1_batched
+                                 : ((NdPlan<double>*)h->p64.get())->dim1_batched) ? 1 : 0;
+  if (h->kind == 4) return (f32 ? h->rn32->batched : h->rn64->batched) ? 1 : 0;
+  if (h->kind == 5) return (f32 ? h->in32->batched : h->in64->batched) ? 1 : 0;
   return 0;
 }
 

@@ -58,6 +58,9 @@ int orc_execute_nd(void* plan, const void* x, void* y);
 // N-d real: rfft (dims = real dims) and irfft/brfft (dims = real dims).
 void* orc_plan_rfft_nd(int dtype, int rank, const int64_t* dims, int nthreads);
 void* orc_plan_irfft_nd(int dtype, int rank, const int64_t* dims, int normalized, int nthreads);
+// 1 when the plan's dim-1 edge runs batched (pencils as lanes): the complex
+// dim-1 chain without the small-stride layout, or the batched real edge.
+int orc_plan_nd_batched(void* plan);
 int orc_execute_rfft_nd(void* plan, const void* x, void* y);
 int orc_execute_irfft_nd(void* plan, const void* x, void* y);
 

@@ -58,6 +58,7 @@ def lib():
         L.orc_plan_irfft_nd.argtypes = [i32, i32, ctypes.POINTER(i64), i32, i32]
         L.orc_execute_rfft_nd.argtypes = [vp, vp, vp]
         L.orc_execute_irfft_nd.argtypes = [vp, vp, vp]
+        L.orc_plan_nd_batched.argtypes = [vp]
         L.orc_dft_f64.argtypes = [i64, vp, vp, i32]
         L.orc_plan_hvdh.restype = vp
         L.orc_plan_hvdh.argtypes = [i32, i64, i32, i32, i32]
@@ -212,6 +213,14 @@ class PlanND:
         if self.kind not in ("fft", "ifft", "bfft"):
             return "NdPlan"
         return ROUTES[lib().orc_plan_route(self.h)]
+
+    @property
+    def batched(self):
+        """True when the dim-1 edge runs batched, pencils as lanes: the
+        complex dim-1 chain built without the small-stride layout
+        (src/ndplan.jl:72-77), or the batched real edge (_real_batched,
+        src/ndplan.jl:343-353)."""
+        return bool(lib().orc_plan_nd_batched(self.h))
 
     def __call__(self, x):
         cshape = tuple(reversed([self.dims[0] // 2 + 1] + self.dims[1:]))

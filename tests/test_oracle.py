@@ -298,3 +298,41 @@ def test_fs2_routing_and_parity(orc):
         assert rel_l2(y, ref) <= parity_tol(T, x.size), (T, shape)
         xi = orc.PlanND(T, list(reversed(shape)), "ifft")(y)
         assert rel_l2(xi, x) <= 2 * parity_tol(T, x.size)
+
+
+def test_batched_dim1_edges(orc):
+    """FFTJ's N-d plans run the dim-1 edge batched, pencils as vector lanes,
+    on a chain built without the small-stride layout: the complex dim-1 pass
+    when its per-pencil chain would not get the fused edge and the pencils
+    fill the lanes (src/ndplan.jl:72-77), and the real edge under
+    _real_batched (src/ndplan.jl:343-353), whose inverse folds every
+    normalization into the pre-pass factor (:466-469). The restated plans
+    choose the same way and match FP64 numpy within the parity bar."""
+    from conftest import parity_tol, rel_l2
+    # 128-bit host (4 F32 / 2 F64 lanes)
+    assert not orc.PlanND(np.float32, [64, 8], "rfft").batched       # h = 32: fused 4·8 pencil
+    assert orc.PlanND(np.float32, [48, 3, 3], "rfft").batched        # h = 24: 3·8, no fused edge
+    assert not orc.PlanND(np.float32, [48, 3, 3], "fft").batched     # 4·3·4: fused edge
+    assert orc.PlanND(np.float32, [12, 10], "fft").batched           # 4·3: one stride-1 radix 4 too short
+    assert not orc.PlanND(np.float32, [14, 2], "irfft").batched      # 2 pencils < 4 lanes
+    assert not orc.PlanND(np.float32, [256, 256, 256], "rfft").batched  # the 256^3 rfft: fused pencils
+    try:
+        orc.set_vector_bits(512)                                     # 16 F32 lanes
+        assert orc.PlanND(np.float32, [64, 32], "rfft").batched      # h = 32: no small first stage at W = 16
+        assert orc.PlanND(np.float32, [128, 16], "rfft").batched     # fused, but 65 x 16 x 4 B is L2-resident
+        assert not orc.PlanND(np.float32, [128, 2048], "rfft").batched  # fused and 532 KB > 512 KB
+    finally:
+        orc.set_vector_bits(128)
+    rng = np.random.default_rng(0xBA7)
+    for T in (np.float32, np.float64):
+        for dims in ([48, 3, 3], [40, 4], [12, 10], [2, 16], [1536, 8]):
+            shape = tuple(reversed(dims))
+            x = rng.standard_normal(shape)
+            n = x.size
+            Y = orc.PlanND(T, dims, "rfft")(x)
+            ref = np.fft.rfftn(x)
+            assert rel_l2(Y, ref) <= parity_tol(T, n), (T, dims)
+            assert rel_l2(orc.PlanND(T, dims, "irfft")(ref), x) <= parity_tol(T, n), (T, dims)
+            assert rel_l2(orc.PlanND(T, dims, "brfft")(ref), n * x) <= parity_tol(T, n), (T, dims)
+            xc = x + 1j * rng.standard_normal(shape)
+            assert rel_l2(orc.PlanND(T, dims, "fft")(xc), np.fft.fftn(xc)) <= parity_tol(T, n), (T, dims)
