@@ -1090,11 +1090,14 @@ struct RsPass {
 };
 
 // ---- Gaussian resampling: HvdhPlan (src/hvdh.jl) ----------------------------
-// Restated from the reference's mathematics and parameters; the reference's
-// SIMD code advances the Gaussian entries and spread weights by
-// multiplicative recurrences with exact re-seeds (src/hvdh.jl:472-510,
-// 397-418), which this restatement evaluates directly with exp() -- the same
-// values up to rounding.
+// Restated with the reference's own evaluation of the Gaussian entries: the
+// band's columns and the spread's weights advance by multiplicative
+// recurrences seeded exactly (by its polynomial exp, _vexp) every few
+// columns / vectors, lane by lane as its SIMD code runs them
+// (src/hvdh.jl:99-114, 337-470, 472-540). The batched pass along a strided
+// axis (HvPass, src/hvdh.jl:690-760) tabulates its spread weights with the
+// library exp instead, factors one cyclic chunk, and transforms with the
+// no-small chain; HvdhPlan's pass form restates that.
 static i64 gcd_i(i64 a, i64 b) {
   a = a < 0 ? -a : a; b = b < 0 ? -b : b;
   while (b) { i64 t = a % b; a = b; b = t; }
@@ -1112,6 +1115,43 @@ static i64 invmod_i(i64 a, i64 m) {  // a^{-1} mod m, gcd(a, m) = 1
 static i64 fld_i(i64 a, i64 b) { i64 q = a / b; if ((a % b != 0) && ((a < 0) != (b < 0))) q--; return q; }
 static i64 cld_i(i64 a, i64 b) { return -fld_i(-a, b); }
 static i64 mod_i(i64 a, i64 m) { i64 r = a % m; return r < 0 ? r + m : r; }
+
+// _vexp (src/hvdh.jl:99-114): exp for |x| <~ 10 by Cody-Waite reduction by
+// ln 2 (hi + lo split) and a Taylor polynomial in Horner form, 14 terms for
+// Float64 and 8 for Float32, scaled by 2^k built from the exponent bits.
+static double fact_inv(int j) {  // 1 / j!, j! exact in a double for j <= 13
+  double f = 1;
+  for (int i = 2; i <= j; ++i) f *= i;
+  return 1.0 / f;
+}
+template <typename T>
+static T vexp(T x);
+template <>
+inline double vexp<double>(double x) {
+  static const struct C { double c[14]; C() { for (int j = 0; j < 14; ++j) c[j] = fact_inv(j); } } k;
+  const double kf = std::nearbyint(x * 1.4426950408889634);
+  double r = std::fma(kf, -6.93147180369123816490e-01, x);
+  r = std::fma(kf, -1.90821492927058770002e-10, r);
+  double p = k.c[13];
+  for (int j = 12; j >= 0; --j) p = std::fma(p, r, k.c[j]);
+  const uint64_t bits = (uint64_t)((int64_t)kf + 1023) << 52;
+  double sc;
+  std::memcpy(&sc, &bits, sizeof sc);
+  return p * sc;
+}
+template <>
+inline float vexp<float>(float x) {
+  static const struct C { float c[8]; C() { for (int j = 0; j < 8; ++j) c[j] = (float)fact_inv(j); } } k;
+  const float kf = std::nearbyint(x * (float)1.4426950408889634);
+  float r = std::fma(kf, -(float)0.693145751953125, x);
+  r = std::fma(kf, -(float)1.428606765330187045e-6, r);
+  float p = k.c[7];
+  for (int j = 6; j >= 0; --j) p = std::fma(p, r, k.c[j]);
+  const uint32_t bits = (uint32_t)((int32_t)kf + 127) << 23;
+  float sc;
+  std::memcpy(&sc, &bits, sizeof sc);
+  return p * sc;
+}
 
 static const double HVDH_THETA_MIN = 1.0 / 128;  // src/hvdh.jl:67
 static const i64 HVDH_LTARGET = 256;             // src/hvdh.jl:68
@@ -1203,21 +1243,33 @@ static void hvdh_e(i64 n, i64 t, i64 q, i64* e, i64* l) {
 
 // HvdhPlan (src/hvdh.jl:30-58, 153-230): scatter, Gaussian spread onto the
 // t-grid, length-t transform, banded solve by chunks (K chunks per group,
-// L core rows + H halo rows per side), scale n/t.
+// L core rows + H halo rows per side), scale n/t. The pass form is the
+// batched HvPass's arithmetic for one lane (_hv_parts / _hv_chunk!,
+// src/hvdh.jl:727-836): K = 1 and one cyclic chunk (G = 1, L = t),
+// tabulated spread weights accumulated tap by tap, the length-t chain
+// without the small-stride layout, output scale T(n/t).
 template <typename T>
 struct HvdhPlan : PlanBase {
   int D;
   T scale;
-  i64 t, Delta, c, h, w, B, H, K, G, L, R;
+  bool pass_form;
+  i64 t, Delta, c, h, w, B, H, K, G, L, R, rsm;
   double alpha, a, b;
+  T aT, dT;                  // T(a), T(Delta/n): the column seeds' arguments
+  T rc[7];                   // column-recurrence factors (_hvdh_step)
+  std::vector<T> chT;        // ch[d] = exp(-a d^2), d = 1..B
   std::vector<i64> se, sx, so;
   std::unique_ptr<PlanBase> pt;
+  std::vector<Stage<T>> tstages;  // pass form: the length-t chain
   bool tab;  // factors precomputed (:table) or rebuilt per call (:fly)
   // per chunk: multipliers f[i][k] (k = 1..B), 1/U_ii, U_{i,i+1..i+B}, output index
   std::vector<T> lt, ut;
   std::vector<i64> ot;
+  static const i64 kReseed = 4;   // _HVDH_RESEED (src/hvdh.jl:70)
+  static const i64 kSReseed = 8;  // _HVDH_SRESEED (src/hvdh.jl:72)
+  static const i64 kJ = 8;        // spread rows per block (_hvdh_spread!'s J)
   // factors: 0 :auto, 1 :table, 2 :fly (src/hvdh.jl:187-191)
-  HvdhPlan(i64 n_, int D_, T scale_, int factors) : D(D_), scale(scale_) {
+  HvdhPlan(i64 n_, int D_, T scale_, int factors, bool pass = false) : D(D_), scale(scale_), pass_form(pass) {
     n = n_;
     route = ORC_HVDH;
     t = hvdh_t(n);
@@ -1225,7 +1277,7 @@ struct HvdhPlan : PlanBase {
     Delta = t - n;
     c = invmod_i(Delta, n);
     alpha = sizeof(T) >= 8 ? 1.45 : 1.0;  // _hvdh_alpha (src/hvdh.jl:64)
-    a = M_PI * alpha * alpha;
+    a = M_PI * (alpha * alpha);
     b = M_PI / (alpha * alpha);
     const double tol = (sizeof(T) >= 8 ? 2.220446049250313e-16 : 1.1920928955078125e-07) / 4;
     h = (i64)std::ceil(alpha * std::sqrt(std::log(1 / tol) / M_PI));
@@ -1233,10 +1285,18 @@ struct HvdhPlan : PlanBase {
     B = (i64)std::floor(std::sqrt(std::log(1 / tol) / a) + 0.5);
     if (2 * B + 1 > 8) throw std::invalid_argument("band too wide");
     H = hvdh_halo(n, t, a, B, tol);
-    K = pick_width<T>();
-    G = std::max<i64>(1, cld_i(t, K * HVDH_LTARGET));
+    K = pass ? 1 : pick_width<T>();
+    G = pass ? 1 : std::max<i64>(1, cld_i(t, K * HVDH_LTARGET));
     L = cld_i(t, K * G);
     R = L + 2 * H;
+    rsm = kReseed - 1;
+    const double d = (double)Delta / (double)n;
+    aT = (T)a;
+    dT = (T)d;
+    const double rcd[7] = {std::exp(2 * a), std::exp(-2 * a), std::exp(-a), std::exp(2 * a * d),
+                           std::exp(-2 * a * d), std::exp(-a * (d * d)), std::exp(-2 * a * (d * d))};
+    for (int k = 0; k < 7; ++k) rc[k] = (T)rcd[k];
+    for (i64 dd = 1; dd <= B; ++dd) chT.push_back((T)std::exp(-a * (double)(dd * dd)));
     se.resize(G * K); sx.resize(G * K); so.resize(G * K);
     for (i64 ch = 0; ch < G * K; ++ch) {
       const i64 q0 = mod_i(ch * L - H, t);
@@ -1247,46 +1307,72 @@ struct HvdhPlan : PlanBase {
       hvdh_e(n, t, q0, &e, &l);
       so[ch] = mod_i((i64)((__int128)Delta * l % n), n);
     }
-    pt.reset(anyplan<T>(t, D, (T)1, 1));
+    if (pass) tstages = build_stages<T>(t, D, false);
+    else pt.reset(anyplan<T>(t, D, (T)1, 1));
     const i64 ufl = (R + B) * (B + 1) * K;
     const i64 tbytes = G * (R * B * K * (i64)sizeof(T) + ufl * (i64)sizeof(T) + R * K * 8);
-    tab = factors == 1 || (factors == 0 && tbytes <= HVDH_TABLE_MAX);
+    tab = pass || factors == 1 || (factors == 0 && tbytes <= HVDH_TABLE_MAX);
     if (tab) {
       lt.resize(G * K * R * B); ut.resize(G * K * R * (B + 1)); ot.resize(G * K * R);
       for (i64 ch = 0; ch < G * K; ++ch)
         factor(ch, &lt[ch * R * B], &ut[ch * R * (B + 1)], &ot[ch * R]);
     }
   }
-  // the band of chunk ch, eliminated row by row without pivoting
-  // (_hvdh_prime!, _hvdh_row!, _hvdh_factor!: src/hvdh.jl:500-540, 617-633)
+  // column state at e, beta' = (e - n)/2n: (G, 1/G, A', Hh) = (exp(-2a beta'),
+  // exp(2a beta'), exp(-a beta'^2), exp(-2a beta' delta)) (_hvdh_seed,
+  // src/hvdh.jl:472-479)
+  struct Col { T g, gi, A, hh; };
+  Col seed(i64 e) const {
+    const T beta = (T)(e - n) * (T)(1.0 / (2.0 * (double)n));
+    Col s;
+    s.g = vexp<T>((T)(-2) * aT * beta);
+    s.gi = (T)1 / s.g;
+    s.A = vexp<T>(-aT * beta * beta);
+    s.hh = vexp<T>((T)(-2) * aT * dT * beta);
+    return s;
+  }
+  // one column on: off the unknowns e -= 2n, on one e += 2 Delta
+  // (_hvdh_step, src/hvdh.jl:481-496; rc = exp of 2a, -2a, -a, 2ad, -2ad, -ad^2, -2ad^2)
+  void step(i64& e, Col& s) const {
+    const bool hit = e < 2 * n;
+    s.A *= hit ? s.hh * rc[5] : s.gi * rc[2];
+    s.g *= hit ? rc[4] : rc[0];
+    s.gi *= hit ? rc[3] : rc[1];
+    s.hh *= hit ? rc[6] : rc[3];
+    e = hit ? e + 2 * Delta : e - 2 * n;
+  }
+  // the band of chunk ch, built from a ring of 8 columns and eliminated row
+  // by row without pivoting (_hvdh_prime!, _hvdh_row!, _hvdh_factor!:
+  // src/hvdh.jl:498-560, 637-654)
   void factor(i64 ch, T* lf, T* uf, i64* ob) const {
-    // column j (relative to the chunk's first row, j in [-B, R + B)):
-    // beta' = (e - n) / 2n, an unknown sits there when e < 2n
-    const i64 nc = R + 2 * B;
-    std::vector<double> beta(nc);
-    std::vector<char> hit(nc);
+    T rA[8], rG[8], rGi[8];  // A' (0 off the unknowns), G, 1/G per ring slot
+    auto put = [&](i64 slot, i64 e, const Col& s) {
+      rA[slot] = e < 2 * n ? s.A : (T)0;
+      rG[slot] = s.g;
+      rGi[slot] = s.gi;
+    };
     i64 e = se[ch];
-    for (i64 j = 0; j < nc; ++j) {
-      hit[j] = e < 2 * n;
-      beta[j] = (double)(e - n) / (2.0 * n);
-      e = hit[j] ? e + 2 * Delta : e - 2 * n;
-    }
+    Col cs = seed(e);
+    for (i64 cc = -B; cc < B; ++cc) { put(cc & 7, e, cs); step(e, cs); }
     i64 on = so[ch];
     // rows -B .. -1: identity pads
     std::vector<T> U((R + B) * (B + 1), (T)0);
     for (i64 i = 0; i < B; ++i) U[i * (B + 1)] = (T)1;
+    std::vector<T> r(2 * B + 1);
     for (i64 i = 0; i < R; ++i) {
-      const i64 ci = i + B;  // column index of row i
-      std::vector<T> r(2 * B + 1, (T)0);
-      if (hit[ci]) {
-        for (i64 m = -B; m <= B; ++m) {
-          const i64 cj = ci + m;
-          if (!hit[cj]) continue;
-          const double d = (double)m + beta[cj];
-          r[m + B] = (T)std::exp(-a * d * d);
-        }
-      } else {
-        r[B] = (T)1;
+      if (((i + 2 * B) & rsm) == 0) cs = seed(e);
+      put((i + B) & 7, e, cs);
+      step(e, cs);
+      const T Aq = rA[i & 7];
+      const bool hit = Aq > (T)0;
+      // entry at column i + m: exp(-a m^2) A' G^m
+      for (i64 m = -B; m <= B; ++m) {
+        if (m == 0) { r[B] = hit ? Aq : (T)1; continue; }
+        const i64 o = (i + m) & 7;
+        const T gc = m > 0 ? rG[o] : rGi[o];
+        T gm = gc;
+        for (i64 k = 2; k <= (m < 0 ? -m : m); ++k) gm *= gc;
+        r[m + B] = hit ? chT[(m < 0 ? -m : m) - 1] * rA[o] * gm : (T)0;
       }
       for (i64 k = B; k >= 1; --k) {
         const T* ur = &U[(i - k + B) * (B + 1)];
@@ -1298,8 +1384,109 @@ struct HvdhPlan : PlanBase {
       ur[0] = (T)1 / r[B];
       for (i64 j = 1; j <= B; ++j) ur[j] = r[B + j];
       for (i64 j = 0; j <= B; ++j) uf[i * (B + 1) + j] = ur[j];
-      ob[i] = hit[ci] ? on : -1;
-      if (hit[ci]) { on += Delta; if (on >= n) on -= n; }
+      ob[i] = hit ? on : -1;
+      if (hit) { on += Delta; if (on >= n) on -= n; }
+    }
+  }
+  // _hvdh_spread! (src/hvdh.jl:337-470): v[q] = sum over taps o of
+  // exp(-b (delta_q - o)^2) / alpha * ys[(q + (o - 1) Delta) mod n],
+  // delta_q = (t - q) / t, o = 1 - w/2 .. w/2, rows q = i Delta + j in blocks
+  // of J rows, V lanes along j; per lane E = exp(-b delta^2)/alpha, G =
+  // exp(2b delta), 1/G, R = exp(2b kappa delta - b kappa^2), Hr = exp(2b
+  // theta delta) advance by constant factors per vector and are re-seeded
+  // every kSReseed vectors; row g's weights follow row 0's by Hr and
+  // constants; tap weights E G^o exp(-b o^2), the centre tap first, then
+  // o = 1, 2, .., then o = -1, -2, ...
+  void spread_rec(const std::vector<T>& ys, std::vector<T>& v) const {
+    const i64 V = pick_width<T>(), J = kJ, rs = kSReseed, hw = w / 2;
+    const double th = (double)Delta / (double)t, ka = (double)V / (double)t;
+    const T fE = (T)std::exp(-2 * b * (ka * ka)), fG = (T)std::exp(-2 * b * ka), fGi = (T)std::exp(2 * b * ka),
+            fH = (T)std::exp(-2 * b * th * ka);
+    std::vector<T> kc(w + 1);  // kc[o + hw], o = 1 - hw .. hw
+    for (i64 o = 1 - hw; o <= hw; ++o) kc[o + hw] = (T)std::exp(-b * (double)(o * o));
+    std::vector<T> gc1(J), gc2(J), gc3(J);
+    for (i64 g = 0; g < J; ++g) {
+      const double gt = (double)g * th;
+      gc1[g] = (T)std::exp(-b * (gt * gt));
+      gc2[g] = (T)std::exp(-2 * b * (double)g * th);
+      gc3[g] = (T)std::exp(2 * b * (double)g * th);
+    }
+    const T bT = (T)b, b2T = (T)(2 * b), rkT = (T)(2 * b * ka), rk2T = (T)(b * (ka * ka)), hT = (T)(2 * b * th);
+    const T it = (T)(1.0 / (double)t), ia = (T)(1.0 / alpha);
+    const i64 nseg = cld_i(Delta, rs * V);
+    const i64 nblk = cld_i(cld_i(t, Delta), J);
+    std::vector<T> E(V), Gv(V), Gi(V), Rv(V), Hv(V);
+    for (i64 ib = 0; ib < nblk; ++ib)
+      for (i64 seg = 0; seg < nseg; ++seg) {
+        const i64 i0 = J * ib;
+        i64 j = seg * rs * V;
+        const i64 jend = std::min(Delta, j + rs * V);
+        for (i64 blk = 0; j < jend; j += V, ++blk) {
+          if ((blk & (rs - 1)) == 0)
+            for (i64 s = 0; s < V; ++s) {
+              const T dl = (T)((t - i0 * Delta - j) - s) * it;
+              E[s] = vexp<T>(-bT * dl * dl) * ia;
+              Gv[s] = vexp<T>(b2T * dl);
+              Gi[s] = vexp<T>(-b2T * dl);
+              Rv[s] = vexp<T>(rkT * dl - rk2T);
+              Hv[s] = vexp<T>(hT * dl);
+            }
+          for (i64 s = 0; s < V; ++s) {
+            T F = E[s];
+            for (i64 g = 0; g < J; ++g) {
+              if (g > 0) F *= Hv[s];
+              const i64 lim = std::min(std::max<i64>(t - (i0 + g) * Delta, 0), Delta);
+              if (j + s >= lim) continue;  // past the row's end or t
+              const T Eg = F * gc1[g], Gg = Gv[s] * gc2[g], Gig = Gi[s] * gc3[g];
+              auto at = [&](i64 o) { return mod_i((i0 + g + o - 1) * Delta + j + s, n); };
+              const i64 m0 = at(0);
+              T re = Eg * ys[2 * m0], im = Eg * ys[2 * m0 + 1];
+              T P = Eg;
+              for (i64 o = 1; o <= hw; ++o) {
+                P *= Gg;
+                const T W = P * kc[o + hw];
+                const i64 m = at(o);
+                re = std::fma(W, ys[2 * m], re);
+                im = std::fma(W, ys[2 * m + 1], im);
+              }
+              P = Eg;
+              for (i64 o = -1; o >= 1 - hw; --o) {
+                P *= Gig;
+                const T W = P * kc[o + hw];
+                const i64 m = at(o);
+                re = std::fma(W, ys[2 * m], re);
+                im = std::fma(W, ys[2 * m + 1], im);
+              }
+              const i64 q = (i0 + g) * Delta + j + s;
+              v[2 * q] = re; v[2 * q + 1] = im;
+            }
+          }
+          for (i64 s = 0; s < V; ++s) {
+            E[s] *= Rv[s];
+            Rv[s] *= fE;
+            Gv[s] *= fG;
+            Gi[s] *= fGi;
+            Hv[s] *= fH;
+          }
+        }
+      }
+  }
+  // HvPass's tabulated weights T(exp(-b (delta_q - o)^2) / alpha), summed
+  // tap by tap from o = 1 - w/2 (_hv_parts, _rows_spread!: src/hvdh.jl:
+  // 743-750, 856-871)
+  void spread_tab(const std::vector<T>& ys, std::vector<T>& v) const {
+    const i64 hw = w / 2;
+    for (i64 q = 0; q < t; ++q) {
+      const double dq = (double)(t - q) / (double)t;
+      T re = 0, im = 0;
+      for (i64 o = 1 - hw; o <= hw; ++o) {
+        const double d = dq - (double)o;
+        const T wt = (T)(std::exp(-b * (d * d)) / alpha);
+        const i64 m = mod_i(q + (o - 1) * Delta, n);
+        re = std::fma(wt, ys[2 * m], re);
+        im = std::fma(wt, ys[2 * m + 1], im);
+      }
+      v[2 * q] = re; v[2 * q + 1] = im;
     }
   }
   void exec(const void* xv, void* yv) override {
@@ -1311,31 +1498,27 @@ struct HvdhPlan : PlanBase {
       const i64 m = (i64)((__int128)l * Delta % n);
       ys[2 * m] = x[2 * l]; ys[2 * m + 1] = x[2 * l + 1];
     }
-    // _hvdh_spread! (src/hvdh.jl:337-470): v[q] = sum over taps o of
-    // exp(-b (delta_q - o)^2) / alpha * ys[(q + (o - 1) Delta) mod n],
-    // delta_q = (t - q) / t, o = 1 - w/2 .. w/2
     std::vector<T> v(2 * t), Y(2 * t);
-    const i64 hw = w / 2;
-    for (i64 q = 0; q < t; ++q) {
-      const double dq = (double)(t - q) / (double)t;
-      T re = 0, im = 0;
-      for (i64 o = 1 - hw; o <= hw; ++o) {
-        const double d = dq - (double)o;
-        const T wt = (T)(std::exp(-b * d * d) / alpha);
-        const i64 m = mod_i(q + (o - 1) * Delta, n);
-        re = std::fma(wt, ys[2 * m], re);
-        im = std::fma(wt, ys[2 * m + 1], im);
-      }
-      v[2 * q] = re; v[2 * q + 1] = im;
+    if (pass_form) {
+      spread_tab(ys, v);
+      std::vector<T> are(t), aim(t), bre(t), bim(t);
+      for (i64 q = 0; q < t; ++q) { are[q] = v[2 * q]; aim[q] = v[2 * q + 1]; }
+      const bool sw = run_chain(are.data(), aim.data(), bre.data(), bim.data(), tstages, 0, tstages.size(), t, 1, 1,
+                                D, 1);
+      const T* cr = sw ? bre.data() : are.data();
+      const T* ci = sw ? bim.data() : aim.data();
+      for (i64 q = 0; q < t; ++q) { Y[2 * q] = cr[q]; Y[2 * q + 1] = ci[q]; }
+    } else {
+      spread_rec(ys, v);
+      pt->exec(v.data(), Y.data());
     }
-    pt->exec(v.data(), Y.data());
     // _hvdh_groups! -> _hvdh_subst! / _hvdh_group!, _hvdh_back!
     // (src/hvdh.jl:232-240, 560-686)
     std::vector<T> lf, uf;
     std::vector<i64> ob;
     if (!tab) { lf.resize(R * B); uf.resize(R * (B + 1)); ob.resize(R); }
     std::vector<T> zr(R + 2 * B), zi(R + 2 * B);
-    const T sc = scale * (T)n / (T)t;
+    const T sc = pass_form ? (T)((double)n / (double)t) : scale * (T)n / (T)t;
     for (i64 ch = 0; ch < G * K; ++ch) {
       const T* L_ = tab ? &lt[ch * R * B] : lf.data();
       const T* U_ = tab ? &ut[ch * R * (B + 1)] : uf.data();
@@ -1426,8 +1609,8 @@ struct TwoLevel {
 // w_n^(j1 k2), then the length-p transforms over j1 for each k2 by
 // resampling -- batched HvdH (HvPass) for p >= 500, else batched
 // oversampled resampling (RsPass). The restatement runs each lane's
-// length-p transform with the single-transform HvdH plan (the batched pass
-// shares its weights and factors one cyclic band; same mathematics).
+// length-p transform through HvdhPlan's pass form, the HvPass arithmetic
+// for one lane (tabulated weights, one cyclic band, the no-small chain).
 template <typename T>
 struct CompositePlan : PlanBase {
   int D;
@@ -1443,7 +1626,7 @@ struct CompositePlan : PlanBase {
     s = smooth_part(n);
     p = n / s;
     stages = build_stages<T>(s, D, false);
-    if (p >= COMPOSITE_HV_MINP) hv.reset(new HvdhPlan<T>(p, D, (T)1, 0));
+    if (p >= COMPOSITE_HV_MINP) hv.reset(new HvdhPlan<T>(p, D, (T)1, 1, true));
     else rs.reset(new RsPass<T>(p, D, s));
   }
   void exec(const void* xv, void* yv) override {
