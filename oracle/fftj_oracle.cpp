@@ -1057,14 +1057,17 @@ struct RsPass {
     m = parts.m; w = parts.w;
     stages = build_stages<T>(m, D, B == 1);
   }
-  // rows of B lanes at xre/xim + off (row j lane i at off + B*j + i), in place
-  void run(T* xre, T* xim, i64 off, int D) {
+  // rows of B lanes at xre/xim + off (row j lane i at off + B*j + i), in
+  // place. load(j, i, c, xr, xi, &yr, &yi), when given, replaces the
+  // deconvolution x c of row j, lane i (CompositePlan folds its twiddles in).
+  template <class Load>
+  void run(T* xre, T* xim, i64 off, int D, Load load) {
     std::vector<T> pre(m * B), pim(m * B), qre(m * B), qim(m * B);
     i64 hp = (n + 1) / 2;
     for (i64 j = 0; j < n; ++j) {
       i64 jj = j < hp ? j : m - n + j;
       T c = parts.corr[j];
-      for (i64 i = 0; i < B; ++i) { pre[B * jj + i] = xre[off + B * j + i] * c; pim[B * jj + i] = xim[off + B * j + i] * c; }
+      for (i64 i = 0; i < B; ++i) load(j, i, c, xre[off + B * j + i], xim[off + B * j + i], &pre[B * jj + i], &pim[B * jj + i]);
     }
     for (i64 j = hp; j < m - n + hp; ++j)
       for (i64 i = 0; i < B; ++i) { pre[B * j + i] = 0; pim[B * j + i] = 0; }
@@ -1086,6 +1089,9 @@ struct RsPass {
         xim[off + B * k + i] = ai;
       }
     }
+  }
+  void run(T* xre, T* xim, i64 off, int D) {
+    run(xre, xim, off, D, [](i64, i64, T c, T xr, T xi, T* yr, T* yi) { *yr = xr * c; *yi = xi * c; });
   }
 };
 
@@ -1604,6 +1610,64 @@ struct TwoLevel {
   }
 };
 
+// Lane twiddles lv[W r + l] = w_n^(r l), l < W lanes (src/composite.jl:
+// 76-80, 162-167).
+template <typename T>
+struct LaneTw {
+  i64 W;
+  std::vector<T> lr, li;
+  LaneTw(i64 n, i64 rows, int D) : W(pick_width<T>()) {
+    lr.resize(W * rows); li.resize(W * rows);
+    for (i64 r = 0; r < rows; ++r)
+      for (i64 l = 0; l < W; ++l) {
+        double sn, cs;
+        sincospi((double)(2 * D * (r * l)) / (double)n, &sn, &cs);
+        lr[W * r + l] = (T)cs; li[W * r + l] = (T)sn;
+      }
+  }
+};
+
+// x (c w_n^(r k)) for lane k of a run of L lanes from lane0, as FFTJ's
+// W-lane windows build it (_rows_scale_tw!, _split_twiddle!:
+// src/composite.jl:239-301): the window's first lane k0 by the two-level
+// table, times the lane twiddle w_n^(r (k - k0)), with c folded in; windows
+// step by W and the last one overlaps the previous, its values the ones
+// kept. Runs shorter than W take the scalar form c (x w).
+template <typename T>
+static void tw_window(const TwoLevel<T>& tw, const LaneTw<T>& lv, T c, i64 r, i64 k, i64 lane0, i64 L, T xr, T xi,
+                      T* yr, T* yi) {
+  const i64 W = lv.W;
+  if (W > 1 && L >= W) {
+    const i64 rel = k - lane0;
+    const i64 k0 = lane0 + (rel >= L - W ? L - W : rel / W * W);
+    T ar, ai;
+    tw.at(r * k0, &ar, &ai);
+    const T vr = lv.lr[W * r + (k - k0)], vi = lv.li[W * r + (k - k0)];
+    const T car = c * ar, cai = c * ai;
+    const T twr = std::fma(car, vr, -(cai * vi));
+    const T twi = std::fma(car, vi, cai * vr);
+    *yr = std::fma(xr, twr, -(xi * twi));
+    *yi = std::fma(xr, twi, xi * twr);
+  } else {
+    T wr, wi;
+    tw.at(r * k, &wr, &wi);
+    *yr = c * (xr * wr - xi * wi);
+    *yi = c * (xr * wi + xi * wr);
+  }
+}
+
+// lanes per chunk of a batched resampling pass over B lanes whose work
+// rows number M (_rs_pass / _hv_pass, src/resample.jl:453-461,
+// src/hvdh.jl:752-755); the last chunk takes the rest
+static const i64 RS_CHUNK_MAX = 1 << 19;
+template <typename T>
+static i64 rs_chunk_lanes(i64 M, i64 B) {
+  const i64 W = pick_width<T>();
+  if (B < 2 * W) return B;
+  const i64 c = RS_CHUNK_MAX / (4 * M * (i64)sizeof(T)) / W * W;
+  return std::min(std::max(c, W), B / W * W);
+}
+
 // CompositePlan (src/composite.jl:10-101): n = p s, j = j1 + p j2,
 // k = k2 + s k1: length-s transforms over j2 (batch p), twiddles
 // w_n^(j1 k2), then the length-p transforms over j1 for each k2 by
@@ -1620,11 +1684,13 @@ struct CompositePlan : PlanBase {
   std::unique_ptr<HvdhPlan<T>> hv;
   std::unique_ptr<RsPass<T>> rs;
   TwoLevel<T> tw;
+  std::unique_ptr<LaneTw<T>> lv;
   CompositePlan(i64 n_, int D_, T scale_) : D(D_), scale(scale_), tw(n_, D_) {
     n = n_;
     route = ORC_COMPOSITE;
     s = smooth_part(n);
     p = n / s;
+    lv.reset(new LaneTw<T>(n, p, D));
     stages = build_stages<T>(s, D, false);
     if (p >= COMPOSITE_HV_MINP) hv.reset(new HvdhPlan<T>(p, D, (T)1, 1, true));
     else rs.reset(new RsPass<T>(p, D, s));
@@ -1637,23 +1703,33 @@ struct CompositePlan : PlanBase {
     const bool sw = run_chain(are.data(), aim.data(), bre.data(), bim.data(), stages, 0, stages.size(), s, 1, p, D, 1);
     const T* cre = sw ? bre.data() : are.data();
     const T* cim = sw ? bim.data() : aim.data();
-    // c[j1 + p k2] -> o[k2 + s j1] with the twiddle w_n^(j1 k2)
+    // c[j1 + p k2] -> o[k2 + s j1]; the twiddle w_n^(j1 k2) is applied in
+    // the resampling pass's load, per chunk of lanes (_rs_chunk! /
+    // _hv_chunk! with _rows_scale_tw!)
     std::vector<T> ore(n), oim(n);
     for (i64 k2 = 0; k2 < s; ++k2)
-      for (i64 j1 = 0; j1 < p; ++j1) {
-        T wr, wi;
-        tw.at(j1 * k2, &wr, &wi);
-        const T zr = cre[j1 + p * k2], zi = cim[j1 + p * k2];
-        ore[k2 + s * j1] = zr * wr - zi * wi;
-        oim[k2 + s * j1] = zr * wi + zi * wr;
-      }
+      for (i64 j1 = 0; j1 < p; ++j1) { ore[k2 + s * j1] = cre[j1 + p * k2]; oim[k2 + s * j1] = cim[j1 + p * k2]; }
+    const i64 M = rs ? rs->m : std::max(hv->t, hv->R + 2 * hv->B);
+    const i64 C = rs_chunk_lanes<T>(M, s), nc = std::max<i64>(1, s / C);
+    auto chunk = [&](i64 k2, i64* lane0, i64* L) {
+      const i64 c = std::min(k2 / C, nc - 1);
+      *lane0 = c * C;
+      *L = c == nc - 1 ? s - c * C : C;
+    };
     if (rs) {
-      rs->run(ore.data(), oim.data(), 0, D);  // rows j1 of s lanes k2, in place: rows k1
+      rs->run(ore.data(), oim.data(), 0, D, [&](i64 j1, i64 k2, T c, T xr, T xi, T* yr, T* yi) {
+        i64 lane0, L;
+        chunk(k2, &lane0, &L);
+        tw_window(tw, *lv, c, j1, k2, lane0, L, xr, xi, yr, yi);
+      });  // rows j1 of s lanes k2, in place: rows k1
       for (i64 i = 0; i < n; ++i) { y[2 * i] = ore[i] * scale; y[2 * i + 1] = oim[i] * scale; }
     } else {
       std::vector<T> lin(2 * p), lout(2 * p);
       for (i64 k2 = 0; k2 < s; ++k2) {
-        for (i64 j1 = 0; j1 < p; ++j1) { lin[2 * j1] = ore[k2 + s * j1]; lin[2 * j1 + 1] = oim[k2 + s * j1]; }
+        i64 lane0, L;
+        chunk(k2, &lane0, &L);
+        for (i64 j1 = 0; j1 < p; ++j1)
+          tw_window(tw, *lv, (T)1, j1, k2, lane0, L, ore[k2 + s * j1], oim[k2 + s * j1], &lin[2 * j1], &lin[2 * j1 + 1]);
         hv->exec(lin.data(), lout.data());
         for (i64 k1 = 0; k1 < p; ++k1) {
           y[2 * (k2 + s * k1)] = lout[2 * k1] * scale;
@@ -1677,11 +1753,13 @@ struct SplitPlan : PlanBase {
   std::unique_ptr<HvdhPlan<T>> hv;
   std::vector<Stage<T>> stages;
   TwoLevel<T> tw;
+  std::unique_ptr<LaneTw<T>> lv;
   SplitPlan(i64 n_, int D_, T scale_) : D(D_), scale(scale_), tw(n_, D_) {
     n = n_;
     route = ORC_SPLIT;
     s = smooth_part(n);
     p = n / s;
+    lv.reset(new LaneTw<T>(n, s, D));
     hv.reset(new HvdhPlan<T>(p, D, (T)1, 0));
     stages = build_stages<T>(s, D, false);
   }
@@ -1692,12 +1770,8 @@ struct SplitPlan : PlanBase {
     for (i64 r = 0; r < s; ++r) {
       for (i64 j = 0; j < p; ++j) { xs[2 * j] = x[2 * (s * j + r)]; xs[2 * j + 1] = x[2 * (s * j + r) + 1]; }
       hv->exec(xs.data(), ys.data());
-      for (i64 k1 = 0; k1 < p; ++k1) {  // _split_twiddle! (src/composite.jl:240-272)
-        T wr, wi;
-        tw.at(r * k1, &wr, &wi);
-        are[p * r + k1] = ys[2 * k1] * wr - ys[2 * k1 + 1] * wi;
-        aim[p * r + k1] = ys[2 * k1] * wi + ys[2 * k1 + 1] * wr;
-      }
+      for (i64 k1 = 0; k1 < p; ++k1)  // _split_twiddle! (src/composite.jl:237-266)
+        tw_window(tw, *lv, (T)1, r, k1, 0, p, ys[2 * k1], ys[2 * k1 + 1], &are[p * r + k1], &aim[p * r + k1]);
     }
     const bool sw = run_chain(are.data(), aim.data(), bre.data(), bim.data(), stages, 0, stages.size(), s, 1, p, D, 1);
     const T* cre = sw ? bre.data() : are.data();
