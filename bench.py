@@ -148,35 +148,44 @@ def replica_reduce(ms, units, pg=None, device="cpu"):
 # reference arm: FFTJ's algorithm on the host cores (oracle restatement)
 
 def cpu_sample(steps_hint=1, max_seconds=20.0):
-    """Time the FFTJ-restated CPU plans (all host threads, threads inside each
-    transform as FFTJ runs them) on a bounded sample of the workload: `nb`
-    transforms of every part. Returns (GFLOP/s, cores, sample description)."""
+    """Time the FFTJ-restated CPU plans on all host threads on a bounded
+    sample of the workload: `nb` transforms of every part, the transforms of
+    a part spread over the threads, each worker with its own serial plan
+    (FFTJ's serial plan copies). Returns (GFLOP/s, cores, sample text)."""
+    from concurrent.futures import ThreadPoolExecutor
     from oracle import oracle as O
     O.build()
     nt = O.max_threads()
     rng = np.random.default_rng(1)
+    ex = ThreadPoolExecutor(nt)
     plans, xs = [], []
     for dt, n in PARTS:
         T = np.float32 if dt == "c32" else np.float64
-        plans.append(O.Plan1D(T, n, "fft", nthreads=nt))
+        plans.append(list(ex.map(lambda _: O.Plan1D(T, n, "fft", nthreads=1), range(nt))))
         xs.append(((rng.standard_normal(n) + 1j * rng.standard_normal(n)) / math.sqrt(2)).astype(
             np.complex64 if dt == "c32" else np.complex128))
-    for p, x in zip(plans, xs):  # warm plans
-        p(x)
+
+    def part(k, nb):
+        xb = np.broadcast_to(xs[k], (nb, xs[k].size)).copy()
+        per = [(w * nb // nt, (w + 1) * nb // nt) for w in range(nt)]
+        list(ex.map(lambda w: plans[k][w](xb[per[w][0]:per[w][1]]) if per[w][1] > per[w][0] else None, range(nt)))
+
+    for k in range(len(PARTS)):  # warm plans
+        part(k, nt)
     # size the sample: per-part transforms so the total stays within budget
     t0 = time.perf_counter()
-    for p, x in zip(plans, xs):
-        p(x)
-    one = time.perf_counter() - t0
-    nb = int(max(1, min(BATCH, max_seconds / max(one, 1e-6) / max(steps_hint, 1))))
+    for k in range(len(PARTS)):
+        part(k, nt)
+    one = (time.perf_counter() - t0) / nt
+    nb = int(max(nt, min(BATCH, max_seconds / max(one, 1e-6) / max(steps_hint, 1))))
     t0 = time.perf_counter()
-    for p, x in zip(plans, xs):
-        xb = np.broadcast_to(x, (nb, x.size)).copy()
-        p(xb)
+    for k in range(len(PARTS)):
+        part(k, nb)
     dt = time.perf_counter() - t0
+    ex.shutdown()
     fl = sum(flops(n, nb) for _, n in PARTS)
-    return fl / dt / 1e9, nt, "%d of %d transforms of each of the 6 parts (FFTJ-restated C++ plans, %d threads)" % (
-        nb, BATCH, nt)
+    return fl / dt / 1e9, nt, ("%d of %d transforms of each of the 6 parts (FFTJ-restated C++ plans, %d threads, "
+                               "a part's transforms spread over them on serial plans)" % (nb, BATCH, nt))
 
 
 def run_reference_mixed(args):
@@ -480,29 +489,38 @@ def uneven_config(items):
 
 
 def cpu_uneven(items, steps, warmup, stride=CPU_SAMPLE_STRIDE, nthreads=None):
-    """The FFTJ-restated CPU plans (the oracle: FFTJ's algorithms in C++, all
-    host threads inside each transform as FFTJ runs them, transforms one after
-    another as FFTJ's callers loop) on a fixed sample of the same item list:
-    every `stride`-th item. Returns (GFLOP/s, threads, sample text)."""
+    """The FFTJ-restated CPU plans (the oracle: FFTJ's algorithms in C++) on a
+    fixed sample of the same item list, every `stride`-th item, on all host
+    threads: a transform whose work exceeds one thread's share of the step
+    (total flops / threads) runs with every thread inside it, as FFTJ's
+    threaded plans run it; the rest run concurrently, each worker thread with
+    its own serial plans (FFTJ's serial plan copies) for the lengths dealt to
+    it by cost, largest first to the least loaded. Returns (GFLOP/s,
+    threads, sample text)."""
     from concurrent.futures import ThreadPoolExecutor
     from oracle import oracle as O
     O.build()
     nt = nthreads or O.max_threads()
     sample = items[::stride]
 
-    def mk(it):
+    def mk(it, threads):
         kind, dt, n = it
         if kind == "c2c":
-            return O.Plan1D(dt, n, "fft", nthreads=nt)
+            return O.Plan1D(dt, n, "fft", nthreads=threads)
         if kind == "r2c":
-            return O.PlanReal(dt, n, "rfft", nthreads=nt)
-        return O.PlanND(dt, n, "rfft", nthreads=nt)
+            return O.PlanReal(dt, n, "rfft", nthreads=threads)
+        return O.PlanND(dt, n, "rfft", nthreads=threads)
 
-    keys = sorted({(k, np.dtype(d).name, n) for k, d, n in sample}, key=str)
-    with ThreadPoolExecutor(16) as ex:
-        made = dict(zip(keys, ex.map(lambda k: mk((k[0], np.dtype(k[1]).type, k[2])), keys)))
+    share = sum(uneven_flops(k, n) for k, _, n in sample) / nt
+
+    def is_big(kind, n):
+        return uneven_flops(kind, n) > share
+
+    def key(it):
+        return (it[0], np.dtype(it[1]).name, it[2])
+
     rng = np.random.default_rng(0xF17)
-    work = []
+    xs = []
     for kind, dt, n in sample:
         if kind == "c2c":
             x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / math.sqrt(2)
@@ -511,21 +529,53 @@ def cpu_uneven(items, steps, warmup, stride=CPU_SAMPLE_STRIDE, nthreads=None):
             x = rng.standard_normal(n).astype(dt)
         else:
             x = rng.standard_normal(tuple(reversed(n))).astype(dt)
-        work.append((made[(kind, np.dtype(dt).name, n)], x))
+        xs.append(x)
+    big = [i for i, it in enumerate(sample) if is_big(it[0], it[2])]
+    small = [i for i, it in enumerate(sample) if not is_big(it[0], it[2])]
+    # the small lengths dealt to the workers, largest cost first, each to the
+    # least loaded worker; a worker owns every item of its lengths
+    cost = {}
+    for i in small:
+        k = key(sample[i])
+        cost[k] = cost.get(k, 0.0) + uneven_flops(sample[i][0], sample[i][2])
+    load, owner = [0.0] * nt, {}
+    for k in sorted(cost, key=lambda k: (-cost[k], str(k))):
+        w = int(np.argmin(load))
+        owner[k] = w
+        load[w] += cost[k]
+    lanes = [[i for i in small if owner[key(sample[i])] == w] for w in range(nt)]
+    ex = ThreadPoolExecutor(max(nt, 16))
+    big_keys = sorted({key(sample[i]) for i in big}, key=str)
+    big_plans = dict(zip(big_keys, ex.map(lambda k: mk((k[0], np.dtype(k[1]).type, k[2]), nt), big_keys)))
+
+    def lane_plans(w):
+        ks = sorted({key(sample[i]) for i in lanes[w]}, key=str)
+        return {k: mk((k[0], np.dtype(k[1]).type, k[2]), 1) for k in ks}
+
+    serial = list(ex.map(lane_plans, range(nt)))
     fl = sum(uneven_flops(k, n) for k, _, n in sample)
+
+    def run_lane(w):
+        ps = serial[w]
+        for i in lanes[w]:
+            ps[key(sample[i])](xs[i])
 
     def one():
         t0 = time.perf_counter()
-        for p, x in work:
-            p(x)
+        for i in big:
+            big_plans[key(sample[i])](xs[i])
+        list(ex.map(run_lane, range(nt)))
         return time.perf_counter() - t0
 
     for _ in range(warmup):
         one()
     ts = [one() for _ in range(steps)]
+    ex.shutdown()
     desc = ("every %dth item of the same list (%d transforms, %.2f GFLOP per step incl. the 256^3 rfft): "
-            "FFTJ-restated C++ plans, %d threads inside each transform, transforms in sequence; %d timed steps"
-            % (stride, len(sample), fl / 1e9, nt, steps))
+            "FFTJ-restated C++ plans on %d threads -- %d transform(s) above one thread's share of the step with "
+            "every thread inside, then the other %d concurrently on serial plans, one worker per thread, "
+            "dealt by cost; "
+            "%d timed steps" % (stride, len(sample), fl / 1e9, nt, len(big), len(small), steps))
     return fl * len(ts) / sum(ts) / 1e9, nt, desc
 
 

@@ -121,8 +121,14 @@ def test_nd_reference_shapes(fftj, golden, orc, T):
         rref = golden["ndr_y_" + key[5:]]
         Y = fftj.rfft(dev(xr, T))
         assert tuple(Y.shape) == rref.shape and rel_l2(host(Y), rref) <= tol, dims
-        assert rel_l2(host(fftj.irfft(dev(rref, T), dims[0])), xr) <= tol, dims
-        assert rel_l2(host(fftj.brfft(dev(rref, T), dims[0])), n * xr) <= tol, dims
+        # the oracle's real N-d plans (batched real edge where FFTJ batches it)
+        assert rel_l2(host(Y), orc.PlanND(T, dims, "rfft")(xr)) <= tol, dims
+        xi = host(fftj.irfft(dev(rref, T), dims[0]))
+        assert rel_l2(xi, xr) <= tol, dims
+        assert rel_l2(xi, orc.PlanND(T, dims, "irfft")(rref)) <= tol, dims
+        xb = host(fftj.brfft(dev(rref, T), dims[0]))
+        assert rel_l2(xb, n * xr) <= tol, dims
+        assert rel_l2(xb, orc.PlanND(T, dims, "brfft")(rref)) <= tol, dims
 
 
 @pytest.mark.parametrize("T", T_LIST)
@@ -140,7 +146,10 @@ def test_nd_nonsmooth_dims(fftj, orc, T, shape):
     xr = rng.standard_normal(shape)
     Y = fftj.rfft(dev(xr, T))
     assert rel_l2(host(Y), np.fft.rfftn(xr)) <= tol, shape
-    assert rel_l2(host(fftj.irfft(Y, shape[-1])), xr) <= tol, shape
+    assert rel_l2(host(Y), orc.PlanND(T, list(reversed(shape)), "rfft")(xr)) <= tol, shape
+    xi = host(fftj.irfft(Y, shape[-1]))
+    assert rel_l2(xi, xr) <= tol, shape
+    assert rel_l2(xi, orc.PlanND(T, list(reversed(shape)), "irfft")(host(Y))) <= tol, shape
 
 
 # --------------------------------------------------------------------------
