@@ -2289,6 +2289,7 @@ int orc_plan_nd_batched(void* p) {
 }
 
 void orc_dft_f64(int64_t n, const double* x, double* y, int sign) { dft_f64(n, x, y, sign); }
+double orc_vexp(int dtype, double x) { return dtype == 0 ? (double)vexp<float>((float)x) : vexp<double>(x); }
 
 int orc_factor_radices(int64_t n, int64_t* a, int64_t* primes, int64_t* counts, int64_t cap) {
   Fac f = factor_radices(n);

@@ -61,6 +61,9 @@ void* orc_plan_irfft_nd(int dtype, int rank, const int64_t* dims, int normalized
 // 1 when the plan's dim-1 edge runs batched (pencils as lanes): the complex
 // dim-1 chain without the small-stride layout, or the batched real edge.
 int orc_plan_nd_batched(void* plan);
+// FFTJ's polynomial exp (_vexp) that seeds the HvdH recurrences, in F32
+// (dtype 0, x rounded to F32 first) or F64.
+double orc_vexp(int dtype, double x);
 int orc_execute_rfft_nd(void* plan, const void* x, void* y);
 int orc_execute_irfft_nd(void* plan, const void* x, void* y);
 

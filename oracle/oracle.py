@@ -59,6 +59,8 @@ def lib():
         L.orc_execute_rfft_nd.argtypes = [vp, vp, vp]
         L.orc_execute_irfft_nd.argtypes = [vp, vp, vp]
         L.orc_plan_nd_batched.argtypes = [vp]
+        L.orc_vexp.restype = ctypes.c_double
+        L.orc_vexp.argtypes = [i32, ctypes.c_double]
         L.orc_dft_f64.argtypes = [i64, vp, vp, i32]
         L.orc_plan_hvdh.restype = vp
         L.orc_plan_hvdh.argtypes = [i32, i64, i32, i32, i32]
@@ -259,6 +261,12 @@ def dft_f64(x, sign=-1):
 
 def set_vector_bits(bits):
     lib().orc_set_vector_bits(int(bits))
+
+
+def vexp(dtype, x):
+    """FFTJ's polynomial exp (_vexp, src/hvdh.jl:99-114) as the oracle
+    restates it, in the given float type."""
+    return lib().orc_vexp(_dt(dtype), float(x))
 
 
 def max_threads():

@@ -336,3 +336,28 @@ def test_batched_dim1_edges(orc):
             assert rel_l2(orc.PlanND(T, dims, "brfft")(ref), n * x) <= parity_tol(T, n), (T, dims)
             xc = x + 1j * rng.standard_normal(shape)
             assert rel_l2(orc.PlanND(T, dims, "fft")(xc), np.fft.fftn(xc)) <= parity_tol(T, n), (T, dims)
+
+
+def test_vexp_and_hvdh_recurrences(orc):
+    """FFTJ's HvdH seeds its Gaussian recurrences with its own polynomial exp
+    (_vexp, src/hvdh.jl:99-114: Cody-Waite reduction, 14 / 8 Taylor terms):
+    the restated one stays within 2 ulp of the correctly rounded exp over the
+    arguments the seeds see, and the restated HvdH (band columns re-seeded
+    every 4, spread states every 8 vectors) stays within FFTJ's 50 eps."""
+    from conftest import rel_l2
+    from oracle import oracle as O
+    import math
+    for T in T_LIST:
+        xs = np.linspace(-10.0, 10.0, 2001).astype(T)
+        for x in xs:
+            e = O.vexp(T, float(x))
+            ref = math.exp(float(x))
+            ulp = float(np.spacing(T(ref)))
+            assert abs(e - ref) <= 2 * ulp, (T, float(x), e, ref)
+    rng = np.random.default_rng(0xE1)
+    for T in T_LIST:
+        ct = np.complex64 if T == np.float32 else np.complex128
+        for n in (1001, 16385, 65537):
+            x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(ct)
+            y = orc.PlanDirect(T, n, "hvdh")(x)
+            assert rel_l2(y, np.fft.fft(x.astype(np.complex128))) <= 50 * EPS[T], (T, n)
