@@ -9,7 +9,7 @@
 //              concurrently), replayed by one cudaGraphLaunch;
 //  PERSISTENT  one persistent kernel (one CTA per resident slot) that drains
 //              a device work queue of (op, tile range) items, captured with
-//              the queue reset as a CUDA graph. Items are queued level by
+//              a small kernel that resets the queue as a CUDA graph. Items are queued level by
 //              level (every plan's first op, then every plan's second op,
 //              ...); an item of op k of a plan waits until all tiles of op
 //              k-1 of that plan are done. A CTA claims items in queue order
@@ -148,6 +148,16 @@ __device__ __forceinline__ void group_elementwise(const GroupOp& op, uint32_t t0
       break;
     default: break;
   }
+}
+
+// Zeroes the queue head, the error word, the failed op and every done
+// counter before an execution. A kernel rather than memset nodes: memsets
+// can be queued on a copy engine behind multi-gigabyte host copies of other
+// streams, holding the execution back until those copies finish.
+__global__ void k_group_reset(uint32_t* ctl, int nops) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 3) ctl[i] = 0;
+  if (i < nops) ctl[kCtlWords + i] = 0;
 }
 
 __global__ void __launch_bounds__(kGroupThreads, 2)
@@ -386,8 +396,8 @@ int build_persistent(fftj_group_s* g) {
     return gfail(FFTJ_ERR_CUDA, "persistent group: upload failed");
   if (cudaStreamBeginCapture(g->cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     return gfail(FFTJ_ERR_CUDA, "persistent group: graph capture failed");
-  cudaMemsetAsync(g->d_ctl, 0, 3 * sizeof(uint32_t), g->cap);
-  cudaMemsetAsync(g->d_ctl + kCtlWords, 0, (size_t)g->nops * sizeof(uint32_t), g->cap);
+  const int nreset = std::max(g->nops, 3);
+  k_group_reset<<<(nreset + 255) / 256, 256, 0, g->cap>>>(g->d_ctl, g->nops);
   k_group<<<g->ctas, kGroupThreads, g->smem, g->cap>>>(g->d_ops, g->d_items, g->nitems, g->d_ctl);
   const cudaError_t le = cudaGetLastError();
   if (cudaStreamEndCapture(g->cap, &g->graph) != cudaSuccess || le != cudaSuccess ||
@@ -512,7 +522,7 @@ int fftj_group_get_info(fftj_group g, fftj_group_info_t* info) {
   info->ctas = g->ctas;
   info->smem_bytes = (int)g->smem;
   info->branches = g->branches;
-  info->kernels = g->mode == FFTJ_GROUP_PERSISTENT ? 1 : g->nops;
+  info->kernels = g->mode == FFTJ_GROUP_PERSISTENT ? 2 : g->nops;  // persistent: the reset and the queue kernel
   return FFTJ_OK;
 }
 

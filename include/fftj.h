@@ -317,9 +317,10 @@ int fftj_execute_noalloc_c2c(int dtype, int64_t n, int64_t batch, int dir, doubl
  *                          with the plans on parallel branches;
  *   FFTJ_GROUP_PERSISTENT  one persistent kernel draining a device queue of
  *                          (op, tile range) items with bounded dependency
- *                          waits, captured with its queue reset as a CUDA
- *                          graph. Every pass must use <= 256 threads per CTA
- *                          (plan with opts.threads_max = 256).
+ *                          waits, captured with a small queue-reset kernel
+ *                          as a CUDA graph (2 kernels per execution). Every
+ *                          pass must use <= 256 threads per CTA (plan with
+ *                          opts.threads_max = 256).
  * Plans must outlive the group and must not run elsewhere while it runs.
  */
 typedef struct fftj_group_s* fftj_group;
