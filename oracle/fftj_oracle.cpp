@@ -925,9 +925,39 @@ struct ResamplePlan : PlanBase {
     bool sw = run_chain(are, aim, p->bre.data(), p->bim.data(), p->stages, 0, p->stages.size(), m, 1, 1, D, 1);
     const T* gre = sw ? p->bre.data() : are;
     const T* gim = sw ? p->bim.data() : aim;
-    // _interp! (src/resample.jl:392-424)
-    i64 w = parts.w;
-    for (i64 k = 0; k < n; ++k) {
+    // _interp! (src/resample.jl:392-424): blocks of V/2 outputs whose
+    // windows lie inside the grid sum as _interp_block! does, the others
+    // tap by tap (the ordered sum of a vector)
+    const i64 w = parts.w, V = pick_width<T>();
+    const i64 sl = std::min(w, V);
+    const bool blockable = V > 1 && (w % V == 0 || V % w == 0) && (sl & (sl - 1)) == 0;  // _blockable
+    const i64 Bk = blockable ? V / 2 : 0;
+    std::vector<T> pr(w), cs(sl);
+    // _chunksum to sl lanes (chunks added left to right), then the tree
+    // halving of _tree_reduce_code: lane j += lane j + L/2
+    auto block_dot = [&](const T* g, i64 lk, const T* wv) {
+      for (i64 i = 0; i < w; ++i) pr[i] = g[lk + i] * wv[i];
+      for (i64 j = 0; j < sl; ++j) {
+        T c = pr[j];
+        for (i64 ch = 1; ch < w / sl; ++ch) c = c + pr[ch * sl + j];
+        cs[j] = c;
+      }
+      for (i64 L = sl; L > 1; L /= 2)
+        for (i64 j = 0; j < L / 2; ++j) cs[j] = cs[j] + cs[j + L / 2];
+      return cs[0];
+    };
+    i64 k = 0;
+    while (k < n) {
+      if (Bk > 0 && k + Bk <= n && parts.l0[k] >= 0 && parts.l0[k + Bk - 1] + w <= m) {
+        for (i64 j = 0; j < Bk; ++j) {
+          const T* wv = &parts.wt[(k + j) * w];
+          const T re = block_dot(gre, parts.l0[k + j], wv);
+          const T im = block_dot(gim, parts.l0[k + j], wv);
+          y[2 * (k + j)] = re; y[2 * (k + j) + 1] = im;
+        }
+        k += Bk;
+        continue;
+      }
       i64 lk = parts.l0[k];
       const T* wv = &parts.wt[k * w];
       T re = 0, im = 0;
@@ -939,6 +969,7 @@ struct ResamplePlan : PlanBase {
         im += wv[i] * gim[l];
       }
       y[2 * k] = re; y[2 * k + 1] = im;
+      ++k;
     }
   }
   void info(std::vector<i64>& v) override {
