@@ -853,14 +853,91 @@ static inline double es_(double z, double beta) {  // src/resample.jl:55
   return std::fabs(z) >= 1 ? 0.0 : std::exp(beta * (std::sqrt(1 - z * z) - 1));
 }
 
-// Plan-independent resampling parts (src/resample.jl:202-256), table weights.
+// _fit_weights_d (src/resample.jl:137-169): degree-d Chebyshev interpolants
+// of every tap's weight on each of P pieces of the offset, converted to
+// monomials in the local variable t in [-1, 1] and rounded to T; returns the
+// largest error of the rounded polynomials on 4d + 4 points.
+template <typename T>
+static double fit_weights_d(double beta, i64 w, i64 P, int d, std::vector<T>& C) {
+  const i64 h = w / 2;
+  std::vector<double> tj(d + 1), fj(d + 1), mono(d + 1), Tkm(d + 1), Tk(d + 1), Tn(d + 1);
+  for (int j = 0; j <= d; ++j) tj[j] = cospi_((j + 0.5) / (double)(d + 1));
+  C.assign((size_t)(P * (d + 1) * w), (T)0);
+  double err = 0;
+  for (i64 p = 0; p < P; ++p)
+    for (i64 i = 0; i < w; ++i) {
+      auto f = [&](double t) { return es_((((double)p + (t + 1) / 2) / (double)P + h - 1 - i) / (double)h, beta); };
+      for (int j = 0; j <= d; ++j) fj[j] = f(tj[j]);
+      std::fill(mono.begin(), mono.end(), 0.0);
+      std::fill(Tkm.begin(), Tkm.end(), 0.0);
+      std::fill(Tk.begin(), Tk.end(), 0.0);
+      Tkm[0] = 1;  // T_0, T_1 in monomials
+      Tk[1] = 1;
+      for (int k = 0; k <= d; ++k) {
+        double a = 0;
+        for (int j = 0; j <= d; ++j) {
+          const double term = fj[j] * cospi_((double)k * (j + 0.5) / (double)(d + 1));
+          a = j == 0 ? term : a + term;
+        }
+        a = a * 2 / (double)(d + 1);
+        if (k == 0) a /= 2;
+        const std::vector<double>& Tc = k == 0 ? Tkm : Tk;
+        for (int c = 0; c <= d; ++c) mono[c] = mono[c] + a * Tc[c];
+        if (k >= 1) {  // T_{k+1} = 2t T_k - T_{k-1}
+          for (int c = 0; c <= d; ++c) Tn[c] = -Tkm[c];
+          for (int c = 1; c <= d; ++c) Tn[c] = Tn[c] + 2 * Tk[c - 1];
+          Tkm.swap(Tk);
+          Tk.swap(Tn);
+        }
+      }
+      for (int c = 0; c <= d; ++c) {
+        const T v = (T)mono[c];
+        C[(size_t)((p * (d + 1) + c) * w + i)] = v;
+        mono[c] = (double)v;
+      }
+      const int ns = 4 * d + 4;
+      for (int q = 0; q < ns; ++q) {
+        const double t = -1.0 + 2.0 * (double)q / (double)(ns - 1);
+        double ev = mono[d];  // evalpoly (Horner)
+        for (int c = d - 1; c >= 0; --c) ev = std::fma(t, ev, mono[c]);
+        err = std::max(err, std::fabs(ev - f(t)));
+      }
+    }
+  return err;
+}
+// _fit_weights (src/resample.jl:126-135): the degree grows until the fit
+// error is <= tolw or stops halving
+template <typename T>
+static int fit_weights(double beta, i64 w, i64 P, double tolw, std::vector<T>& C) {
+  std::vector<T> prev, cur;
+  double preverr = fit_weights_d<T>(beta, w, P, 1, prev);
+  for (int d = 2; d <= 30; ++d) {
+    const double err = fit_weights_d<T>(beta, w, P, d, cur);
+    if (err <= tolw) { C.swap(cur); return d; }
+    if (err > preverr / 2) { C.swap(prev); return d - 1; }
+    prev.swap(cur);
+    preverr = err;
+  }
+  C.swap(prev);
+  return 30;
+}
+
+static const i64 RS_TABLE_MAX = 1 << 21;  // _RS_TABLE_MAX (src/resample.jl:173)
+
+// Plan-independent resampling parts (src/resample.jl:202-256): a weight
+// table, or -- for a 1-D plan whose table would exceed RS_TABLE_MAX --
+// piecewise polynomial weights (WPoly, src/resample.jl:62-118).
 template <typename T>
 struct RsParts {
   i64 n, m, w, h;
   double beta;
   std::vector<T> corr, wt;
   std::vector<int32_t> l0;
-  RsParts(i64 n_, int D, T scale, i64 m_ = 0) : n(n_) {
+  bool poly = false;
+  int deg = 0;
+  i64 P = 0;
+  std::vector<T> C;  // C[(p (deg + 1) + c) w + i]: coefficient c of tap i, piece p
+  RsParts(i64 n_, int D, T scale, i64 m_ = 0, bool allow_poly = false) : n(n_) {
     (void)D;
     const double epsT = sizeof(T) >= 8 ? 2.220446049250313e-16 : 1.1920928955078125e-07;
     double tol = 10 * epsT;
@@ -884,15 +961,40 @@ struct RsParts {
       }
       corr[j] = (T)((double)scale / (w * Phi));
     }
-    wt.resize(n * w);
     l0.resize(n);
     for (i64 k = 0; k < n; ++k) {
       __int128 km = (__int128)k * m;
-      i64 q = (i64)(km / n), r = (i64)(km % n);
-      l0[k] = (int32_t)(q - h + 1);
+      l0[k] = (int32_t)((i64)(km / n) - h + 1);
+    }
+    poly = allow_poly && n * w * (i64)sizeof(T) > RS_TABLE_MAX;
+    if (poly) {
+      P = sizeof(T) >= 8 ? 32 : 64;
+      deg = fit_weights<T>(beta, w, P, tol / 16, C);
+      return;
+    }
+    wt.resize(n * w);
+    for (i64 k = 0; k < n; ++k) {
+      __int128 km = (__int128)k * m;
+      i64 r = (i64)(km % n);
       double delta = (double)r / n;
       for (i64 i = 0; i < w; ++i) wt[k * w + i] = (T)es_((delta + h - 1 - i) / h, beta);
     }
+  }
+  // the w weights of output k (_wget: a table row, or Horner across the
+  // taps in t = 2 (s - piece) - 1, s = (k m mod n) P / n)
+  const T* weights(i64 k, T* buf) const {
+    if (!poly) return &wt[k * w];
+    const i64 r = (i64)(((__int128)k * m) % n);
+    const double sp = (double)r * ((double)P / (double)n);
+    const i64 pc = std::min((i64)sp, P - 1);
+    const T t = (T)(2 * (sp - (double)pc) - 1);
+    const size_t base = (size_t)(pc * (deg + 1));
+    for (i64 i = 0; i < w; ++i) {
+      T v = C[(base + deg) * w + i];
+      for (int c = deg - 1; c >= 0; --c) v = std::fma(v, t, C[(base + c) * w + i]);
+      buf[i] = v;
+    }
+    return buf;
   }
 };
 
@@ -903,7 +1005,7 @@ struct ResamplePlan : PlanBase {
   T scale;
   RsParts<T> parts;
   std::unique_ptr<FFTPlan<T>> p;
-  ResamplePlan(i64 n_, int D_, T scale_) : D(D_), scale(scale_), parts(n_, D_, scale_) {
+  ResamplePlan(i64 n_, int D_, T scale_) : D(D_), scale(scale_), parts(n_, D_, scale_, 0, true) {
     n = n_;
     route = ORC_RESAMPLE;
     p.reset(new FFTPlan<T>(parts.m, D, (T)1, 1));
@@ -932,7 +1034,7 @@ struct ResamplePlan : PlanBase {
     const i64 sl = std::min(w, V);
     const bool blockable = V > 1 && (w % V == 0 || V % w == 0) && (sl & (sl - 1)) == 0;  // _blockable
     const i64 Bk = blockable ? V / 2 : 0;
-    std::vector<T> pr(w), cs(sl);
+    std::vector<T> pr(w), cs(sl), wbuf(w);
     // _chunksum to sl lanes (chunks added left to right), then the tree
     // halving of _tree_reduce_code: lane j += lane j + L/2
     auto block_dot = [&](const T* g, i64 lk, const T* wv) {
@@ -946,11 +1048,19 @@ struct ResamplePlan : PlanBase {
         for (i64 j = 0; j < L / 2; ++j) cs[j] = cs[j] + cs[j + L / 2];
       return cs[0];
     };
+    // _wblock_ok: the table's windows, or (polynomial weights) a bound from
+    // the block's first grid row and floor((B - 1) m / n) + 1 rows on
+    auto block_ok = [&](i64 k) {
+      if (!parts.poly) return parts.l0[k] >= 0 && parts.l0[k + Bk - 1] + w <= m;
+      const i64 q = (i64)(((__int128)k * m) / n);
+      const i64 g = (i64)(((__int128)(Bk - 1) * m) / n);
+      return q - parts.h + 1 >= 0 && q + g + 1 - parts.h + 1 + w <= m;
+    };
     i64 k = 0;
     while (k < n) {
-      if (Bk > 0 && k + Bk <= n && parts.l0[k] >= 0 && parts.l0[k + Bk - 1] + w <= m) {
+      if (Bk > 0 && k + Bk <= n && block_ok(k)) {
         for (i64 j = 0; j < Bk; ++j) {
-          const T* wv = &parts.wt[(k + j) * w];
+          const T* wv = parts.weights(k + j, wbuf.data());
           const T re = block_dot(gre, parts.l0[k + j], wv);
           const T im = block_dot(gim, parts.l0[k + j], wv);
           y[2 * (k + j)] = re; y[2 * (k + j) + 1] = im;
@@ -959,7 +1069,7 @@ struct ResamplePlan : PlanBase {
         continue;
       }
       i64 lk = parts.l0[k];
-      const T* wv = &parts.wt[k * w];
+      const T* wv = parts.weights(k, wbuf.data());
       T re = 0, im = 0;
       for (i64 i = 0; i < w; ++i) {
         i64 l = lk + i;
@@ -972,8 +1082,9 @@ struct ResamplePlan : PlanBase {
       ++k;
     }
   }
-  void info(std::vector<i64>& v) override {
+  void info(std::vector<i64>& v) override {  // route, n, m, w, polynomial weight degree (0: table)
     v.push_back(route); v.push_back(n); v.push_back(parts.m); v.push_back(parts.w);
+    v.push_back(parts.poly ? parts.deg : 0);
   }
 };
 

@@ -361,3 +361,21 @@ def test_vexp_and_hvdh_recurrences(orc):
             x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(ct)
             y = orc.PlanDirect(T, n, "hvdh")(x)
             assert rel_l2(y, np.fft.fft(x.astype(np.complex128))) <= 50 * EPS[T], (T, n)
+
+
+def test_resample_polynomial_weights(orc):
+    """A 1-D ResamplePlan whose weight table would exceed _RS_TABLE_MAX
+    (2 MiB: n w sizeof(T)) evaluates Chebyshev-fitted piecewise polynomials
+    instead (src/resample.jl:123-169, 229-250): Float32 8 x 10007 = 80056
+    (w = 8, 2.6 MB) routes to ResamplePlan with polynomial weights, 60002 (1.9
+    MB) keeps the table; both within FFTJ's 50 eps of FP64."""
+    from conftest import rel_l2
+    rng = np.random.default_rng(0x9017)
+    for n, poly in ((80056, True), (60002, False)):
+        p = orc.Plan1D(np.float32, n, "fft")
+        route, n_, m, w, deg = p.info()[:5]
+        assert p.route == "ResamplePlan" and w == 8 and (deg > 0) == poly, (n, p.info())
+        x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+        ref = np.fft.fft(x.astype(np.complex128))
+        assert rel_l2(p(x), ref) <= 50 * EPS[np.float32], n
+        assert rel_l2(orc.Plan1D(np.float32, n, "ifft")(ref), x) <= 50 * EPS[np.float32], n
